@@ -1,0 +1,451 @@
+"""Benchmark of the GAS hot path on the scale-22 workload.
+
+Workload (one "step"): SSSP from 8 sources and CC on an R-MAT graph of scale
+22 (4,194,304 vertices, edge factor 16, (a,b,c,d) = (0.57,0.19,0.19,0.05),
+seed 2, symmetrised, self loops and duplicates removed); SSSP weights
+uniform in [1,64] (seed 3, both directions equal); sources drawn uniformly
+from the largest component (seed 2); CC on the same graph plus 4,096
+disjoint 32x32 4-neighbour grid islands.  Synthetic data: the reference's
+real-world datasets are not available.
+
+Metric: GTEPS with the reference's definition (sssp.cu:202-211): for every
+run, the sum of out-degrees of the vertices it reached, divided by time
+(for CC every vertex is reached, so a run counts all its edges).
+
+  value  -- device-resident: graph and initial vertex states already in HBM,
+            timed with CUDA events on the engine's stream.
+  e2e    -- through the public Python API with pinned host buffers: each
+            run uploads its initial vertex data and downloads its result
+            inside the timed region.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SCALE = 22
+EDGE_FACTOR = 16
+RMAT_ABC = (0.57, 0.19, 0.19)
+GRAPH_SEED, WEIGHT_SEED, SOURCE_SEED = 2, 3, 2
+N_SOURCES = 8
+N_ISLANDS, ISLAND_SIDE = 4096, 32
+METRIC = "GTEPS (SSSP x8 + CC, R-MAT scale 22)"
+MAX_ITERS = 20000  # far above any run of this workload; bounds a device loop
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_workload(scale):
+    from graphreduce_gb300.graph import EdgeList
+    t = time.time()
+    base = EdgeList.rmat(scale, EDGE_FACTOR, *RMAT_ABC, seed=GRAPH_SEED, symmetrize=True)
+    ssp = base.with_uniform_weights(1, 64, WEIGHT_SEED)
+    sources = ssp.sample_sources(N_SOURCES, SOURCE_SEED)
+    ccg = base.with_grid_islands(N_ISLANDS, ISLAND_SIDE)
+    log(f"workload: scale {scale}: V={ssp.nV} E={ssp.nE}; CC graph V={ccg.nV} E={ccg.nE}; "
+        f"generated in {time.time() - t:.1f}s")
+    return ssp, sources, ccg
+
+
+def edges_visited(el_outdeg, vd, unreached):
+    return int(el_outdeg[vd != unreached].sum(dtype=np.int64))
+
+
+def config_dict(scale, extra=None):
+    d = {"workload": f"sssp8+cc rmat-s{scale}-ef{EDGE_FACTOR}-sym+{N_ISLANDS}x{ISLAND_SIDE}^2-islands",
+         "graph": {"scale": scale, "edge_factor": EDGE_FACTOR, "abcd": [*RMAT_ABC, 0.05],
+                   "seed": GRAPH_SEED, "symmetrized": True, "weights": "uniform[1,64] seed 3",
+                   "sources": f"{N_SOURCES} uniform from the largest component, seed {SOURCE_SEED}",
+                   "cc_islands": f"{N_ISLANDS} x {ISLAND_SIDE}x{ISLAND_SIDE} grids"},
+         "l2": "inputs larger than L2 (CSR+CSC+weights > 2 GB vs 129 MB L2)",
+         "parallelism": "replicas"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.file:
+            return None
+        try:
+            rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+            os.unlink(self.file.name)
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    import torch
+
+    import graphreduce_gb300 as gg
+    from graphreduce_gb300.engine import SSSP_GATHER_ZERO, initial_vertex_data
+
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    gg.load()
+
+    ssp, sources, ccg = make_workload(args.scale)
+    out_sssp = ssp.out_degree()
+    out_cc = ccg.out_degree()
+
+    t = time.time()
+    e_s = gg.GASEngineGPU("sssp")
+    vd_s = initial_vertex_data("sssp", ssp.nV, int(sources[0]))
+    e_s.setGraph(ssp.nV, vd_s, ssp.nE, ssp.weights, ssp.src, ssp.dst, sp)
+    e_c = gg.GASEngineGPU("cc")
+    vd_c = initial_vertex_data("cc", ccg.nV)
+    e_c.setGraph(ccg.nV, vd_c, ccg.nE, None, ccg.src, ccg.dst, sp)
+    log(f"setGraph (host CSR/CSC build + upload) {time.time() - t:.1f}s")
+
+    # initial vertex states resident in HBM (value) and in pinned host memory (e2e)
+    init_s = [torch.from_numpy(initial_vertex_data("sssp", ssp.nV, int(s))) for s in sources]
+    init_c = torch.from_numpy(initial_vertex_data("cc", ccg.nV))
+    dev_s = [x.to(dev) for x in init_s]
+    dev_c = init_c.to(dev)
+    pin_s = [x.pin_memory() for x in init_s]
+    pin_c = init_c.pin_memory()
+    res_s = [torch.empty(ssp.nV, dtype=torch.int32).pin_memory() for _ in sources]
+    res_c = torch.empty(ccg.nV, dtype=torch.int32).pin_memory()
+    torch.cuda.synchronize()
+
+    launches = [0]
+    iters = {"sssp": [], "cc": 0}
+
+    def one_step(e2e):
+        launches[0] = 0
+        iters["sssp"] = []
+        for k in range(len(sources)):
+            e_s.upload_vertex_data_ptr(pin_s[k].data_ptr() if e2e else dev_s[k].data_ptr(), sp)
+            e_s.setActive(0, ssp.nV, sp)
+            st = e_s.run_schedule(args.schedule, max_iterations=MAX_ITERS, stream=sp)
+            iters["sssp"].append(st.iterations)
+            launches[0] += st.kernel_launches + 1
+            if e2e:
+                e_s.download_vertex_data_ptr(res_s[k].data_ptr(), sp)
+        e_c.upload_vertex_data_ptr(pin_c.data_ptr() if e2e else dev_c.data_ptr(), sp)
+        e_c.setActive(0, ccg.nV, sp)
+        st = e_c.run_schedule(args.schedule, max_iterations=MAX_ITERS, stream=sp)
+        iters["cc"] = st.iterations
+        launches[0] += st.kernel_launches + 1
+        if e2e:
+            e_c.download_vertex_data_ptr(res_c.data_ptr(), sp)
+
+    # correctness of this exact workload + units per step
+    one_step(e2e=True)
+    torch.cuda.synchronize()
+    ev_units = 0
+    for k in range(len(sources)):
+        ev_units += edges_visited(out_sssp, res_s[k].numpy(), SSSP_GATHER_ZERO)
+    ev_units += edges_visited(out_cc, res_c.numpy(), -12345)  # every CC vertex is reached
+    first_sssp = res_s[0].numpy().copy()
+
+    def timed(e2e, steps, warmup):
+        for _ in range(warmup):
+            one_step(e2e)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        start.record(stream)
+        for _ in range(steps):
+            one_step(e2e)
+        end.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        ms = start.elapsed_time(end)
+        if world > 1:
+            tt = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            torch.distributed.barrier()
+            ms = float(tt.item())
+        return ms / steps, wall / steps
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms_step, _ = timed(False, args.steps, args.warmup)
+    clocks = clk.summary()
+    ms_e2e, _ = timed(True, max(1, args.steps), 1)
+    launches_per_step = launches[0]
+
+    value = world * ev_units / (ms_step * 1e-3) / 1e9
+    e2e = world * ev_units / (ms_e2e * 1e-3) / 1e9
+    h2d = (len(sources) * ssp.nV + ccg.nV) * 4
+    d2h = h2d
+
+    # per-algorithm split and the dominant kernel's roofline (untimed pass)
+    split = per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources,
+                           args.schedule, sp, stream)
+    roof = gather_roofline(e_s, dev_s[0], ssp, sp, stream)
+    peak, peak_kind = measured_peaks()
+    roof["peak"] = peak
+    roof["frac"] = roof["achieved"] / peak
+    roof["peak_source"] = peak_kind
+
+    result = {
+        "metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded R-MAT + grid islands; reference datasets unavailable)",
+        "config": config_dict(args.scale, {"schedule": args.schedule,
+                                           "edges_visited_per_step": ev_units,
+                                           "iterations": {"sssp": iters["sssp"],
+                                                          "cc": iters["cc"]}}),
+        "e2e": {"value": round(e2e, 4), "unit": "GTEPS", "ms_per_step": round(ms_e2e, 3),
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": roof,
+        "algos": split,
+        "clocks": clocks,
+    }
+    return result, (ssp, sources, out_sssp, first_sssp)
+
+
+def per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources, schedule, sp,
+                   stream):
+    import torch
+    out = {}
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    host = np.empty(ssp.nV, np.int32)
+    torch.cuda.synchronize()
+    a.record(stream)
+    ev = 0
+    its = []
+    for k in range(len(sources)):
+        e_s.upload_vertex_data_ptr(dev_s[k].data_ptr(), sp)
+        e_s.setActive(0, ssp.nV, sp)
+        its.append(e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp).iterations)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    for k in range(len(sources)):
+        e_s.upload_vertex_data_ptr(dev_s[k].data_ptr(), sp)
+        e_s.setActive(0, ssp.nV, sp)
+        e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
+        e_s.download_vertex_data(host, sp)
+        ev += edges_visited(out_sssp, host, 2**31 - 1 - 100000)
+    out["sssp"] = {"ms_per_source": round(ms / len(sources), 3),
+                   "gteps": round(ev / (ms * 1e-3) / 1e9, 4), "iterations": its}
+    a.record(stream)
+    e_c.upload_vertex_data_ptr(dev_c.data_ptr(), sp)
+    e_c.setActive(0, ccg.nV, sp)
+    it = e_c.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp).iterations
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    out["cc"] = {"ms": round(ms, 3), "gteps": round(ccg.nE / (ms * 1e-3) / 1e9, 4),
+                 "iterations": it}
+    return out
+
+
+def gather_roofline(e_s, dev_init, ssp, sp, stream):
+    """Times every launch of the load-balanced gather (+ fused apply) of one
+    SSSP run with CUDA events on its stream; algorithmic bytes per launch:
+    per active vertex 20 B (id, in-degree scan entry, row offset, own state
+    read, state write) and per in-edge 12 B (source id, source state,
+    weight)."""
+    import torch
+    e_s.upload_vertex_data_ptr(dev_init.data_ptr(), sp)
+    e_s.setActive(0, ssp.nV, sp)
+    total_ms, total_bytes, launches = 0.0, 0, 0
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    while e_s.countActive():
+        c = e_s.counters()
+        e_s.gather(True, sp)
+        a.record(stream)
+        e_s.apply(sp)
+        b.record(stream)
+        torch.cuda.synchronize()
+        total_ms += a.elapsed_time(b)
+        total_bytes += 20 * c.n_active + 12 * c.n_edges
+        launches += 1
+        e_s.scatterActivate(True, sp)
+        e_s.nextIter(sp)
+    achieved = total_bytes / (total_ms * 1e-3) / 1e9
+    return {"kernel": "k_gather_tiles+k_gather_fixup (SSSP pull, apply fused)",
+            "bound": "hbm", "achieved": round(achieved, 1), "unit": "GB/s",
+            "traffic": None, "launches": launches,
+            "algorithmic_bytes_per_launch": int(total_bytes / max(1, launches)),
+            "avg_launch_ms": round(total_ms / max(1, launches), 4)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle, a C port of refgas.h)
+# ---------------------------------------------------------------------------
+def cpu_sssp_sample(ssp, sources, out_sssp, n_threads):
+    import oracle
+    from graphreduce_gb300.engine import SSSP_GATHER_ZERO
+    res = [None] * n_threads
+
+    def work(i):
+        t = time.perf_counter()
+        d, it = oracle.sssp(ssp.nV, ssp.src, ssp.dst, ssp.weights, int(sources[i]))
+        res[i] = (d, it, time.perf_counter() - t)
+
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=work, args=(i,)) for i in range(n_threads)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    wall = time.perf_counter() - t0
+    ev = sum(edges_visited(out_sssp, r[0], SSSP_GATHER_ZERO) for r in res)
+    return ev / wall / 1e9, wall, res
+
+
+def run_reference(args):
+    import oracle  # noqa: F401  (the oracle port: the reference's refgas.h in C)
+    ssp, sources, _ = make_workload(args.scale)
+    out_sssp = ssp.out_degree()
+    cores = os.cpu_count() or 1
+    n = min(N_SOURCES, cores)
+    for _ in range(args.warmup):
+        cpu_sssp_sample(ssp, sources, out_sssp, n)
+    vals, walls = [], []
+    for _ in range(max(1, args.steps)):
+        v, w, _ = cpu_sssp_sample(ssp, sources, out_sssp, n)
+        vals.append(v)
+        walls.append(w)
+    value = statistics.median(vals)
+    sample = (f"SSSP from {n} of the {N_SOURCES} sources, one thread each, on the scale-"
+              f"{args.scale} graph (CC part of the step not sampled)")
+    return {"metric": METRIC, "value": round(value, 5), "unit": "GTEPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * statistics.median(walls), 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic", "impl": "reference",
+            "config": config_dict(args.scale),
+            "cpu_baseline": {"value": round(value, 5), "unit": "GTEPS", "cores": n,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 5), "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=int, default=SCALE)
+    ap.add_argument("--schedule", default="auto",
+                    choices=["auto", "generic", "push", "pull", "ordered"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)), flush=True)
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    result, cpu_inputs = run_ours(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            ssp, sources, out_sssp, first_sssp = cpu_inputs
+            import oracle
+            from graphreduce_gb300.engine import SSSP_GATHER_ZERO
+            t = time.perf_counter()
+            d, it = oracle.sssp(ssp.nV, ssp.src, ssp.dst, ssp.weights, int(sources[0]))
+            sec = time.perf_counter() - t
+            ev = edges_visited(out_sssp, d, SSSP_GATHER_ZERO)
+            result["cpu_baseline"] = {
+                "value": round(ev / sec / 1e9, 5), "unit": "GTEPS", "cores": 1, "kind": "port",
+                "sample": f"SSSP from source {int(sources[0])} on the scale-{args.scale} graph, "
+                          f"oracle C port of refgas.h, 1 thread, {sec:.1f}s"}
+            result["verified_against_oracle"] = bool(np.array_equal(d, first_sssp))
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,94 @@
+// gas_engine_impl.h -- the engine object shared by libgas translation units
+// (not installed).
+#ifndef GAS_ENGINE_IMPL_H_
+#define GAS_ENGINE_IMPL_H_
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "gas.h"
+#include "gas_internal.h"
+
+#define CUDA_TRY(call)                                                       \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      return gas::fail(GAS_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__,     \
+                       #call, cudaGetErrorString(e_));                       \
+  } while (0)
+
+#define GAS_TRY(call)                  \
+  do {                                 \
+    gas_status_t s_ = (call);          \
+    if (s_ != GAS_OK) return s_;       \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// The engine object.
+// ---------------------------------------------------------------------------
+// Instantiated CUDA graphs cached per engine (valid until the next
+// set_graph, since their kernels capture the engine's buffers).
+enum { kGraphGeneric = 0, kGraphOrdered = 1, kGraphPagerank = 2,
+       kGraphFast0 = 3, kGraphSlots = 12 };
+
+struct gas_engine {
+  gas_program_t prog = GAS_PROG_USER;
+  size_t vbytes = 0, gbytes = 0, ebytes = 0;
+  int32_t nV = 0, nE = 0;
+  void *host_vd = nullptr;
+  std::vector<int32_t> h_csc_off;  // for host-side counts in setActive
+
+  // device graph
+  int32_t *csc_off = nullptr, *csc_src = nullptr, *csr_off = nullptr,
+          *csr_dst = nullptr;
+  void *csc_ed = nullptr, *csr_ed = nullptr;
+
+  // device vertex + frontier state
+  void *vd = nullptr;
+  int32_t *act = nullptr, *scan = nullptr, *sscan = nullptr;
+  uint8_t *ret = nullptr;
+  void *slot = nullptr, *gres = nullptr;
+  uint32_t *bits = nullptr;
+  void *tile_first = nullptr, *tile_carry = nullptr;
+  int32_t *tile_a0 = nullptr;
+  int32_t tile_cap = 0;
+  int32_t *ppart = nullptr;  // predicated-scan partials
+  int32_t *cpart = nullptr;  // compaction partials (pairs)
+  int32_t n_cblocks = 0;
+  gas_counters *cnt = nullptr;
+  gas_counters *h_cnt = nullptr;  // pinned
+
+  // precision PageRank buffers (lazily allocated)
+  float *pr_rank[2] = {nullptr, nullptr};
+  float *pr_contrib[2] = {nullptr, nullptr};
+  float *pr_inv_deg = nullptr;
+  double *pr_l1 = nullptr;
+  int32_t pr_l1_cap = 0;
+  double pr_damping = 0.0;
+
+  // host view of the step API state
+  int32_t n_active = 0, n_edges = 0;
+  bool counts_dirty = false;
+  bool pending_gather = false;
+  bool have_gres = false;
+  bool slots_pending = false;
+  int32_t level = 0;
+  int num_sms = 0;
+  bool has_graph = false;
+  bool capturing = false;            // launches go into a CUDA graph
+  cudaGraphExec_t graphs[kGraphSlots] = {};
+  bool level_from_counters = false;  // BFS level = counters.iteration
+};
+
+namespace gas {
+// commit pending slots + expansion + compaction of the next frontier
+gas_status_t engine_scatter(gas_engine *e, void *stream);
+// one bulk-synchronous iteration of the generic (step API) kernels
+gas_status_t engine_generic_iteration(gas_engine *e, bool ordered, void *stream);
+// host copy of the counters (synchronises the stream)
+gas_status_t engine_sync_counts(gas_engine *e, void *stream);
+int engine_grid(int64_t work_items, int per_block, int cap);
+}  // namespace gas
+
+#endif  // GAS_ENGINE_IMPL_H_

@@ -1,0 +1,415 @@
+// gas_runs.cu -- whole-algorithm runs on a device-resident graph:
+//   * gas_engine_run_schedule: run() (gpugas.h:1792-1807) with the loop moved
+//     onto the device -- one iteration's kernels are captured once into the
+//     body of a CUDA-graph WHILE node whose condition a tiny kernel sets from
+//     the device counters, so there is no host round trip per iteration;
+//   * gas_engine_pagerank_precision: the normalised PageRank with FP32
+//     compensated (two-sum) gather and an FP64 L1 residual deciding
+//     convergence on the device.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cmath>
+#include <cstdio>
+
+#include "gas.h"
+#include "gas_device.cuh"
+#include "gas_engine_impl.h"
+#include "gas_internal.h"
+#include "gas_sched.h"
+
+using gasdev::kNT;
+using gasdev::SegSource;
+
+namespace {
+
+inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+// Loop condition: one more iteration while the frontier is non-empty and the
+// cap is not reached; hitting the cap with work left raises the error word.
+__global__ void k_loop_cond(gas_counters *cnt, cudaGraphConditionalHandle h) {
+  const int max_iter = cnt->max_iter;
+  const int it = ++cnt->iteration;
+  const bool more = cnt->n_active > 0;
+  if (more && it >= max_iter) cnt->error = GAS_ERR_ITER_CAP;
+  cnt->cond = (more && it < max_iter) ? 1 : 0;
+  cudaGraphSetConditional(h, cnt->cond);
+}
+
+__global__ void k_reset_loop(gas_counters *cnt, int32_t max_iter) {
+  cnt->iteration = 0;
+  cnt->error = 0;
+  cnt->cond = 1;
+  cnt->max_iter = max_iter;
+}
+
+}  // namespace
+
+namespace gas {
+
+// Builds graph = WHILE(cond) { body(stream, handle) } and instantiates it.
+gas_status_t build_while_graph(
+    gas_engine *e,
+    gas_status_t (*body)(gas_engine *, cudaStream_t, cudaGraphConditionalHandle,
+                         void *),
+    void *ctx, cudaGraphExec_t *out) {
+  cudaGraph_t g = nullptr;
+  cudaStream_t cs = nullptr;
+  cudaGraphExec_t x = nullptr;
+  gas_status_t st = GAS_OK;
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams p = {};
+  cudaGraphNode_t node;
+  cudaGraph_t bodyg;
+  CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaError_t ce = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (ce == cudaSuccess) {
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    ce = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p);
+  }
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(GAS_ERR_CUDA, "while-graph setup: %s", cudaGetErrorString(ce));
+  }
+  bodyg = p.conditional.phGraph_out[0];
+  ce = cudaStreamBeginCaptureToGraph(cs, bodyg, nullptr, nullptr, 0,
+                                     cudaStreamCaptureModeRelaxed);
+  if (ce == cudaSuccess) {
+    e->capturing = true;
+    st = body(e, cs, h, ctx);
+    e->capturing = false;
+    cudaGraph_t captured = nullptr;
+    cudaError_t ce2 = cudaStreamEndCapture(cs, &captured);
+    if (st == GAS_OK && ce2 != cudaSuccess)
+      st = fail(GAS_ERR_CUDA, "end capture: %s", cudaGetErrorString(ce2));
+  } else {
+    st = fail(GAS_ERR_CUDA, "begin capture: %s", cudaGetErrorString(ce));
+  }
+  if (st == GAS_OK) {
+    ce = cudaGraphInstantiate(&x, g, 0);
+    if (ce != cudaSuccess)
+      st = fail(GAS_ERR_CUDA, "instantiate: %s", cudaGetErrorString(ce));
+  }
+  cudaStreamDestroy(cs);
+  cudaGraphDestroy(g);
+  if (st == GAS_OK) *out = x;
+  return st;
+}
+
+// Turns the device error word / a non-empty frontier after the loop into a
+// status, and clears the word so the engine stays usable.
+gas_status_t loop_status(gas_engine *e, const gas_counters &c, void *stream) {
+  if (c.error)
+    CUDA_TRY(cudaMemsetAsync(&e->cnt->error, 0, sizeof(int32_t), S(stream)));
+  if (c.error == GAS_ERR_ITER_CAP || (c.error == 0 && c.n_active > 0))
+    return fail(GAS_ERR_ITER_CAP, "no convergence within %d iterations", c.iteration);
+  if (c.error)
+    return fail(GAS_ERR_DEVICE, "device error word %d after %d iterations", c.error,
+                c.iteration);
+  return GAS_OK;
+}
+
+}  // namespace gas
+
+namespace {
+
+struct GenericCtx {
+  bool ordered;
+};
+
+gas_status_t generic_body(gas_engine *e, cudaStream_t cs,
+                          cudaGraphConditionalHandle h, void *ctx) {
+  const GenericCtx *c = static_cast<const GenericCtx *>(ctx);
+  GAS_TRY(gas::engine_generic_iteration(e, c->ordered, cs));
+  k_loop_cond<<<1, 1, 0, cs>>>(e->cnt, h);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+}  // namespace
+
+extern "C" gas_status_t gas_engine_run_schedule(gas_engine *e,
+                                                gas_schedule_t schedule,
+                                                int32_t max_iterations,
+                                                gas_run_stats *stats,
+                                                void *stream) {
+  if (!e || !e->has_graph) return gas::fail(GAS_ERR_STATE, "run before set_graph");
+  if (e->prog == GAS_PROG_USER)
+    return gas::fail(GAS_ERR_UNSUPPORTED, "user programs run through gpugas.h");
+  if (max_iterations <= 0) max_iterations = INT_MAX;
+  if (stats) *stats = gas_run_stats{};
+  int32_t n = 0;
+  GAS_TRY(gas_engine_count_active(e, &n));
+  if (e->pending_gather || e->slots_pending)
+    return gas::fail(GAS_ERR_STATE, "run_schedule in the middle of a step");
+  if (n == 0) return GAS_OK;
+  if (schedule != GAS_SCHED_GENERIC && schedule != GAS_SCHED_ORDERED)
+    return gas::run_fast(e, schedule, max_iterations, stats, stream);
+
+  GenericCtx ctx{schedule == GAS_SCHED_ORDERED};
+  const int slot = ctx.ordered ? kGraphOrdered : kGraphGeneric;
+  if (!e->graphs[slot]) {
+    e->level_from_counters = true;
+    gas_status_t st = gas::build_while_graph(e, generic_body, &ctx, &e->graphs[slot]);
+    e->level_from_counters = false;
+    if (st != GAS_OK) return st;
+  }
+  k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
+  cudaError_t ce = cudaGetLastError();
+  if (ce == cudaSuccess) ce = cudaGraphLaunch(e->graphs[slot], S(stream));
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(stream));
+  if (ce != cudaSuccess)
+    return gas::fail(GAS_ERR_CUDA, "generic run: %s", cudaGetErrorString(ce));
+  gas_counters c;
+  GAS_TRY(gas_engine_read_counters(e, &c, stream));
+  if (stats) {
+    stats->iterations = c.iteration;
+    // per iteration: gather tiles + fixup (or BFS apply), commit, 3 scan
+    // passes, expand, 3 compaction passes, loop condition; plus the reset
+    stats->kernel_launches = c.iteration * (e->prog == GAS_PROG_BFS ? 9 : 11) + 1;
+  }
+  e->level = c.iteration;
+  return gas::loop_status(e, c, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Precision-form PageRank.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct PrVal {
+  float s, c;
+};
+
+// Error-free transformation: a.s + b.s = s + err exactly (Knuth two-sum);
+// compensation terms are carried in c.
+__device__ __forceinline__ PrVal two_sum_add(const PrVal &a, const PrVal &b) {
+  const float s = __fadd_rn(a.s, b.s);
+  const float bp = __fsub_rn(s, a.s);
+  const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bp)), __fsub_rn(b.s, bp));
+  return PrVal{s, __fadd_rn(__fadd_rn(a.c, b.c), err)};
+}
+
+struct PrPol {
+  typedef PrVal Val;
+  const int32_t *csc_src;
+  const int32_t *csr_off;
+  const float *contrib;
+  const float *rank_old;
+  float *rank_new;
+  float *contrib_new;
+  float base;
+  float damping;
+  double l1;
+  __device__ Val zero() const { return PrVal{0.0f, 0.0f}; }
+  __device__ __forceinline__ Val reduce(const Val &a, const Val &b) const {
+    return two_sum_add(a, b);
+  }
+  __device__ __forceinline__ Val map(int, int, int pos) const {
+    return PrVal{__ldg(contrib + __ldg(csc_src + pos)), 0.0f};
+  }
+  __device__ __forceinline__ void emit(int, int v, const Val &g) {
+    const float sum = __fadd_rn(g.s, g.c);
+    const float r = __fadd_rn(base, __fmul_rn(damping, sum));
+    const int deg = __ldg(csr_off + v + 1) - __ldg(csr_off + v);
+    rank_new[v] = r;
+    contrib_new[v] = deg ? __fdiv_rn(r, (float)deg) : 0.0f;
+    l1 += fabs((double)r - (double)rank_old[v]);
+  }
+};
+
+struct PrBufs {
+  float *rank[2];
+  float *contrib[2];
+};
+
+__device__ __forceinline__ void pr_bind(PrPol &pol, const PrBufs &b,
+                                        const gas_counters *cnt) {
+  const int p = cnt->iteration & 1;
+  pol.contrib = b.contrib[p];
+  pol.rank_old = b.rank[p];
+  pol.rank_new = b.rank[p ^ 1];
+  pol.contrib_new = b.contrib[p ^ 1];
+  pol.l1 = 0.0;
+}
+
+__device__ __forceinline__ void block_sum_store(double v, double *out) {
+  __shared__ double s_w[kNT / 32];
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kNT / 32; ++w) t += s_w[w];
+    *out = t;
+  }
+}
+
+__global__ void __launch_bounds__(kNT)
+    k_pr_tiles(PrPol pol, PrBufs bufs, SegSource src, PrVal *tf, PrVal *tc,
+               int32_t *ta0, const gas_counters *cnt, double *l1_part) {
+  pr_bind(pol, bufs, cnt);
+  gasdev::tile_loop<PrPol, true, true>(pol, src, tf, tc, ta0);
+  block_sum_store(pol.l1, l1_part + blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kNT)
+    k_pr_fixup(PrPol pol, PrBufs bufs, SegSource src, const PrVal *tf,
+               const PrVal *tc, const int32_t *ta0, const gas_counters *cnt,
+               double *l1_part) {
+  pr_bind(pol, bufs, cnt);
+  gasdev::fixup_loop<PrPol, true>(pol, src, tf, tc, ta0);
+  block_sum_store(pol.l1, l1_part + blockIdx.x);
+}
+
+// Deterministic sum of the per-CTA residuals; sets the loop condition.
+__global__ void __launch_bounds__(kNT)
+    k_pr_finish(const double *l1_part, int n, const double *tol_p,
+                gas_counters *cnt, double *residual,
+                cudaGraphConditionalHandle h) {
+  __shared__ double s[kNT];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += kNT) v += l1_part[i];
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (int d = kNT / 2; d > 0; d >>= 1) {
+    if (threadIdx.x < d) s[threadIdx.x] += s[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double l1 = s[0];
+    const double tol = *tol_p;
+    const int max_iter = cnt->max_iter;
+    *residual = l1;
+    const int it = ++cnt->iteration;
+    const bool more = !(l1 <= tol);
+    if (more && it >= max_iter) cnt->error = GAS_ERR_ITER_CAP;
+    cnt->cond = (more && it < max_iter) ? 1 : 0;
+    cudaGraphSetConditional(h, cnt->cond);
+  }
+}
+
+__global__ void k_pr_init(float *rank, float *contrib, const int32_t *csr_off,
+                          int n, float r0) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += gridDim.x * blockDim.x) {
+    const int deg = csr_off[v + 1] - csr_off[v];
+    rank[v] = r0;
+    contrib[v] = deg ? __fdiv_rn(r0, (float)deg) : 0.0f;
+  }
+}
+
+struct PrCtx {
+  PrPol pol;
+  PrBufs bufs;
+  SegSource src;
+  int tiles_grid;
+  int fix_grid;
+  double *residual;
+};
+
+gas_status_t pr_body(gas_engine *e, cudaStream_t cs,
+                     cudaGraphConditionalHandle h, void *vctx) {
+  PrCtx *c = static_cast<PrCtx *>(vctx);
+  k_pr_tiles<<<c->tiles_grid, kNT, 0, cs>>>(
+      c->pol, c->bufs, c->src, (PrVal *)e->tile_first, (PrVal *)e->tile_carry,
+      e->tile_a0, e->cnt, e->pr_l1);
+  k_pr_fixup<<<c->fix_grid, kNT, 0, cs>>>(
+      c->pol, c->bufs, c->src, (const PrVal *)e->tile_first,
+      (const PrVal *)e->tile_carry, e->tile_a0, e->cnt,
+      e->pr_l1 + c->tiles_grid);
+  k_pr_finish<<<1, kNT, 0, cs>>>(e->pr_l1, c->tiles_grid + c->fix_grid,
+                                 c->residual + 1, e->cnt, c->residual, h);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+}  // namespace
+
+extern "C" gas_status_t gas_engine_pagerank_precision(
+    gas_engine *e, double damping, double tol, int32_t max_iterations,
+    float *ranks, gas_run_stats *stats, void *stream) {
+  if (!e || !e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
+  if (!(damping > 0.0 && damping < 1.0) || !(tol > 0.0))
+    return gas::fail(GAS_ERR_INVALID, "damping must be in (0,1), tol > 0");
+  if (max_iterations <= 0) max_iterations = 1000;
+  if (stats) *stats = gas_run_stats{};
+  const int nV = e->nV;
+  if (nV == 0) return GAS_OK;
+  for (int i = 0; i < 2; ++i) {
+    if (!e->pr_rank[i]) CUDA_TRY(cudaMalloc(&e->pr_rank[i], (size_t)nV * 4));
+    if (!e->pr_contrib[i]) CUDA_TRY(cudaMalloc(&e->pr_contrib[i], (size_t)nV * 4));
+  }
+  int per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pr_tiles, kNT, 0));
+  if (per_sm < 1) per_sm = 1;
+  PrCtx c;
+  c.tiles_grid = e->num_sms * per_sm;
+  c.fix_grid = 2 * e->num_sms;
+  if (!e->pr_l1 || e->pr_l1_cap < c.tiles_grid + c.fix_grid + 2) {
+    if (e->pr_l1) cudaFree(e->pr_l1);
+    e->pr_l1 = nullptr;
+    if (e->graphs[kGraphPagerank]) cudaGraphExecDestroy(e->graphs[kGraphPagerank]);
+    e->graphs[kGraphPagerank] = nullptr;
+    e->pr_l1_cap = c.tiles_grid + c.fix_grid + 2;
+    CUDA_TRY(cudaMalloc(&e->pr_l1, sizeof(double) * (size_t)e->pr_l1_cap));
+  }
+  c.residual = e->pr_l1 + c.tiles_grid + c.fix_grid;
+  c.pol.csc_src = e->csc_src;
+  c.pol.csr_off = e->csr_off;
+  c.pol.base = (float)((1.0 - damping) / (double)nV);
+  c.pol.damping = (float)damping;
+  c.pol.l1 = 0.0;
+  c.bufs.rank[0] = e->pr_rank[0];
+  c.bufs.rank[1] = e->pr_rank[1];
+  c.bufs.contrib[0] = e->pr_contrib[0];
+  c.bufs.contrib[1] = e->pr_contrib[1];
+  c.src = SegSource{nullptr, nullptr, e->csc_off, nV, e->nE};
+
+  // damping is baked into the captured policy: rebuild when it changes
+  if (e->graphs[kGraphPagerank] && e->pr_damping != damping) {
+    cudaGraphExecDestroy(e->graphs[kGraphPagerank]);
+    e->graphs[kGraphPagerank] = nullptr;
+  }
+  if (!e->graphs[kGraphPagerank]) {
+    GAS_TRY(gas::build_while_graph(e, pr_body, &c, &e->graphs[kGraphPagerank]));
+    e->pr_damping = damping;
+  }
+  CUDA_TRY(cudaMemcpyAsync(c.residual + 1, &tol, sizeof(double),
+                           cudaMemcpyHostToDevice, S(stream)));
+  k_pr_init<<<gas::engine_grid(nV, kNT, 8 * e->num_sms), kNT, 0, S(stream)>>>(
+      e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV));
+  k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
+  cudaError_t ce = cudaGetLastError();
+  if (ce == cudaSuccess) ce = cudaGraphLaunch(e->graphs[kGraphPagerank], S(stream));
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(stream));
+  if (ce != cudaSuccess)
+    return gas::fail(GAS_ERR_CUDA, "pagerank: %s", cudaGetErrorString(ce));
+  gas_counters cnt;
+  GAS_TRY(gas_engine_read_counters(e, &cnt, stream));
+  if (cnt.error && cnt.error != GAS_ERR_ITER_CAP)
+    return gas::loop_status(e, cnt, stream);
+  if (cnt.error) CUDA_TRY(cudaMemsetAsync(&e->cnt->error, 0, sizeof(int32_t), S(stream)));
+  double resid = 0.0;
+  CUDA_TRY(cudaMemcpy(&resid, c.residual, sizeof(double), cudaMemcpyDeviceToHost));
+  const int final_buf = cnt.iteration & 1;
+  if (ranks)
+    CUDA_TRY(cudaMemcpyAsync(ranks, e->pr_rank[final_buf], (size_t)nV * 4,
+                             cudaMemcpyDefault, S(stream)));
+  CUDA_TRY(cudaStreamSynchronize(S(stream)));
+  if (stats) {
+    stats->iterations = cnt.iteration;
+    stats->pull_iters = cnt.iteration;
+    stats->kernel_launches = 3 * cnt.iteration + 2;
+    stats->edges_processed = (int64_t)cnt.iteration * e->nE;
+    stats->residual = resid;
+  }
+  if (!(resid <= tol))
+    return gas::fail(GAS_ERR_ITER_CAP, "pagerank: residual %.3e after %d iterations",
+                     resid, cnt.iteration);
+  return GAS_OK;
+}

@@ -1,0 +1,303 @@
+/*
+ * gas.h -- C ABI of libgas, the GB300 (sm_103a) Gather-Apply-Scatter engine.
+ *
+ * Plain C: pointers, sizes and status codes only.  Every entry point returns a
+ * gas_status_t; gas_last_error() gives a one-line description of the last
+ * failure on the calling thread.  Each declaration names the reference
+ * interface it replaces (paths inside dipanjans12/GraphReduce).
+ *
+ * Three layers:
+ *   1. host edge lists: graph I/O (.gr), synthetic R-MAT / Erdos-Renyi /
+ *      grid-island generators, source pickers, CSR construction;
+ *   2. the engine (GASEngineGPU's step API) for the reference's four vertex
+ *      programs built in (BFS, SSSP, CC, PageRank) and for user programs
+ *      compiled through include/gpugas.h;
+ *   3. whole-algorithm runs on a device-resident graph (the fast schedules,
+ *      device-side convergence, CUDA-graph iteration loop).
+ *
+ * Threading: an engine or graph handle is used by one host thread at a time.
+ * Streams: every call that launches work takes a cudaStream_t passed as
+ * void* (NULL = the legacy default stream, which is what the reference's
+ * apps rely on, bfs.cu:83-90).  Calls that return host values synchronise
+ * that stream.
+ */
+#ifndef GAS_H_
+#define GAS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GAS_OK = 0,
+  GAS_ERR_INVALID = 1,     /* bad argument (null pointer, id out of range...) */
+  GAS_ERR_NOMEM = 2,       /* host or device allocation failed */
+  GAS_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  GAS_ERR_ITER_CAP = 4,    /* iteration cap reached before convergence */
+  GAS_ERR_IO = 5,          /* file could not be read / written / parsed */
+  GAS_ERR_STATE = 6,       /* call out of order (e.g. run before setGraph) */
+  GAS_ERR_UNSUPPORTED = 7, /* operation not available for this program */
+  GAS_ERR_DEVICE = 8,      /* a kernel reported an error through its flag */
+  GAS_ERR_TOO_LARGE = 9    /* sizes beyond the 32-bit index space */
+} gas_status_t;
+
+/* Human-readable name of a status code. */
+const char *gas_status_string(gas_status_t s);
+/* Detail of the last failure on this thread ("" if none). */
+const char *gas_last_error(void);
+/* Library version string. */
+const char *gas_version(void);
+
+/* ======================================================================= */
+/* 1. Host edge lists (graphio.h / graphio.cpp, util.cuh)                  */
+/* ======================================================================= */
+
+/* An edge list in host memory: nV vertices, nE directed edges, optional
+ * 32-bit edge data (weights).  Generators return edges sorted by (src,dst). */
+typedef struct gas_edge_list gas_edge_list;
+
+/* Wrap copies of caller arrays (weights may be NULL).
+ * Replaces the std::vector<int> srcs/dsts/edgeValues triple that
+ * loadGraph fills (graphio.h:63-67). */
+gas_status_t gas_edge_list_create(int32_t nV, int64_t nE, const int32_t *srcs,
+                                  const int32_t *dsts, const int32_t *weights,
+                                  gas_edge_list **out);
+void gas_edge_list_destroy(gas_edge_list *el);
+int32_t gas_edge_list_num_vertices(const gas_edge_list *el);
+int64_t gas_edge_list_num_edges(const gas_edge_list *el);
+const int32_t *gas_edge_list_srcs(const gas_edge_list *el);
+const int32_t *gas_edge_list_dsts(const gas_edge_list *el);
+const int32_t *gas_edge_list_weights(const gas_edge_list *el); /* NULL if none */
+
+/* Seeded R-MAT graph: 2^scale vertices, edge_factor * 2^scale samples with
+ * quadrant probabilities (a, b, c, 1-a-b-c), no vertex permutation.  Self
+ * loops and duplicates are removed; symmetrize adds the reverse of every
+ * edge first.  No reference counterpart (the reference reads files only). */
+gas_status_t gas_rmat(int32_t scale, int32_t edge_factor, double a, double b,
+                      double c, uint64_t seed, int32_t symmetrize,
+                      gas_edge_list **out);
+
+/* Seeded Erdos-Renyi graph with n_samples uniform (src, dst) draws, self
+ * loops and duplicates removed.  No reference counterpart. */
+gas_status_t gas_erdos_renyi(int32_t nV, int64_t n_samples, uint64_t seed,
+                             int32_t symmetrize, gas_edge_list **out);
+
+/* Append n_islands disjoint side x side 4-neighbour grids (both directions)
+ * after the existing vertices, the way createCCGraph.cpp:36-44 concatenates
+ * graphs at vertex offsets. */
+gas_status_t gas_edge_list_append_grid_islands(gas_edge_list *el,
+                                               int32_t n_islands,
+                                               int32_t side);
+
+/* Give every edge a weight uniform in [lo, hi], drawn from (seed, min(u,v),
+ * max(u,v)) so both directions of an undirected edge agree. */
+gas_status_t gas_edge_list_set_uniform_weights(gas_edge_list *el, int32_t lo,
+                                               int32_t hi, uint64_t seed);
+
+/* The first vertex of maximum out-degree (bfs.cu:175-195, sssp.cu:148-168). */
+gas_status_t gas_edge_list_max_out_degree_vertex(const gas_edge_list *el,
+                                                 int32_t *vertex,
+                                                 int32_t *degree);
+
+/* k distinct vertices drawn uniformly (seeded) from the largest weakly
+ * connected component.  No reference counterpart. */
+gas_status_t gas_edge_list_sample_sources(const gas_edge_list *el, int32_t k,
+                                          uint64_t seed, int32_t *out);
+
+/* Lonestar binary CSR ".gr" files (graphio.cpp:265-272 format).
+ * gas_gr_write replaces writeGraph_binaryCSR (graphio.cpp:365-413) and always
+ * writes 4-byte edge data (zeros when the list has none) because the
+ * reference reader rejects files without it (graphio.cpp:298-307).
+ * gas_gr_read replaces loadGraph_binaryCSR with expand=true
+ * (graphio.cpp:274-362); files with 0-byte edge data are accepted too. */
+gas_status_t gas_gr_write(const char *path, const gas_edge_list *el);
+gas_status_t gas_gr_read(const char *path, gas_edge_list **out);
+
+/* edgeListToCSR (util.cuh:80-111): offsets[nV+1], out[nE] = vals in key
+ * order, perm[nE] = original edge index (out / perm may be NULL).  Edges of
+ * one key keep their edge-list order (stable). */
+gas_status_t gas_edge_list_to_csr(int32_t nV, int64_t nE, const int32_t *keys,
+                                  const int32_t *vals, int32_t *offsets,
+                                  int32_t *out, int32_t *perm);
+
+/* ======================================================================= */
+/* 2. Engine: GASEngineGPU (gpugas.h:1025-1809) as a C handle              */
+/* ======================================================================= */
+
+typedef enum {
+  GAS_PROG_USER = 0,     /* user Program compiled through include/gpugas.h */
+  GAS_PROG_BFS = 1,      /* bfs.cu:31-80            VertexData int32 depth  */
+  GAS_PROG_SSSP = 2,     /* sssp.cu:25-66           int32 dist, int32 weight */
+  GAS_PROG_CC = 3,       /* connected_component.cu:25-63  int32 label       */
+  GAS_PROG_PAGERANK = 4  /* pagerank.cu:27-73  {float rank; int32 numOutEdges} */
+} gas_program_t;
+
+typedef struct gas_engine gas_engine;
+
+/* GASEngineGPU() (gpugas.h:1129-1163) for a built-in program. */
+gas_status_t gas_engine_create(gas_program_t program, gas_engine **out);
+
+/* GASEngineGPU<Program>() for a user program: sizes of VertexData,
+ * GatherResult and EdgeData (EdgeData may be an empty struct: pass its
+ * sizeof).  Gather/apply kernels are then launched by include/gpugas.h. */
+gas_status_t gas_engine_create_user(size_t vertex_bytes, size_t gather_bytes,
+                                    size_t edge_bytes, gas_engine **out);
+
+/* ~GASEngineGPU() (gpugas.h:1165-1193). */
+void gas_engine_destroy(gas_engine *e);
+
+/* setGraph (gpugas.h:1314-1503): copies vertex data (nV records) and edge
+ * data (nE records, may be NULL) to the device and builds CSC (gather) and
+ * CSR (scatter) there from the edge list.  The host vertex array stays
+ * registered as the destination of gas_engine_get_results.  May be called
+ * again on the same engine (sssp.cu:85). */
+gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
+                                  int64_t nE, const void *edge_data,
+                                  const int32_t *srcs, const int32_t *dsts,
+                                  void *stream);
+
+/* setActive(start, end) (gpugas.h:1524-1546): active = [start, end). */
+gas_status_t gas_engine_set_active(gas_engine *e, int32_t start, int32_t end,
+                                   void *stream);
+
+/* countActive() (gpugas.h:1548-1551): size of the active set (host value). */
+gas_status_t gas_engine_count_active(gas_engine *e, int32_t *n_active);
+
+/* gather(haveGather) (gpugas.h:1553-1619).  Built-in programs only. */
+gas_status_t gas_engine_gather(gas_engine *e, int32_t have_gather,
+                               void *stream);
+
+/* apply() (gpugas.h:1621-1648).  Built-in programs only. */
+gas_status_t gas_engine_apply(gas_engine *e, void *stream);
+
+/* scatterActivate(haveScatter) (gpugas.h:1650-1759): next active set =
+ * out-neighbours of the vertices whose apply returned true, ascending id.
+ * Program::scatter is not invoked, as in the reference GPU engine. */
+gas_status_t gas_engine_scatter_activate(gas_engine *e, int32_t have_scatter,
+                                         void *stream);
+
+/* nextIter() (gpugas.h:1761-1772): makes the next active set current and
+ * returns its size (synchronises the stream). */
+gas_status_t gas_engine_next_iter(gas_engine *e, int32_t *n_active,
+                                  void *stream);
+
+/* getResults() (gpugas.h:1778-1787): copies device vertex data back to the
+ * host array given to setGraph.  (At the reference's HEAD this body is
+ * compiled out; here it does what its comment says.) */
+gas_status_t gas_engine_get_results(gas_engine *e, void *stream);
+
+/* run() (gpugas.h:1792-1807): iterate until no vertex is active. */
+gas_status_t gas_engine_run(gas_engine *e, int32_t *iterations, void *stream);
+
+/* BFS level used by the built-in BFS apply; mirrors setIterationCount<true>
+ * (bfs.cu:83-90). */
+gas_status_t gas_engine_set_iteration(gas_engine *e, int32_t level);
+
+/* Device vertex data (nV records) and copies into / out of it from host or
+ * device memory (any pointer the CUDA runtime can address), for callers that
+ * keep their state resident on the GPU. */
+gas_status_t gas_engine_vertex_data_device(gas_engine *e, void **ptr);
+gas_status_t gas_engine_upload_vertex_data(gas_engine *e, const void *host,
+                                           void *stream);
+gas_status_t gas_engine_download_vertex_data(gas_engine *e, void *host,
+                                             void *stream);
+
+/* Schedule of the built-in fast runs. */
+typedef enum {
+  GAS_SCHED_AUTO = 0,      /* fixed heuristic per iteration                */
+  GAS_SCHED_GENERIC = 1,   /* the step-API kernels (pull over active set)  */
+  GAS_SCHED_PUSH = 2,      /* push every iteration (SSSP, CC, BFS)         */
+  GAS_SCHED_PULL = 3,      /* dense pull every iteration (SSSP, CC, BFS)   */
+  GAS_SCHED_ORDERED = 4    /* generic, but each vertex folds its in-edges  */
+                           /* sequentially in CSC order (parity mode)      */
+} gas_schedule_t;
+
+typedef struct {
+  int32_t iterations;      /* GAS iterations, counted as run() counts them */
+  int32_t push_iters;      /* iterations run with the push schedule        */
+  int32_t pull_iters;      /* iterations run with the dense pull schedule  */
+  int32_t kernel_launches; /* launches of libgas kernels in the run        */
+  int64_t edges_processed; /* edges read by gather / expand kernels        */
+  double residual;         /* PageRank: last L1 residual                   */
+} gas_run_stats;
+
+/* Runs the built-in program to convergence from the engine's current
+ * vertex data and active set (set_active), like run(), with the chosen
+ * schedule; the iteration count and final vertex data are identical for
+ * every schedule.  Vertex data stays on the device (get_results copies). */
+gas_status_t gas_engine_run_schedule(gas_engine *e, gas_schedule_t schedule,
+                                     int32_t max_iterations,
+                                     gas_run_stats *stats, void *stream);
+
+/* Precision-form PageRank on the engine's graph (no reference counterpart;
+ * the reference formula pagerank.cu:62 scaled by 1/N): r0 = 1/N,
+ * r'_v = (1-d)/N + d * sum_{u->v} r_u / outdeg(u) with every vertex active
+ * every iteration, FP32 gather with two-sum compensation, FP64 L1 residual
+ * sum |r' - r|; stops after the first iteration with residual <= tol, on the
+ * device (CUDA-graph WHILE loop).  ranks: nV floats, device or host pointer
+ * (may be NULL).  Fails with GAS_ERR_ITER_CAP after max_iterations. */
+gas_status_t gas_engine_pagerank_precision(gas_engine *e, double damping,
+                                           double tol, int32_t max_iterations,
+                                           float *ranks, gas_run_stats *stats,
+                                           void *stream);
+
+/* ======================================================================= */
+/* Views used by include/gpugas.h to launch its Program-typed kernels.     */
+/* ======================================================================= */
+
+/* Device-resident counters of the current frontier (one 64-byte line). */
+typedef struct {
+  int32_t n_active;        /* |active|                                     */
+  int32_t n_edges;         /* sum of in-degree over active (gather work)   */
+  int32_t n_scatter_edges; /* sum of out-degree over apply==true vertices  */
+  int32_t error;           /* non-zero: a kernel hit an error              */
+  int32_t iteration;
+  int32_t cond;
+  int32_t n_changed;
+  int32_t max_iter;        /* iteration cap of the current device loop     */
+  int32_t pad[8];
+} gas_counters;
+
+typedef struct {
+  int32_t nV;
+  int32_t nE;
+  const int32_t *csc_off;  /* [nV+1] in-edge offsets                       */
+  const int32_t *csc_src;  /* [nE]   source of each in-edge                */
+  const void *csc_ed;      /* [nE]   edge data in CSC order (may be NULL)  */
+  const int32_t *csr_off;  /* [nV+1] out-edge offsets                      */
+  const int32_t *csr_dst;  /* [nE]   destination of each out-edge          */
+  const void *csr_ed;      /* [nE]   edge data in CSR order (may be NULL)  */
+  void *vertex_data;       /* [nV]   device vertex data                    */
+  int32_t *active;         /* [nV]   active vertex ids, ascending          */
+  int32_t *active_scan;    /* [nV+1] exclusive scan of in-degree over active */
+  uint8_t *apply_ret;      /* [nV]   apply() result per active slot       */
+  void *slot;              /* [nV]   new vertex data per active slot      */
+  void *gather_tmp;        /* [nV]   gather result per active slot        */
+  void *tile_first;        /* [tile_cap] gather partials (see gas_device.cuh) */
+  void *tile_carry;        /* [tile_cap]                                    */
+  int32_t *tile_a0;        /* [tile_cap]                                    */
+  int32_t tile_cap;
+  int32_t num_sms;         /* SM count of the engine's device              */
+  gas_counters *counters;  /* device                                       */
+} gas_engine_view;
+
+/* Device pointers of a user engine (valid until the next set_graph). */
+gas_status_t gas_engine_view_get(gas_engine *e, gas_engine_view *view);
+
+/* Host-side bookkeeping for user engines: the header tells the engine that
+ * its kernels wrote per-slot vertex data (commit pending) or updated the
+ * vertex data in place. */
+gas_status_t gas_engine_note_applied(gas_engine *e, int32_t wrote_slots);
+
+/* Host copy of the counters (synchronises the stream). */
+gas_status_t gas_engine_read_counters(gas_engine *e, gas_counters *out,
+                                      void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GAS_H_ */

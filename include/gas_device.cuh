@@ -1,0 +1,421 @@
+// gas_device.cuh -- device code shared by libgas and include/gpugas.h.
+//
+// The load-balanced gather of the reference (gpugas.h:714-786: a scan of
+// in-degrees, MergePathPartitions, kGatherMap writing E-sized temporaries,
+// then ReduceByKey) becomes one tiled kernel here:
+//
+//   * merge path over "segment ends + edges": the active list with its
+//     exclusive in-degree scan is merged with the edge index range, and every
+//     CTA tile takes kTile merge items, so hubs and zero-degree vertices are
+//     balanced alike;
+//   * the tile's row offsets are staged in shared memory, its edges are read
+//     cooperatively (consecutive threads -> consecutive CSC entries) and
+//     mapped with Program::gatherMap into shared memory;
+//   * each thread folds kVT items with Program::gatherReduce, a warp-shuffle
+//     segmented scan joins segments split across threads, and the segment's
+//     epilogue runs Program::apply (apply fused into the gather);
+//   * segments split across tiles leave a per-tile carry, folded by
+//     k_fixup_tiles in tile order (deterministic).
+//
+// The same walk, without the reduction, drives the scatter-side expansion
+// (frontier activation, gpugas.h:942-1013 + scatter_if_mgpu.h:130-157).
+//
+// Program::gatherZero is treated as the identity of Program::gatherReduce,
+// as the reference's ReduceByKey does (gpugas.h:766-776).
+#ifndef GAS_DEVICE_CUH_
+#define GAS_DEVICE_CUH_
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "gas.h"
+
+namespace gasdev {
+
+constexpr int kNT = 256;  // threads per CTA of the tiled kernels
+
+// Merge items per thread for a reduction value of a given size (keeps the
+// tile's shared memory under 48 KB).
+template <int kValBytes>
+struct TileShape {
+  static constexpr int kVT = kValBytes <= 8 ? 8 : (kValBytes <= 16 ? 4 : 2);
+  static constexpr int kTile = kNT * kVT;
+};
+
+// Shuffle of any trivially copyable value, in 32-bit pieces.
+template <class T>
+__device__ __forceinline__ T shfl_up_any(const T &v, int delta) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  int w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int k = 0; k < W; ++k) w[k] = __shfl_up_sync(0xffffffffu, w[k], delta);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+template <class T>
+__device__ __forceinline__ T shfl_down_any(const T &v, int delta) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  int w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int k = 0; k < W; ++k)
+    w[k] = __shfl_down_sync(0xffffffffu, w[k], delta);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+// Merge path over (segment ends, edge indices): the number of segment ends
+// among the first `diag` merge items.  ends[i] = end of segment i (exclusive
+// edge bound); an end is ordered before the edge with the same index.
+__device__ __forceinline__ int merge_path(const int32_t *__restrict__ ends,
+                                          int n_seg, int n_edge, int diag) {
+  int lo = diag - n_edge > 0 ? diag - n_edge : 0;
+  int hi = diag < n_seg ? diag : n_seg;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(ends + mid) <= diag - 1 - mid)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+template <class Val, int kTile>
+struct TileSmem {
+  int32_t end[kTile + 1];    // tile-local end of each touched segment
+  int32_t delta[kTile + 1];  // array position - edge index, per segment
+  int32_t vert[kTile + 1];   // vertex of each touched segment
+  uint16_t seg[kTile];       // local segment of each tile edge
+  Val val[kTile];            // mapped value of each tile edge
+  Val wv[kNT / 32];
+  int32_t wf[kNT / 32];
+  int32_t bounds[4];
+};
+
+// Where a frontier's segments come from.
+//   dense:  segment a = vertex a, edges off[a]..off[a+1]
+//   listed: segment a = vertex act[a], edge index range scan[a]..scan[a+1],
+//           array positions off[act[a]] + (edge - scan[a])
+struct SegSource {
+  const int32_t *act;
+  const int32_t *scan;
+  const int32_t *off;
+  int32_t n_seg;
+  int32_t n_edge;
+};
+
+// One pass over all tiles of a segment source.  Pol provides
+//   typedef Val; zero(); reduce(a, b); map(seg, vertex, pos) -> Val;
+//   emit(seg, vertex, Val)                     (kReduce)
+//   visit(seg, vertex, pos)                    (!kReduce)
+// Tiles whose first segment started in an earlier tile and ends here leave
+// tile_first[t] / tile_a0[t] for k_fixup_tiles; every tile leaves
+// tile_carry[t], the fold of its trailing open segment.
+template <class Pol, bool kDense, bool kReduce>
+__device__ __forceinline__ void tile_loop(Pol &pol, const SegSource src,
+                                          typename Pol::Val *tile_first,
+                                          typename Pol::Val *tile_carry,
+                                          int32_t *tile_a0) {
+  using Val = typename Pol::Val;
+  constexpr int kVT = TileShape<sizeof(Val)>::kVT;
+  constexpr int kTile = TileShape<sizeof(Val)>::kTile;
+  __shared__ TileSmem<Val, kTile> sm;
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const int nA = src.n_seg;
+  const int E = src.n_edge;
+  const int32_t *ends = kDense ? src.off + 1 : src.scan + 1;
+  const int64_t M = (int64_t)nA + E;
+  const int ntiles = (int)((M + kTile - 1) / kTile);
+
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int d0 = t * kTile;
+    const int d1 = (int)((int64_t)d0 + kTile < M ? (int64_t)d0 + kTile : M);
+    if (tid == 0) sm.bounds[0] = merge_path(ends, nA, E, d0);
+    if (tid == 32) sm.bounds[1] = merge_path(ends, nA, E, d1);
+    __syncthreads();
+    const int a0 = sm.bounds[0];
+    const int a1 = sm.bounds[1];
+    const int b0 = d0 - a0;
+    const int b1 = d1 - a1;
+    const int nX = a1 - a0;                  // segment ends inside the tile
+    const int nS = nX + (a1 < nA ? 1 : 0);   // segments touched by the tile
+    for (int i = tid; i < nS; i += kNT) {
+      const int a = a0 + i;
+      int v, beg, end, delta;
+      if (kDense) {
+        v = a;
+        beg = __ldg(src.off + a);
+        end = __ldg(src.off + a + 1);
+        delta = 0;
+      } else {
+        v = __ldg(src.act + a);
+        beg = __ldg(src.scan + a);
+        end = __ldg(src.scan + a + 1);
+        delta = __ldg(src.off + v) - beg;
+      }
+      sm.end[i] = end - b0;
+      sm.delta[i] = delta;
+      sm.vert[i] = v;
+      if (i == 0) sm.bounds[2] = (beg < b0) ? 1 : 0;  // segment a0 open-start
+    }
+    if (nS == 0 && tid == 0) sm.bounds[2] = 0;
+    __syncthreads();
+
+    const int nItems = d1 - d0;
+    const int nY = b1 - b0;
+    const int dl = tid * kVT < nItems ? tid * kVT : nItems;
+    const int dend = dl + kVT < nItems ? dl + kVT : nItems;
+    int la;
+    {
+      int lo = dl - nY > 0 ? dl - nY : 0;
+      int hi = dl < nX ? dl : nX;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (sm.end[mid] <= dl - 1 - mid)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      la = lo;
+    }
+    const int lb = dl - la;
+    {
+      int a = la, b = lb;
+      for (int k = dl; k < dend; ++k) {
+        if (a < nX && sm.end[a] <= b) {
+          ++a;
+        } else {
+          sm.seg[b] = (uint16_t)a;
+          ++b;
+        }
+      }
+    }
+    __syncthreads();
+
+    for (int j = tid; j < nY; j += kNT) {
+      const int ls = sm.seg[j];
+      const int pos = b0 + j + sm.delta[ls];
+      if constexpr (kReduce)
+        sm.val[j] = pol.map(a0 + ls, sm.vert[ls], pos);
+      else
+        pol.visit(a0 + ls, sm.vert[ls], pos);
+    }
+    __syncthreads();
+    if constexpr (!kReduce) continue;
+
+    Val acc = pol.zero();
+    Val lead = pol.zero();
+    int first = -1;
+    {
+      int a = la, b = lb;
+      for (int k = dl; k < dend; ++k) {
+        if (a < nX && sm.end[a] <= b) {
+          if (first < 0) {
+            first = a;
+            lead = acc;
+          } else {
+            pol.emit(a0 + a, sm.vert[a], acc);
+          }
+          acc = pol.zero();
+          ++a;
+        } else {
+          acc = pol.reduce(acc, sm.val[b]);
+          ++b;
+        }
+      }
+    }
+
+    // CTA-wide exclusive segmented scan of (has_end, tail fold).
+    Val incl = acc;
+    int fi = first >= 0 ? 1 : 0;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const Val ov = shfl_up_any(incl, d);
+      const int of = __shfl_up_sync(0xffffffffu, fi, d);
+      if (lane >= d) {
+        if (!fi) incl = pol.reduce(ov, incl);
+        fi |= of;
+      }
+    }
+    if (lane == 31) {
+      sm.wv[warp] = incl;
+      sm.wf[warp] = fi;
+    }
+    __syncthreads();
+    Val wp = pol.zero();
+    for (int w = 0; w < warp; ++w) {
+      if (sm.wf[w])
+        wp = sm.wv[w];
+      else
+        wp = pol.reduce(wp, sm.wv[w]);
+    }
+    Val ex = shfl_up_any(incl, 1);
+    int exf = __shfl_up_sync(0xffffffffu, fi, 1);
+    if (lane == 0) {
+      ex = pol.zero();
+      exf = 0;
+    }
+    const Val carry = exf ? ex : pol.reduce(wp, ex);
+    if (first >= 0) {
+      const Val g = pol.reduce(carry, lead);
+      if (first == 0 && sm.bounds[2]) {
+        tile_first[t] = g;
+      } else {
+        pol.emit(a0 + first, sm.vert[first], g);
+      }
+    }
+    if (tid == kNT - 1) tile_carry[t] = fi ? incl : pol.reduce(wp, incl);
+    if (tid == 0) tile_a0[t] = (sm.bounds[2] && nX > 0) ? a0 : -1;
+    __syncthreads();
+  }
+}
+
+// Completes the segments that span tiles: fold tile_carry over the tiles the
+// segment started in, then tile_first of the tile that ends it.  One warp
+// per tile; the fold order is fixed, so results are deterministic.
+template <class Pol, bool kDense>
+__device__ __forceinline__ void fixup_loop(Pol &pol, const SegSource src,
+                                           const typename Pol::Val *tile_first,
+                                           const typename Pol::Val *tile_carry,
+                                           const int32_t *tile_a0) {
+  using Val = typename Pol::Val;
+  constexpr int kTile = TileShape<sizeof(Val)>::kTile;
+  const int64_t M = (int64_t)src.n_seg + src.n_edge;
+  const int ntiles = (int)((M + kTile - 1) / kTile);
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int t = gwarp; t < ntiles; t += nwarps) {
+    const int a0 = tile_a0[t];
+    if (a0 < 0) continue;
+    const int beg = kDense ? __ldg(src.off + a0) : __ldg(src.scan + a0);
+    const int s_first = (int)(((int64_t)beg + a0) / kTile);
+    Val acc = pol.zero();
+    for (int s = s_first; s < t; s += 32) {
+      Val x = (s + lane < t) ? tile_carry[s + lane] : pol.zero();
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const Val y = shfl_down_any(x, d);
+        if (lane + d < 32) x = pol.reduce(x, y);
+      }
+      acc = pol.reduce(acc, x);  // lane 0 holds the chunk's ordered fold
+    }
+    if (lane == 0) {
+      const Val g = pol.reduce(acc, tile_first[t]);
+      const int v = kDense ? a0 : __ldg(src.act + a0);
+      pol.emit(a0, v, g);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Policies for a user Program (the gather step of GASEngineGPU).
+// ---------------------------------------------------------------------------
+
+template <class P>
+struct GenericGather {
+  typedef typename P::VertexData VD;
+  typedef typename P::EdgeData ED;
+  typedef typename P::GatherResult Val;
+  const int32_t *csc_src;
+  const ED *csc_ed;
+  const VD *vd;
+  VD *slot;      // fused: new vertex data per active slot
+  uint8_t *ret;  // fused: apply() result per active slot
+  Val *gres;     // gather-only: gather result per active slot
+  int fuse;
+
+  __device__ __forceinline__ Val zero() const { return P::gatherZero; }
+  __device__ __forceinline__ Val reduce(const Val &a, const Val &b) const {
+    return P::gatherReduce(a, b);
+  }
+  __device__ __forceinline__ Val map(int, int dst, int pos) const {
+    const int s = __ldg(csc_src + pos);
+    return P::gatherMap(vd + dst, vd + s, csc_ed + pos);
+  }
+  __device__ __forceinline__ void emit(int a, int v, const Val &g) const {
+    if (fuse) {
+      VD tmp = vd[v];
+      const bool r = P::apply(&tmp, g);
+      slot[a] = tmp;
+      ret[a] = r ? 1 : 0;
+    } else {
+      gres[a] = g;
+    }
+  }
+};
+
+template <class P>
+__global__ void __launch_bounds__(kNT)
+    k_gather_tiles(GenericGather<P> pol, SegSource src,
+                   typename P::GatherResult *tile_first,
+                   typename P::GatherResult *tile_carry, int32_t *tile_a0,
+                   const gas_counters *cnt) {
+  SegSource s = src;
+  if (cnt) {
+    s.n_seg = cnt->n_active;
+    s.n_edge = cnt->n_edges;
+  }
+  tile_loop<GenericGather<P>, false, true>(pol, s, tile_first, tile_carry,
+                                           tile_a0);
+}
+
+template <class P>
+__global__ void __launch_bounds__(kNT)
+    k_gather_fixup(GenericGather<P> pol, SegSource src,
+                   const typename P::GatherResult *tile_first,
+                   const typename P::GatherResult *tile_carry,
+                   const int32_t *tile_a0, const gas_counters *cnt) {
+  SegSource s = src;
+  if (cnt) {
+    s.n_seg = cnt->n_active;
+    s.n_edge = cnt->n_edges;
+  }
+  fixup_loop<GenericGather<P>, false>(pol, s, tile_first, tile_carry, tile_a0);
+}
+
+// Parity mode: one thread per active vertex folds its in-edges sequentially
+// in CSC order, exactly like refgas.h:143-160.
+template <class P>
+__global__ void __launch_bounds__(kNT)
+    k_gather_ordered(GenericGather<P> pol, const int32_t *act,
+                     const int32_t *csc_off, const gas_counters *cnt) {
+  const int n = cnt->n_active;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const int v = act[i];
+    typename P::GatherResult acc = P::gatherZero;
+    const int e1 = csc_off[v + 1];
+    for (int e = csc_off[v]; e < e1; ++e)
+      acc = P::gatherReduce(acc, pol.map(i, v, e));
+    pol.emit(i, v, acc);
+  }
+}
+
+// apply() without a preceding gather this iteration (BFS: gather(false)):
+// the vertex is updated in place, since no gather reads it concurrently.
+template <class P>
+__global__ void __launch_bounds__(kNT)
+    k_apply_only(const int32_t *act, const gas_counters *cnt,
+                 typename P::VertexData *vd,
+                 const typename P::GatherResult *gres, uint8_t *ret) {
+  const int n = cnt->n_active;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const typename P::GatherResult g = gres ? gres[i] : P::gatherZero;
+    ret[i] = P::apply(vd + act[i], g) ? 1 : 0;
+  }
+}
+
+}  // namespace gasdev
+
+#endif  // GAS_DEVICE_CUH_

@@ -1,0 +1,234 @@
+/*
+ * gpugas.h -- drop-in replacement for the reference's GPU engine header
+ * (gpugas.h:1025-1809, class GASEngineGPU), for one GB300 (sm_103a).
+ *
+ * The reference apps (bfs.cu, sssp.cu, pagerank.cu, connected_component.cu)
+ * compile unchanged against this header when it sits beside them (or comes
+ * first on the include path) and the program links libgas:
+ *
+ *   nvcc -gencode arch=compute_103a,code=sm_103a -std=c++17 \
+ *        -I<repo>/include app.cu util.cu graphio.cpp -L<lib dir> -lgas -lz
+ *
+ * The Program-typed kernels (the load-balanced gather with Program::apply in
+ * its epilogue, and apply without gather) are templates from gas_device.cuh
+ * instantiated in the app's own translation unit, so user functors and the
+ * app's __constant__ variables (bfs.cu:28) are visible to them.  Everything
+ * that does not depend on the Program -- CSR/CSC construction, the commit of
+ * applied vertex data, frontier expansion and compaction -- is libgas code
+ * reached through the C ABI of gas.h.
+ *
+ * Semantics kept from the reference: bulk-synchronous iterations (gather
+ * reads the vertex data of the previous iteration), active lists in
+ * ascending vertex id, setGraph re-callable on one engine (sssp.cu:85),
+ * all work on the legacy default stream (the apps write __constant__ data
+ * with cudaMemcpyToSymbol between steps), errors printed as
+ * "file(line): ..." followed by abort() (gpugas.h:1105-1112).
+ * Differences: getResults() really copies the vertex data back (at the
+ * reference's HEAD its body is compiled out, gpugas.h:1778-1787); there are
+ * no shards, because the whole graph stays resident in HBM.
+ */
+#ifndef GPUGAS_H__
+#define GPUGAS_H__
+
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+
+#include "gas.h"
+#include "gas_device.cuh"
+
+template <typename Program, typename Int = int32_t,
+          bool sortEdgesForGather = true>
+class GASEngineGPU {
+ public:
+  typedef typename Program::VertexData VertexData;
+  typedef typename Program::EdgeData EdgeData;
+  typedef typename Program::GatherResult GatherResult;
+
+ private:
+  gas_engine *m_engine;
+  gas_engine_view m_view;
+  bool m_haveGraph;
+  bool m_pendingGather;  // gather() called, kernels not launched yet
+  bool m_haveGatherTmp;  // gather_tmp holds this iteration's gather results
+  int m_gatherGrid;
+  int m_applyGrid;
+
+  void check(gas_status_t s, const char *file, int line) {
+    if (s != GAS_OK) {
+      printf("%s(%d): gas error %d (%s): %s\n", file, line, (int)s,
+             gas_status_string(s), gas_last_error());
+      abort();
+    }
+  }
+  void checkCuda(cudaError_t err, const char *file, int line) {
+    if (err != cudaSuccess) {
+      printf("%s(%d): cuda error %d (%s)\n", file, line, (int)err,
+             cudaGetErrorString(err));
+      abort();
+    }
+  }
+#define GPUGAS_CHECK(X) check((X), __FILE__, __LINE__)
+#define GPUGAS_CUDA(X) checkCuda((X), __FILE__, __LINE__)
+
+  gasdev::GenericGather<Program> policy(bool fuse) const {
+    gasdev::GenericGather<Program> p;
+    p.csc_src = m_view.csc_src;
+    p.csc_ed = static_cast<const EdgeData *>(m_view.csc_ed);
+    p.vd = static_cast<const VertexData *>(m_view.vertex_data);
+    p.slot = static_cast<VertexData *>(m_view.slot);
+    p.ret = m_view.apply_ret;
+    p.gres = static_cast<GatherResult *>(m_view.gather_tmp);
+    p.fuse = fuse ? 1 : 0;
+    return p;
+  }
+
+  // The load-balanced gather over the current active list; with fuse, apply
+  // runs in the epilogue and the new vertex data waits in per-slot storage
+  // until scatterActivate commits it.
+  void launchGather(bool fuse) {
+    gas_counters c;
+    GPUGAS_CHECK(gas_engine_read_counters(m_engine, &c, 0));
+    if (c.n_active == 0) return;
+    gasdev::SegSource src;
+    src.act = m_view.active;
+    src.scan = m_view.active_scan;
+    src.off = m_view.csc_off;
+    src.n_seg = c.n_active;
+    src.n_edge = c.n_edges;
+    typedef gasdev::TileShape<sizeof(GatherResult)> Shape;
+    const long long items = (long long)c.n_active + c.n_edges;
+    const long long tiles = (items + Shape::kTile - 1) / Shape::kTile;
+    const int grid = (int)(tiles < m_gatherGrid ? tiles : m_gatherGrid);
+    gasdev::k_gather_tiles<Program><<<grid, gasdev::kNT>>>(
+        policy(fuse), src, static_cast<GatherResult *>(m_view.tile_first),
+        static_cast<GatherResult *>(m_view.tile_carry), m_view.tile_a0,
+        m_view.counters);
+    GPUGAS_CUDA(cudaGetLastError());
+    const long long fix = (tiles + 7) / 8;
+    const int fgrid = (int)(fix < 4 * m_view.num_sms ? fix : 4 * m_view.num_sms);
+    gasdev::k_gather_fixup<Program><<<fgrid > 0 ? fgrid : 1, gasdev::kNT>>>(
+        policy(fuse), src, static_cast<GatherResult *>(m_view.tile_first),
+        static_cast<GatherResult *>(m_view.tile_carry), m_view.tile_a0,
+        m_view.counters);
+    GPUGAS_CUDA(cudaGetLastError());
+  }
+
+  void flushGather() {
+    if (!m_pendingGather) return;
+    m_pendingGather = false;
+    launchGather(false);
+    m_haveGatherTmp = true;
+  }
+
+ public:
+  GASEngineGPU()
+      : m_engine(0), m_haveGraph(false), m_pendingGather(false),
+        m_haveGatherTmp(false), m_gatherGrid(1), m_applyGrid(1) {
+    static_assert(sizeof(Int) == 4, "libgas indexes vertices and edges with 32 bits");
+    GPUGAS_CHECK(gas_engine_create_user(sizeof(VertexData), sizeof(GatherResult),
+                                        sizeof(EdgeData), &m_engine));
+  }
+
+  ~GASEngineGPU() { gas_engine_destroy(m_engine); }
+
+  // gpugas.h:1314-1503
+  void setGraph(Int nVertices, VertexData *vertexData, Int nEdges,
+                EdgeData *edgeData, const Int *edgeListSrcs,
+                const Int *edgeListDsts) {
+    GPUGAS_CHECK(gas_engine_set_graph(m_engine, nVertices, vertexData, nEdges,
+                                      edgeData, edgeListSrcs, edgeListDsts, 0));
+    GPUGAS_CHECK(gas_engine_view_get(m_engine, &m_view));
+    int perSm = 0;
+    GPUGAS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &perSm, gasdev::k_gather_tiles<Program>, gasdev::kNT, 0));
+    m_gatherGrid = m_view.num_sms * (perSm > 0 ? perSm : 1);
+    m_applyGrid = 8 * m_view.num_sms;
+    m_haveGraph = true;
+    m_pendingGather = false;
+    m_haveGatherTmp = false;
+  }
+
+  // gpugas.h:1524-1546
+  void setActive(Int vertexStart, Int vertexEnd) {
+    flushGather();
+    GPUGAS_CHECK(gas_engine_set_active(m_engine, vertexStart, vertexEnd, 0));
+  }
+
+  // gpugas.h:1548-1551
+  Int countActive() {
+    int32_t n = 0;
+    GPUGAS_CHECK(gas_engine_count_active(m_engine, &n));
+    return n;
+  }
+
+  // gpugas.h:1553-1619.  The launch is deferred to apply() so that gather and
+  // apply run as one kernel.
+  void gather(bool haveGather = true) {
+    m_haveGatherTmp = false;
+    m_pendingGather = haveGather;
+  }
+
+  // gpugas.h:1621-1648
+  void apply() {
+    if (m_pendingGather) {
+      m_pendingGather = false;
+      launchGather(true);
+      GPUGAS_CHECK(gas_engine_note_applied(m_engine, 1));
+      return;
+    }
+    gas_counters c;
+    GPUGAS_CHECK(gas_engine_read_counters(m_engine, &c, 0));
+    if (c.n_active == 0) return;
+    const int g = (c.n_active + gasdev::kNT - 1) / gasdev::kNT;
+    gasdev::k_apply_only<Program><<<g < m_applyGrid ? g : m_applyGrid, gasdev::kNT>>>(
+        m_view.active, m_view.counters, static_cast<VertexData *>(m_view.vertex_data),
+        m_haveGatherTmp ? static_cast<const GatherResult *>(m_view.gather_tmp) : 0,
+        m_view.apply_ret);
+    GPUGAS_CUDA(cudaGetLastError());
+    GPUGAS_CHECK(gas_engine_note_applied(m_engine, 0));
+  }
+
+  // gpugas.h:1650-1759
+  void scatterActivate(bool haveScatter = true) {
+    flushGather();
+    GPUGAS_CHECK(gas_engine_scatter_activate(m_engine, haveScatter ? 1 : 0, 0));
+    m_haveGatherTmp = false;
+  }
+
+  // gpugas.h:1761-1772
+  Int nextIter() {
+    int32_t n = 0;
+    GPUGAS_CHECK(gas_engine_next_iter(m_engine, &n, 0));
+    return n;
+  }
+
+  // gpugas.h:1778-1787 (with the copy-back its comment describes)
+  void getResults() {
+    flushGather();
+    GPUGAS_CHECK(gas_engine_get_results(m_engine, 0));
+  }
+
+  // gpugas.h:1792-1807
+  void run() {
+    int i = 1;
+    while (countActive()) {
+      gather();
+      apply();
+      scatterActivate();
+      nextIter();
+      ++i;
+    }
+    printf("Iterations: %d\n", i - 1);
+  }
+
+#undef GPUGAS_CHECK
+#undef GPUGAS_CUDA
+};
+
+#endif  // GPUGAS_H__

@@ -1,0 +1,212 @@
+"""THE ORACLE -- test infrastructure only.
+
+ctypes access to oracle/_build/liboracle.so (gas_oracle.c, the C restatement
+of the reference's CPU engine refgas.h and its four programs) and, when it was
+built from the reference sources, oracle/_ref/libref.so (the reference's own
+refgas.h / graphio.cpp).  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg import this package; the engine never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+import threading
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIBORACLE = HERE / "_build" / "liboracle.so"
+LIBREF = HERE / "_ref" / "libref.so"
+
+_lock = threading.Lock()
+_orc = None
+_ref = None
+
+c_i32, c_i64, c_dbl, c_vp = C.c_int32, C.c_int64, C.c_double, C.c_void_p
+
+
+def _oracle():
+    global _orc
+    with _lock:
+        if _orc is None:
+            if not LIBORACLE.exists():
+                subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+            lib = C.CDLL(str(LIBORACLE))
+            lib.orc_edge_list_to_csr.argtypes = [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]
+            lib.orc_edge_list_to_csr.restype = C.c_int
+            lib.orc_bfs.argtypes = [c_i32, c_i64, c_vp, c_vp, c_i32, c_vp]
+            lib.orc_sssp.argtypes = [c_i32, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp]
+            lib.orc_cc.argtypes = [c_i32, c_i64, c_vp, c_vp, c_vp]
+            lib.orc_pagerank.argtypes = [c_i32, c_i64, c_vp, c_vp, c_vp]
+            lib.orc_pagerank_fp64.argtypes = [c_i32, c_i64, c_vp, c_vp, c_dbl, c_dbl, c_i64,
+                                              c_vp, c_vp]
+            lib.orc_pagerank_fp64_step.argtypes = [c_i32, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp]
+            lib.orc_pagerank_fp64_step.restype = c_dbl
+            for f in ("orc_bfs", "orc_sssp", "orc_cc", "orc_pagerank", "orc_pagerank_fp64"):
+                getattr(lib, f).restype = c_i64
+            _orc = lib
+    return _orc
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, np.int32)
+
+
+def _check(it: int, what: str) -> int:
+    if it < 0:
+        raise RuntimeError(f"oracle {what} failed with code {it}")
+    return int(it)
+
+
+def bfs(nV, src, dst, source):
+    """bfs.cu:93-134 on refgas.h semantics -> (depth int32[nV], iterations)."""
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(nV, np.int32)
+    it = _oracle().orc_bfs(nV, s.shape[0], s.ctypes.data, d.ctypes.data, source, out.ctypes.data)
+    return out, _check(it, "bfs")
+
+
+def sssp(nV, src, dst, weights, source):
+    """sssp.cu:69-111 (one run) -> (dist int32[nV], iterations)."""
+    s, d, w = _i32(src), _i32(dst), _i32(weights)
+    out = np.zeros(nV, np.int32)
+    it = _oracle().orc_sssp(nV, s.shape[0], s.ctypes.data, d.ctypes.data, w.ctypes.data,
+                            source, out.ctypes.data)
+    return out, _check(it, "sssp")
+
+
+def cc(nV, src, dst):
+    """connected_component.cu:66-81 -> (label int32[nV], iterations)."""
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(nV, np.int32)
+    it = _oracle().orc_cc(nV, s.shape[0], s.ctypes.data, d.ctypes.data, out.ctypes.data)
+    return out, _check(it, "cc")
+
+
+def pagerank(nV, src, dst):
+    """pagerank.cu:85-101 -> (rank float32[nV], iterations)."""
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(nV, np.float32)
+    it = _oracle().orc_pagerank(nV, s.shape[0], s.ctypes.data, d.ctypes.data, out.ctypes.data)
+    return out, _check(it, "pagerank")
+
+
+def pagerank_fp64(nV, src, dst, damping=0.85, tol=1e-6, max_iter=1000):
+    """Precision-form PageRank in FP64 -> (rank float64[nV], iterations, L1)."""
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(nV, np.float64)
+    l1 = C.c_double()
+    it = _oracle().orc_pagerank_fp64(nV, s.shape[0], s.ctypes.data, d.ctypes.data, damping,
+                                     tol, max_iter, out.ctypes.data, C.byref(l1))
+    return out, _check(it, "pagerank_fp64"), l1.value
+
+
+def pagerank_fp64_step(nV, src, dst, r, damping=0.85):
+    """One FP64 precision-form step from ranks r -> (r', L1)."""
+    s, d = _i32(src), _i32(dst)
+    r = np.ascontiguousarray(r, np.float64)
+    out = np.zeros(nV, np.float64)
+    l1 = _oracle().orc_pagerank_fp64_step(nV, s.shape[0], s.ctypes.data, d.ctypes.data,
+                                          damping, r.ctypes.data, out.ctypes.data)
+    return out, l1
+
+
+def edge_list_to_csr(nV, keys, vals):
+    """util.cuh:80-111 restated (stable) -> (offsets int64, out, perm)."""
+    k, v = _i32(keys), _i32(vals)
+    off = np.zeros(nV + 1, np.int64)
+    out = np.zeros(k.shape[0], np.int32)
+    perm = np.zeros(k.shape[0], np.int32)
+    rc = _oracle().orc_edge_list_to_csr(nV, k.shape[0], k.ctypes.data, v.ctypes.data,
+                                        off.ctypes.data, out.ctypes.data, perm.ctypes.data)
+    if rc:
+        raise ValueError(f"edge_list_to_csr: code {rc}")
+    return off, out, perm
+
+
+# ---------------------------------------------------------------------------
+# The reference itself (oracle/_ref/libref.so), when built in this container.
+# ---------------------------------------------------------------------------
+
+def reference_available() -> bool:
+    return LIBREF.exists()
+
+
+def _reference():
+    global _ref
+    with _lock:
+        if _ref is None:
+            lib = C.CDLL(str(LIBREF))
+            lib.ref_bfs.argtypes = [c_i32, c_i32, c_vp, c_vp, c_i32, c_vp]
+            lib.ref_sssp.argtypes = [c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp]
+            lib.ref_cc.argtypes = [c_i32, c_i32, c_vp, c_vp, c_vp]
+            lib.ref_pagerank.argtypes = [c_i32, c_i32, c_vp, c_vp, c_vp]
+            for f in ("ref_bfs", "ref_sssp", "ref_cc", "ref_pagerank"):
+                getattr(lib, f).restype = c_i64
+            lib.ref_edge_list_to_csr.argtypes = [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]
+            lib.ref_write_gr.argtypes = [C.c_char_p, c_i32, c_i32, c_vp, c_vp, c_vp]
+            lib.ref_load_graph.argtypes = [C.c_char_p, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]
+            lib.ref_load_graph.restype = c_i64
+            _ref = lib
+    return _ref
+
+
+def ref_bfs(nV, src, dst, source):
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(nV, np.int32)
+    it = _reference().ref_bfs(nV, s.shape[0], s.ctypes.data, d.ctypes.data, source,
+                              out.ctypes.data)
+    return out, int(it)
+
+
+def ref_sssp(nV, src, dst, weights, source):
+    s, d, w = _i32(src), _i32(dst), _i32(weights)
+    out = np.zeros(nV, np.int32)
+    it = _reference().ref_sssp(nV, s.shape[0], s.ctypes.data, d.ctypes.data, w.ctypes.data,
+                               source, out.ctypes.data)
+    return out, int(it)
+
+
+def ref_cc(nV, src, dst):
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(nV, np.int32)
+    it = _reference().ref_cc(nV, s.shape[0], s.ctypes.data, d.ctypes.data, out.ctypes.data)
+    return out, int(it)
+
+
+def ref_pagerank(nV, src, dst):
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(nV, np.float32)
+    it = _reference().ref_pagerank(nV, s.shape[0], s.ctypes.data, d.ctypes.data,
+                                   out.ctypes.data)
+    return out, int(it)
+
+
+def ref_edge_list_to_csr(nV, keys, vals):
+    k, v = _i32(keys), _i32(vals)
+    off = np.zeros(nV + 1, np.int32)
+    out = np.zeros(k.shape[0], np.int32)
+    perm = np.zeros(k.shape[0], np.int32)
+    _reference().ref_edge_list_to_csr(nV, k.shape[0], k.ctypes.data, v.ctypes.data,
+                                      off.ctypes.data, out.ctypes.data, perm.ctypes.data)
+    return off, out, perm
+
+
+def ref_write_gr(path, nV, offsets, dsts, weights):
+    o, d = _i32(offsets), _i32(dsts)
+    w = None if weights is None else _i32(weights)
+    _reference().ref_write_gr(str(path).encode(), nV, d.shape[0], o.ctypes.data, d.ctypes.data,
+                              None if w is None else w.ctypes.data)
+
+
+def ref_load_graph(path, cap, want_weights=True):
+    s = np.zeros(cap, np.int32)
+    d = np.zeros(cap, np.int32)
+    w = np.zeros(cap, np.int32)
+    nV = C.c_int32()
+    n = _reference().ref_load_graph(str(path).encode(), int(want_weights), cap, C.byref(nV),
+                                    s.ctypes.data, d.ctypes.data, w.ctypes.data)
+    if n < 0:
+        raise ValueError("capacity too small")
+    return nV.value, s[:n], d[:n], (w[:n] if want_weights else None)

@@ -1,0 +1,370 @@
+/*
+ * gas_oracle.c -- THE ORACLE (test infrastructure, not product code).
+ *
+ * A plain-C restatement of the reference's CPU Gather-Apply-Scatter engine
+ * `GASEngineRef` (refgas.h:30-230) driving restatements of the reference's four
+ * vertex programs (bfs.cu:31-80, sssp.cu:25-66, connected_component.cu:25-63,
+ * pagerank.cu:27-73) exactly the way the reference apps drive them
+ * (bfs.cu:93-134, sssp.cu:69-111 one run, connected_component.cu:66-81,
+ * pagerank.cu:85-101), plus an FP64 power-iteration PageRank in the
+ * normalised "precision form" (r = (1-d)/N + d * sum r_u/outdeg_u, stop when
+ * the global L1 residual <= tol) used to judge the FP32 GPU PageRank.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+ * this library, and only as the checker / the timed CPU baseline.  The GPU
+ * engine never calls into it.
+ *
+ * Parity pin: tests/test_oracle.py checks every function here against golden
+ * vectors that tests/golden/make_golden.py produced by running the reference's
+ * own refgas.h (compiled by oracle/Makefile into oracle/_ref/libref.so).
+ *
+ * One deliberate difference from the reference: edgeListToCSR (util.cuh:80-111)
+ * orders the edges of one vertex with an unstable std::sort (util.cuh:49-72);
+ * this restatement uses a stable counting sort, so edges of one vertex keep
+ * their edge-list order.  Integer programs (min / level) do not depend on that
+ * order; PageRank sums can differ in the last ulp, which the tests allow for.
+ *
+ * Build: oracle/Makefile (gcc -O2 -ffp-contract=off, so x86 and Arm agree).
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <limits.h>
+
+#define ORC_EXPORT __attribute__((visibility("default")))
+
+/* ------------------------------------------------------------------------ */
+/* CSR / CSC construction: util.cuh:80-121 (edgeListToCSR / edgeListToCSC).  */
+/* ------------------------------------------------------------------------ */
+
+/* offsets[nV+1]; out[nE] = vals[perm[i]]; perm[nE] = original edge index.
+ * Keys outside [0,nV) are a caller error and return -1. */
+ORC_EXPORT int orc_edge_list_to_csr(int32_t nV, int64_t nE,
+                                    const int32_t *keys, const int32_t *vals,
+                                    int64_t *offsets, int32_t *out,
+                                    int32_t *perm)
+{
+  int64_t i;
+  int32_t v;
+  int64_t *cursor;
+  for (v = 0; v <= nV; ++v) offsets[v] = 0;
+  for (i = 0; i < nE; ++i) {
+    if (keys[i] < 0 || keys[i] >= nV) return -1;
+    offsets[keys[i] + 1]++;
+  }
+  for (v = 0; v < nV; ++v) offsets[v + 1] += offsets[v];
+  cursor = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nV > 0 ? nV : 1));
+  if (!cursor) return -2;
+  for (v = 0; v < nV; ++v) cursor[v] = offsets[v];
+  for (i = 0; i < nE; ++i) {
+    int64_t pos = cursor[keys[i]]++;
+    if (out) out[pos] = vals[i];
+    if (perm) perm[pos] = (int32_t)i;
+  }
+  free(cursor);
+  return 0;
+}
+
+typedef struct {
+  int32_t nV;
+  int64_t nE;
+  /* gather side (CSC): in-edges grouped by destination, refgas.h:43-46 */
+  int64_t *csc_off;
+  int32_t *csc_src;
+  int32_t *csc_eid;
+  /* scatter side (CSR): out-edges grouped by source, refgas.h:48-51 */
+  int64_t *csr_off;
+  int32_t *csr_dst;
+  int32_t *csr_eid;
+} orc_graph;
+
+static void graph_free(orc_graph *g)
+{
+  free(g->csc_off); free(g->csc_src); free(g->csc_eid);
+  free(g->csr_off); free(g->csr_dst); free(g->csr_eid);
+}
+
+/* refgas.h:81-113 (setGraph): CSR for scatter, CSC for gather. */
+static int graph_init(orc_graph *g, int32_t nV, int64_t nE,
+                      const int32_t *srcs, const int32_t *dsts)
+{
+  size_t ne = (size_t)(nE > 0 ? nE : 1);
+  memset(g, 0, sizeof(*g));
+  g->nV = nV;
+  g->nE = nE;
+  g->csc_off = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nV + 1));
+  g->csr_off = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nV + 1));
+  g->csc_src = (int32_t *)malloc(sizeof(int32_t) * ne);
+  g->csc_eid = (int32_t *)malloc(sizeof(int32_t) * ne);
+  g->csr_dst = (int32_t *)malloc(sizeof(int32_t) * ne);
+  g->csr_eid = (int32_t *)malloc(sizeof(int32_t) * ne);
+  if (!g->csc_off || !g->csr_off || !g->csc_src || !g->csc_eid ||
+      !g->csr_dst || !g->csr_eid) {
+    graph_free(g);
+    return -2;
+  }
+  if (orc_edge_list_to_csr(nV, nE, srcs, dsts, g->csr_off, g->csr_dst,
+                           g->csr_eid) ||
+      orc_edge_list_to_csr(nV, nE, dsts, srcs, g->csc_off, g->csc_src,
+                           g->csc_eid)) {
+    graph_free(g);
+    return -1;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The engine, instantiated once per program through gas_oracle_engine.inc.  */
+/* ------------------------------------------------------------------------ */
+
+/* BFS::apply reads the level from a global (bfs.cu:27-28, 58-71). */
+static int32_t g_bfs_level;
+
+typedef struct { float rank; int32_t numOutEdges; } orc_pr_vertex;
+
+/* BFS: bfs.cu:31-80 */
+#define ENG bfs
+#define VD int32_t
+#define ED int32_t
+#define GR int32_t
+#define ZERO (INT_MAX - 1)
+#define MAP(dst, src, e) ((void)(dst), (void)(src), (void)(e), 0)
+#define REDUCE(a, b) ((void)(a), (void)(b), 0)
+static inline int bfs_apply(int32_t *v, int32_t g)
+{
+  (void)g;
+  if (*v == -1) { *v = g_bfs_level; return 1; }
+  return 0;
+}
+#define APPLY(v, g) bfs_apply((v), (g))
+#include "gas_oracle_engine.inc"
+
+/* SSSP: sssp.cu:25-66 */
+#define ENG sssp
+#define VD int32_t
+#define ED int32_t
+#define GR int32_t
+#define ZERO (INT_MAX - 100000)
+#define MAP(dst, src, e) ((void)(dst), *(src) + *(e))
+#define REDUCE(a, b) ((a) < (b) ? (a) : (b))
+static inline int min_apply(int32_t *v, int32_t g)
+{
+  int changed = g < *v;
+  if (g < *v) *v = g;
+  return changed;
+}
+#define APPLY(v, g) min_apply((v), (g))
+#include "gas_oracle_engine.inc"
+
+/* CC: connected_component.cu:25-63 */
+#define ENG cc
+#define VD int32_t
+#define ED int32_t
+#define GR int32_t
+#define ZERO INT_MAX
+#define MAP(dst, src, e) ((void)(dst), (void)(e), *(src))
+#define REDUCE(a, b) ((a) < (b) ? (a) : (b))
+#define APPLY(v, g) min_apply((v), (g))
+#include "gas_oracle_engine.inc"
+
+/* PageRank, reference (unnormalised) form: pagerank.cu:27-73 */
+#define ENG pr
+#define VD orc_pr_vertex
+#define ED int32_t
+#define GR float
+#define ZERO 0.0f
+#define MAP(dst, src, e) ((void)(dst), (void)(e), (src)->rank / (float)(src)->numOutEdges)
+#define REDUCE(a, b) ((a) + (b))
+static inline int pr_apply(orc_pr_vertex *v, float g)
+{
+  const float pageConst = 0.15f, tol = 0.01f;
+  float newRank = pageConst + (1.0f - pageConst) * g;
+  int ret = fabsf(newRank - v->rank) >= tol;
+  v->rank = newRank;
+  return ret;
+}
+#define APPLY(v, g) pr_apply((v), (g))
+#include "gas_oracle_engine.inc"
+
+/* ------------------------------------------------------------------------ */
+/* Drivers, each mirroring how the reference app runs the engine.           */
+/* All return the number of GAS iterations, or a negative error code.       */
+/* ------------------------------------------------------------------------ */
+
+/* bfs.cu:93-134: depth=-1, setActive(src,src+1), step loop with
+ * gather(false)/apply/scatterActivate(false)/nextIter and ++level. */
+ORC_EXPORT int64_t orc_bfs(int32_t nV, int64_t nE, const int32_t *srcs,
+                           const int32_t *dsts, int32_t source,
+                           int32_t *depth)
+{
+  orc_graph g;
+  bfs_engine e;
+  int64_t it = 0;
+  int32_t v;
+  if (nV > 0 && (source < 0 || source >= nV)) return -1;
+  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
+  for (v = 0; v < nV; ++v) depth[v] = -1;
+  if (bfs_engine_init(&e, &g, depth, NULL)) { graph_free(&g); return -2; }
+  if (nV > 0) bfs_set_active(&e, source, source + 1);
+  g_bfs_level = 0;
+  while (bfs_count_active(&e)) {
+    bfs_gather(&e);
+    bfs_apply_all(&e);
+    bfs_scatter_activate(&e);
+    bfs_next_iter(&e);
+    g_bfs_level = (int32_t)(++it);
+  }
+  bfs_engine_free(&e);
+  graph_free(&g);
+  return it;
+}
+
+/* sssp.cu:69-111 (one of its ten identical runs): dist = gatherZero except
+ * the source, setActive(0,n), step loop with gather/apply/scatter/nextIter. */
+ORC_EXPORT int64_t orc_sssp(int32_t nV, int64_t nE, const int32_t *srcs,
+                            const int32_t *dsts, const int32_t *weights,
+                            int32_t source, int32_t *dist)
+{
+  orc_graph g;
+  sssp_engine e;
+  int64_t it = 0;
+  int32_t v;
+  if (nV > 0 && (source < 0 || source >= nV)) return -1;
+  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
+  for (v = 0; v < nV; ++v) dist[v] = INT_MAX - 100000;
+  if (nV > 0) dist[source] = 0;
+  if (sssp_engine_init(&e, &g, dist, weights)) { graph_free(&g); return -2; }
+  sssp_set_active(&e, 0, nV);
+  while (sssp_count_active(&e)) {
+    sssp_gather(&e);
+    sssp_apply_all(&e);
+    sssp_scatter_activate(&e);
+    sssp_next_iter(&e);
+    ++it;
+  }
+  sssp_engine_free(&e);
+  graph_free(&g);
+  return it;
+}
+
+/* connected_component.cu:66-81 and 386-389: label = id, setActive(0,n), run(). */
+ORC_EXPORT int64_t orc_cc(int32_t nV, int64_t nE, const int32_t *srcs,
+                          const int32_t *dsts, int32_t *label)
+{
+  orc_graph g;
+  cc_engine e;
+  int64_t it;
+  int32_t v;
+  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
+  for (v = 0; v < nV; ++v) label[v] = v;
+  if (cc_engine_init(&e, &g, label, NULL)) { graph_free(&g); return -2; }
+  cc_set_active(&e, 0, nV);
+  it = cc_run(&e);
+  cc_engine_free(&e);
+  graph_free(&g);
+  return it;
+}
+
+/* pagerank.cu:85-101 and 374-382: rank = 0.15, numOutEdges = out-degree,
+ * setActive(0,n), run().  rank[] receives the final ranks. */
+ORC_EXPORT int64_t orc_pagerank(int32_t nV, int64_t nE, const int32_t *srcs,
+                                const int32_t *dsts, float *rank)
+{
+  orc_graph g;
+  pr_engine e;
+  orc_pr_vertex *vd;
+  int64_t it;
+  int32_t v;
+  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
+  vd = (orc_pr_vertex *)malloc(sizeof(orc_pr_vertex) * (size_t)(nV > 0 ? nV : 1));
+  if (!vd) { graph_free(&g); return -2; }
+  for (v = 0; v < nV; ++v) {
+    vd[v].rank = 0.15f;
+    vd[v].numOutEdges = (int32_t)(g.csr_off[v + 1] - g.csr_off[v]);
+  }
+  if (pr_engine_init(&e, &g, vd, NULL)) { free(vd); graph_free(&g); return -2; }
+  pr_set_active(&e, 0, nV);
+  it = pr_run(&e);
+  for (v = 0; v < nV; ++v) rank[v] = vd[v].rank;
+  pr_engine_free(&e);
+  free(vd);
+  graph_free(&g);
+  return it;
+}
+
+/* Precision-form PageRank in FP64: r0 = 1/N; every vertex active every
+ * iteration; r'_v = (1-d)/N + d * sum_{u->v} r_u / outdeg(u) (no dangling
+ * redistribution); stop after the first iteration whose L1 residual
+ * sum |r' - r| <= tol, or fail with -3 after max_iter iterations.
+ * Returns iterations; *l1_out = last residual. */
+ORC_EXPORT int64_t orc_pagerank_fp64(int32_t nV, int64_t nE,
+                                     const int32_t *srcs, const int32_t *dsts,
+                                     double damping, double tol,
+                                     int64_t max_iter, double *rank,
+                                     double *l1_out)
+{
+  orc_graph g;
+  double *r, *rn, *contrib;
+  int64_t it = 0;
+  int32_t v;
+  double l1 = 0.0;
+  if (nV <= 0) { if (l1_out) *l1_out = 0.0; return 0; }
+  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
+  r = (double *)malloc(sizeof(double) * (size_t)nV);
+  rn = (double *)malloc(sizeof(double) * (size_t)nV);
+  contrib = (double *)malloc(sizeof(double) * (size_t)nV);
+  if (!r || !rn || !contrib) {
+    free(r); free(rn); free(contrib); graph_free(&g); return -2;
+  }
+  for (v = 0; v < nV; ++v) r[v] = 1.0 / (double)nV;
+  for (;;) {
+    if (it >= max_iter) { it = -3; break; }
+    for (v = 0; v < nV; ++v) {
+      int64_t od = g.csr_off[v + 1] - g.csr_off[v];
+      contrib[v] = od ? r[v] / (double)od : 0.0;
+    }
+    l1 = 0.0;
+    for (v = 0; v < nV; ++v) {
+      double s = 0.0;
+      int64_t ie;
+      for (ie = g.csc_off[v]; ie < g.csc_off[v + 1]; ++ie)
+        s += contrib[g.csc_src[ie]];
+      rn[v] = (1.0 - damping) / (double)nV + damping * s;
+      l1 += fabs(rn[v] - r[v]);
+    }
+    { double *t = r; r = rn; rn = t; }
+    ++it;
+    if (l1 <= tol) break;
+  }
+  for (v = 0; v < nV; ++v) rank[v] = r[v];
+  if (l1_out) *l1_out = l1;
+  free(r); free(rn); free(contrib);
+  graph_free(&g);
+  return it;
+}
+
+/* One precision-form step on given ranks (FP64), for per-iteration checks
+ * of a GPU step: out[v] = (1-d)/N + d * sum r_u/outdeg(u); returns L1. */
+ORC_EXPORT double orc_pagerank_fp64_step(int32_t nV, int64_t nE,
+                                         const int32_t *srcs,
+                                         const int32_t *dsts, double damping,
+                                         const double *r, double *out)
+{
+  orc_graph g;
+  double l1 = 0.0;
+  int32_t v;
+  if (graph_init(&g, nV, nE, srcs, dsts)) return -1.0;
+  for (v = 0; v < nV; ++v) {
+    double s = 0.0;
+    int64_t ie;
+    for (ie = g.csc_off[v]; ie < g.csc_off[v + 1]; ++ie) {
+      int32_t u = g.csc_src[ie];
+      s += r[u] / (double)(g.csr_off[u + 1] - g.csr_off[u]);
+    }
+    out[v] = (1.0 - damping) / (double)nV + damping * s;
+    l1 += fabs(out[v] - r[v]);
+  }
+  graph_free(&g);
+  return l1;
+}

@@ -1,0 +1,34 @@
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+GOLDEN = ROOT / "tests" / "golden"
+REF_DIR = Path("/root/reference")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); run with -m gpu")
+
+
+def golden_names():
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem != "csr_ties")
+
+
+def load_golden(name):
+    with np.load(GOLDEN / f"{name}.npz") as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.fixture(scope="session")
+def libgas():
+    from graphreduce_gb300.build import build, build_oracle
+    from graphreduce_gb300 import _lib
+    build()
+    build_oracle(with_reference=(REF_DIR / "refgas.h").exists())
+    return _lib.load()

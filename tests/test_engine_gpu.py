@@ -1,0 +1,170 @@
+"""Parity of the CUDA engine (through the C ABI) with the reference's outputs
+and the oracle.  Integer programs: bit-exact, iteration counts included.
+PageRank (reference form): the ordered-fold schedule is bit-exact with the
+oracle; the load-balanced gather differs only in float summation order and
+is held to checkPageRank.py's rule and rtol 1e-5.  Precision-form PageRank:
+L1 error <= 1e-6 against the FP64 oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden_names, load_golden
+from graphreduce_gb300 import GASEngineGPU, GasError, run_program
+from graphreduce_gb300.engine import initial_vertex_data
+from graphreduce_gb300.graph import EdgeList
+from test_oracle import pr_histogram_ok
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_names()
+INT_PROGRAMS = ["bfs", "sssp", "cc"]
+KEY = {"bfs": ("bfs_depth", "bfs_iters"), "sssp": ("sssp_dist", "sssp_iters"),
+       "cc": ("cc_label", "cc_iters")}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(libgas):
+    return libgas
+
+
+def golden_el(g):
+    return EdgeList(int(g["nV"]), g["src"], g["dst"], g["w"])
+
+
+@pytest.mark.parametrize("schedule", ["step", "generic", "ordered"])
+@pytest.mark.parametrize("program", INT_PROGRAMS)
+@pytest.mark.parametrize("name", CASES)
+def test_integer_programs_match_reference(name, program, schedule):
+    g = load_golden(name)
+    vd, it = run_program(program, golden_el(g), int(g["source"]), schedule)
+    out, iters = KEY[program]
+    np.testing.assert_array_equal(vd, g[out])
+    assert it == g[iters]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_pagerank_ordered_is_bitexact_with_oracle(name):
+    g = load_golden(name)
+    el = golden_el(g)
+    vd, it = run_program("pagerank", el, 0, "ordered")
+    rank, oit = oracle.pagerank(el.nV, el.src, el.dst)
+    np.testing.assert_array_equal(vd["rank"], rank)
+    assert it == oit
+    assert pr_histogram_ok(vd["rank"], g["pr_rank"])
+
+
+@pytest.mark.parametrize("schedule", ["step", "generic"])
+@pytest.mark.parametrize("name", CASES)
+def test_pagerank_load_balanced_within_tolerance(name, schedule):
+    g = load_golden(name)
+    vd, it = run_program("pagerank", golden_el(g), 0, schedule)
+    assert pr_histogram_ok(vd["rank"], g["pr_rank"])
+    np.testing.assert_allclose(vd["rank"], g["pr_rank"], rtol=1e-5, atol=1e-5)
+    assert abs(it - int(g["pr_iters"])) <= 1
+
+
+@pytest.mark.parametrize("scale,ef,seed", [(14, 16, 41), (16, 16, 42), (15, 4, 43)])
+def test_random_rmat_against_oracle(scale, ef, seed):
+    el = EdgeList.rmat(scale, ef, seed=seed).with_uniform_weights(1, 64, 3)
+    s = int(el.sample_sources(1, seed)[0])
+    for program in INT_PROGRAMS:
+        if program == "bfs":
+            ref, rit = oracle.bfs(el.nV, el.src, el.dst, s)
+        elif program == "sssp":
+            ref, rit = oracle.sssp(el.nV, el.src, el.dst, el.weights, s)
+        else:
+            ref, rit = oracle.cc(el.nV, el.src, el.dst)
+        for schedule in ("step", "generic"):
+            vd, it = run_program(program, el, s, schedule)
+            np.testing.assert_array_equal(vd, ref, err_msg=f"{program}/{schedule}")
+            assert it == rit, (program, schedule)
+
+
+def test_cc_with_grid_islands_against_oracle():
+    el = EdgeList.rmat(12, 16, seed=2).with_grid_islands(16, 32)
+    ref, rit = oracle.cc(el.nV, el.src, el.dst)
+    vd, it = run_program("cc", el, 0, "generic")
+    np.testing.assert_array_equal(vd, ref)
+    assert it == rit and it >= 62      # a 32x32 grid needs 62 label hops
+
+
+@pytest.mark.parametrize("scale,seed", [(12, 4), (14, 4)])
+def test_pagerank_precision_against_fp64_oracle(scale, seed):
+    el = EdgeList.rmat(scale, 16, seed=seed, symmetrize=False)
+    ref, rit, rl1 = oracle.pagerank_fp64(el.nV, el.src, el.dst, 0.85, 1e-6)
+    eng = GASEngineGPU("pagerank")
+    vd = initial_vertex_data("pagerank", el.nV, 0, el.out_degree())
+    eng.setGraph(el.nV, vd, el.nE, None, el.src, el.dst)
+    ranks, st = eng.pagerank_precision(0.85, 1e-6)
+    err = np.abs(ranks.astype(np.float64) - ref)
+    assert err.sum() <= 1e-6, err.sum()          # L1 error vs FP64
+    assert err.max() <= 1e-7
+    assert abs(st.iterations - rit) <= 1
+    assert st.residual <= 1e-6
+
+
+def test_gather_without_apply_then_scatter():
+    """gather() followed by scatterActivate() without apply(): the reference
+    runs the gather and keeps the previous apply flags."""
+    g = load_golden("rmat8_sym")
+    el = golden_el(g)
+    eng = GASEngineGPU("cc")
+    vd = initial_vertex_data("cc", el.nV)
+    eng.setGraph(el.nV, vd, el.nE, None, el.src, el.dst)
+    eng.setActive(0, el.nV)
+    eng.gather()
+    eng.apply()
+    eng.scatterActivate()
+    n1 = eng.nextIter()
+    eng.gather()
+    eng.scatterActivate()      # no apply: stale flags, no vertex change
+    eng.getResults()
+    assert n1 > 0
+    ref, _ = oracle.cc(el.nV, el.src, el.dst)
+    assert np.all(vd >= ref)
+
+
+def test_setgraph_recall_and_empty_active_set():
+    g = load_golden("rmat10_sym")
+    el = golden_el(g)
+    s = int(g["source"])
+    eng = GASEngineGPU("sssp")
+    for _ in range(2):
+        vd = initial_vertex_data("sssp", el.nV, s)
+        eng.setGraph(el.nV, vd, el.nE, el.weights, el.src, el.dst)
+        eng.setActive(0, el.nV)
+        eng.run_schedule("generic")
+        eng.getResults()
+        np.testing.assert_array_equal(vd, g["sssp_dist"])
+    eng.setActive(5, 5)
+    assert eng.countActive() == 0
+    assert eng.run_schedule("generic").iterations == 0
+
+
+def test_iteration_cap_reports_error_without_fault():
+    el = EdgeList.rmat(10, 16, seed=1).with_grid_islands(2, 16)
+    eng = GASEngineGPU("cc")
+    vd = initial_vertex_data("cc", el.nV)
+    eng.setGraph(el.nV, vd, el.nE, None, el.src, el.dst)
+    eng.setActive(0, el.nV)
+    with pytest.raises(GasError) as ei:
+        eng.run_schedule("generic", max_iterations=3)
+    assert ei.value.status == 4
+    # the context stays usable
+    eng.setActive(0, el.nV)
+    eng.run_schedule("generic")
+
+
+def test_invalid_arguments_raise():
+    g = load_golden("path6")
+    el = golden_el(g)
+    eng = GASEngineGPU("bfs")
+    vd = initial_vertex_data("bfs", el.nV)
+    eng.setGraph(el.nV, vd, el.nE, None, el.src, el.dst)
+    with pytest.raises(GasError):
+        eng.setActive(0, el.nV + 1)
+    with pytest.raises(GasError):
+        eng.setActive(3, 2)
+    e2 = GASEngineGPU("sssp")
+    with pytest.raises(GasError):
+        e2.setGraph(el.nV, initial_vertex_data("sssp", el.nV, 0), el.nE, None, el.src, el.dst)
