@@ -205,6 +205,12 @@ def run_ours(args, rank, world):
         if e2e:
             e_c.download_vertex_data_ptr(res_c.data_ptr(), sp)
 
+    if args.launch_list:
+        # one device-resident step and nothing else (for an ncu launch list)
+        one_step(e2e=False)
+        torch.cuda.synchronize()
+        return {"launch_list": True, "gpu_launches": launches[0]}, None
+
     # correctness of this exact workload + units per step
     one_step(e2e=True)
     torch.cuda.synchronize()
@@ -409,6 +415,8 @@ def main():
     ap.add_argument("--schedule", default="auto",
                     choices=["auto", "generic", "push", "pull", "ordered"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--launch-list", action="store_true",
+                    help="run one device-resident step only (profiling)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -427,7 +435,7 @@ def main():
         dist.init_process_group("nccl")
     result, cpu_inputs = run_ours(args, rank, world)
     if rank == 0:
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and cpu_inputs is not None:
             ssp, sources, out_sssp, first_sssp = cpu_inputs
             import oracle
             from graphreduce_gb300.engine import SSSP_GATHER_ZERO

@@ -51,7 +51,9 @@ class RunStats(C.Structure):
 class Counters(C.Structure):
     _fields_ = [("n_active", c_i32), ("n_edges", c_i32), ("n_scatter_edges", c_i32),
                 ("error", c_i32), ("iteration", c_i32), ("cond", c_i32),
-                ("n_changed", c_i32), ("max_iter", c_i32), ("pad", c_i32 * 8)]
+                ("n_changed", c_i32), ("max_iter", c_i32), ("mode", c_i32),
+                ("n_push", c_i32), ("n_pull", c_i32), ("pull_div", c_i32),
+                ("pad", c_i32 * 4)]
 
 
 # name -> (restype, argtypes); restype "status" means gas_status_t checked.

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -297,11 +298,8 @@ struct ExpandPol {
 };
 
 __global__ void __launch_bounds__(kNT)
-    k_expand(ExpandPol pol, SegSource src, const gas_counters *cnt) {
-  SegSource s = src;
-  s.n_seg = cnt->n_active;
-  s.n_edge = cnt->n_scatter_edges;
-  gasdev::tile_loop<ExpandPol, false, false>(pol, s, nullptr, nullptr, nullptr);
+    k_expand(ExpandPol pol, SegSource src) {
+  gasdev::tile_loop<ExpandPol, false, false>(pol, src, nullptr, nullptr, nullptr);
 }
 
 // Compaction of the next-frontier bitmap into the ascending active list with
@@ -461,9 +459,12 @@ void free_graph(gas_engine *e) {
   dfree(e->vd); dfree(e->act); dfree(e->scan); dfree(e->sscan); dfree(e->ret);
   dfree(e->slot); dfree(e->gres); dfree(e->bits);
   dfree(e->tile_first); dfree(e->tile_carry); dfree(e->tile_a0);
+  dfree(e->tpart); dfree(e->dpart);
   dfree(e->ppart); dfree(e->cpart); dfree(e->cnt);
   for (int i = 0; i < 2; ++i) { dfree(e->pr_rank[i]); dfree(e->pr_contrib[i]); }
   dfree(e->pr_inv_deg); dfree(e->pr_l1);
+  dfree(e->q_ids); dfree(e->q_vals); dfree(e->q_scan); dfree(e->snap);
+  dfree(e->qpart); dfree(e->cbits); dfree(e->mbits);
   for (int i = 0; i < kGraphSlots; ++i) {
     if (e->graphs[i]) cudaGraphExecDestroy(e->graphs[i]);
     e->graphs[i] = nullptr;
@@ -526,21 +527,24 @@ gas_status_t launch_generic_gather(gas_engine *e, bool fuse, bool ordered,
     CUDA_TRY(cudaGetLastError());
     return GAS_OK;
   }
-  SegSource src{e->act, e->scan, e->csc_off, e->n_active, e->n_edges};
+  const SegSource src = gasdev::frontier_source(
+      e->act, e->scan, e->csc_off, &e->cnt->n_active, &e->cnt->n_edges, e->tpart);
   constexpr int kTile = gasdev::TileShape<sizeof(GR)>::kTile;
   const int64_t items = (int64_t)e->n_active + e->n_edges;
+  gasdev::k_partition<kTile, false>
+      <<<gas::engine_partition_grid(e, items, kTile), 256, 0, S(stream)>>>(src, e->tpart);
   const int cap = occupancy_grid(e, gasdev::k_gather_tiles<P>);
   const int grid = e->capturing ? cap : grid_for(items, kTile, cap);
   gasdev::k_gather_tiles<P><<<grid, kNT, 0, S(stream)>>>(
       pol, src, static_cast<GR *>(e->tile_first),
-      static_cast<GR *>(e->tile_carry), e->tile_a0, e->cnt);
+      static_cast<GR *>(e->tile_carry), e->tile_a0);
   CUDA_TRY(cudaGetLastError());
   const int64_t ntiles = (items + kTile - 1) / kTile;
   const int fgrid = e->capturing ? 4 * e->num_sms
                                   : grid_for(ntiles, kNT / 32, 4 * e->num_sms);
   gasdev::k_gather_fixup<P><<<fgrid, kNT, 0, S(stream)>>>(
       pol, src, static_cast<GR *>(e->tile_first),
-      static_cast<GR *>(e->tile_carry), e->tile_a0, e->cnt);
+      static_cast<GR *>(e->tile_carry), e->tile_a0);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -605,8 +609,14 @@ gas_status_t scatter_common(gas_engine *e, void *stream) {
                                              e->ppart, e->sscan);
   CUDA_TRY(cudaGetLastError());
   ExpandPol pol{e->csr_dst, e->bits};
-  SegSource src{e->act, e->sscan, e->csr_off, 0, 0};
-  k_expand<<<occupancy_grid(e, k_expand), kNT, 0, S(stream)>>>(pol, src, e->cnt);
+  const SegSource src = gasdev::frontier_source(
+      e->act, e->sscan, e->csr_off, &e->cnt->n_active, &e->cnt->n_scatter_edges,
+      e->tpart);
+  constexpr int kTile = gasdev::TileShape<sizeof(int32_t)>::kTile;
+  // the scatter edge count is only known on the device: fixed grids
+  gasdev::k_partition<kTile, false>
+      <<<gas::engine_partition_grid(e, -1, kTile), 256, 0, S(stream)>>>(src, e->tpart);
+  k_expand<<<occupancy_grid(e, k_expand), kNT, 0, S(stream)>>>(pol, src);
   CUDA_TRY(cudaGetLastError());
   const int nW = (e->nV + 31) / 32;
   k_compact_count<<<e->n_cblocks, kNT, 0, S(stream)>>>(e->bits, e->csc_off, nW,
@@ -667,6 +677,10 @@ gas_status_t gas_engine_create(gas_program_t program, gas_engine **out) {
   e->vbytes = program_vbytes(program);
   e->gbytes = 4;
   e->ebytes = 4;
+  if (const char *pd = getenv("GAS_PULL_DIV")) {
+    const int v = atoi(pd);
+    if (v > 0) e->pull_div = v;
+  }
   *out = e;  // CUDA is first touched by set_graph
   return GAS_OK;
 }
@@ -775,6 +789,8 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   GAS_TRY(dalloc((uint8_t **)&e->tile_first, (size_t)e->tile_cap * tv));
   GAS_TRY(dalloc((uint8_t **)&e->tile_carry, (size_t)e->tile_cap * tv));
   GAS_TRY(dalloc(&e->tile_a0, (size_t)e->tile_cap));
+  GAS_TRY(dalloc(&e->tpart, (size_t)e->tile_cap + 2));
+  GAS_TRY(dalloc(&e->dpart, (size_t)e->tile_cap + 2));
   GAS_TRY(dalloc(&e->ppart, (V + kScanBlock - 1) / kScanBlock + 1));
   e->n_cblocks = (int32_t)std::max<size_t>(1, (nW + kCompactBlock - 1) / kCompactBlock);
   GAS_TRY(dalloc(&e->cpart, 2 * (size_t)e->n_cblocks));
@@ -961,6 +977,7 @@ gas_status_t gas_engine_view_get(gas_engine *e, gas_engine_view *v) {
   v->tile_first = e->tile_first;
   v->tile_carry = e->tile_carry;
   v->tile_a0 = e->tile_a0;
+  v->tile_part = e->tpart;
   v->tile_cap = e->tile_cap;
   v->num_sms = e->num_sms;
   v->counters = e->cnt;
@@ -997,6 +1014,29 @@ gas_status_t engine_sync_counts(gas_engine *e, void *stream) {
 }
 int engine_grid(int64_t work_items, int per_block, int cap) {
   return grid_for(work_items, per_block, cap);
+}
+int engine_partition_grid(gas_engine *e, int64_t items, int tile) {
+  const int cap = 2 * e->num_sms;
+  if (e->capturing || items < 0) return cap;
+  return grid_for((items + tile - 1) / tile + 1, 256, cap);
+}
+
+gas_status_t engine_gather_apply(gas_engine *e, void *stream) {
+  GAS_TRY(builtin_gather(e, true, false, stream));
+  e->slots_pending = true;
+  return GAS_OK;
+}
+gas_status_t engine_apply_only(gas_engine *e, void *stream) {
+  return builtin_apply_only(e, stream);
+}
+gas_status_t engine_commit(gas_engine *e, void *stream) {
+  const int g = e->capturing ? 8 * e->num_sms
+                             : grid_for(e->n_active, kNT, 8 * e->num_sms);
+  k_commit<<<g, kNT, 0, S(stream)>>>(e->act, e->cnt, (const uint8_t *)e->slot,
+                                     (uint8_t *)e->vd, (int)e->vbytes);
+  CUDA_TRY(cudaGetLastError());
+  e->slots_pending = false;
+  return GAS_OK;
 }
 
 gas_status_t engine_generic_iteration(gas_engine *e, bool ordered, void *stream) {

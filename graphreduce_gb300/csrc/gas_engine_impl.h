@@ -53,6 +53,8 @@ struct gas_engine {
   void *tile_first = nullptr, *tile_carry = nullptr;
   int32_t *tile_a0 = nullptr;
   int32_t tile_cap = 0;
+  int32_t *tpart = nullptr;  // tile partitions of the current frontier pass
+  int32_t *dpart = nullptr;  // tile partitions of the dense CSC (pull passes)
   int32_t *ppart = nullptr;  // predicated-scan partials
   int32_t *cpart = nullptr;  // compaction partials (pairs)
   int32_t n_cblocks = 0;
@@ -66,6 +68,14 @@ struct gas_engine {
   double *pr_l1 = nullptr;
   int32_t pr_l1_cap = 0;
   double pr_damping = 0.0;
+
+  // fast-schedule state (lazily allocated): frontier queue of C_k with the
+  // values its members had at the end of iteration k, out-degree scan,
+  // changed bitmap (being built), membership bitmap of C_k, snapshots
+  int32_t *q_ids = nullptr, *q_vals = nullptr, *q_scan = nullptr;
+  int32_t *snap = nullptr, *qpart = nullptr;
+  uint32_t *cbits = nullptr, *mbits = nullptr;
+  int32_t pull_div = 4;
 
   // host view of the step API state
   int32_t n_active = 0, n_edges = 0;
@@ -86,9 +96,15 @@ namespace gas {
 gas_status_t engine_scatter(gas_engine *e, void *stream);
 // one bulk-synchronous iteration of the generic (step API) kernels
 gas_status_t engine_generic_iteration(gas_engine *e, bool ordered, void *stream);
+// pieces of it: fused gather+apply into slots / apply only / commit slots
+gas_status_t engine_gather_apply(gas_engine *e, void *stream);
+gas_status_t engine_apply_only(gas_engine *e, void *stream);
+gas_status_t engine_commit(gas_engine *e, void *stream);
 // host copy of the counters (synchronises the stream)
 gas_status_t engine_sync_counts(gas_engine *e, void *stream);
 int engine_grid(int64_t work_items, int per_block, int cap);
+// grid of a k_partition launch (fixed while capturing)
+int engine_partition_grid(gas_engine *e, int64_t items, int tile);
 }  // namespace gas
 
 #endif  // GAS_ENGINE_IMPL_H_

@@ -140,7 +140,10 @@ extern "C" gas_status_t gas_engine_run_schedule(gas_engine *e,
   if (!e || !e->has_graph) return gas::fail(GAS_ERR_STATE, "run before set_graph");
   if (e->prog == GAS_PROG_USER)
     return gas::fail(GAS_ERR_UNSUPPORTED, "user programs run through gpugas.h");
-  if (max_iterations <= 0) max_iterations = INT_MAX;
+  // default cap: nV + 2 bounds every correct BFS / SSSP / CC run (each
+  // iteration settles at least one more vertex); PageRank gets 100000
+  if (max_iterations <= 0)
+    max_iterations = e->prog == GAS_PROG_PAGERANK ? 100000 : e->nV + 2;
   if (stats) *stats = gas_run_stats{};
   int32_t n = 0;
   GAS_TRY(gas_engine_count_active(e, &n));
@@ -368,7 +371,7 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
   c.bufs.rank[1] = e->pr_rank[1];
   c.bufs.contrib[0] = e->pr_contrib[0];
   c.bufs.contrib[1] = e->pr_contrib[1];
-  c.src = SegSource{nullptr, nullptr, e->csc_off, nV, e->nE};
+  c.src = gasdev::dense_source(e->csc_off, nV, e->nE, e->dpart);
 
   // damping is baked into the captured policy: rebuild when it changes
   if (e->graphs[kGraphPagerank] && e->pr_damping != damping) {
@@ -381,6 +384,12 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
   }
   CUDA_TRY(cudaMemcpyAsync(c.residual + 1, &tol, sizeof(double),
                            cudaMemcpyHostToDevice, S(stream)));
+  {
+    constexpr int kTile = gasdev::TileShape<sizeof(PrVal)>::kTile;
+    const int64_t items = (int64_t)nV + e->nE;
+    gasdev::k_partition<kTile, true>
+        <<<gas::engine_partition_grid(e, items, kTile), 256, 0, S(stream)>>>(c.src, e->dpart);
+  }
   k_pr_init<<<gas::engine_grid(nV, kNT, 8 * e->num_sms), kNT, 0, S(stream)>>>(
       e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV));
   k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);

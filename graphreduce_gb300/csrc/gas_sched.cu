@@ -1,19 +1,603 @@
-// gas_sched.cu -- fast schedules of the built-in programs.
+// gas_sched.cu -- fast schedules of the built-in programs (BFS, SSSP, CC).
+//
+// The reference iterates "pull over the active set": A_{k+1} = out-neighbours
+// of C_k, the vertices whose apply() returned true, and every active vertex
+// folds all of its in-edges (refgas.h:143-214).  For the monotone min
+// programs the same vertex data, the same C_k and the same iteration count
+// come out of cheaper schedules:
+//
+//   iteration 0   the generic kernels on the caller's active set (exact);
+//   push          every u in C_k sends d_u (+ w) along its out-edges with
+//                 atomicMin; v joins C_{k+1} iff a send lowered it.  The d_u
+//                 sent are the values at the end of iteration k, captured in
+//                 the frontier queue, so the iteration stays bulk-synchronous;
+//   dense pull    every vertex folds its in-edges from C_k (bitmap test,
+//                 snapshot values), for frontiers whose out-edges are a large
+//                 share of the graph.
+//
+// Why push == pull: after every iteration each edge u->v satisfies
+// d_v <= d_u + w unless u is in C_k (induction from iteration 0, which folds
+// every in-edge), so in-neighbours outside C_k can neither lower d_v nor make
+// apply() return true.  Iteration k+1 exists iff C_k has an out-edge.
+//
+// BFS (bfs.cu:58-71): C_k = vertices first reached at level k; push marks
+// unvisited out-neighbours with atomicCAS.
+//
+// The whole run is one CUDA graph: the iteration-0 kernels, a kernel that
+// sets the loop condition, then a WHILE node whose body runs push or pull
+// (each kernel returns at once when the other mode is selected), the
+// frontier compaction and the condition kernel, which also picks the next
+// iteration's mode.
 #include <cuda_runtime.h>
 
+#include <climits>
+#include <vector>
+
 #include "gas.h"
+#include "gas_device.cuh"
 #include "gas_engine_impl.h"
 #include "gas_internal.h"
 #include "gas_sched.h"
 
+using gasdev::kNT;
+using gasdev::SegSource;
+
+namespace {
+
+inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+constexpr int kWordsPerThread = 4;
+constexpr int kCompactBlock = kNT * kWordsPerThread;  // bitmap words per block
+
+enum { kModePush = 0, kModePull = 1 };
+
+__device__ __forceinline__ int cta_excl_sum(int v, int *total) {
+  __shared__ int s_w[kNT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int o = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += o;
+  }
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  int pre = 0, tot = 0;
+  for (int w = 0; w < kNT / 32; ++w) {
+    if (w < warp) pre += s_w[w];
+    tot += s_w[w];
+  }
+  __syncthreads();
+  *total = tot;
+  return pre + incl - v;
+}
+
+// ---------------------------------------------------------------------------
+// iteration 0 -> the changed set
+// ---------------------------------------------------------------------------
+__global__ void k_seed_changed(const int32_t *act, const uint8_t *ret,
+                               const gas_counters *cnt, uint32_t *cbits) {
+  const int n = cnt->n_active;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    if (ret[i]) {
+      const uint32_t v = (uint32_t)act[i];
+      atomicOr(cbits + (v >> 5), 1u << (v & 31));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// frontier compaction: changed bitmap -> queue (id, value), out-degree scan;
+// the bitmap moves to mbits (membership of C_k for the dense pull)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void qword_stats(const uint32_t *bits,
+                                            const int32_t *csr_off, int nW,
+                                            int w, int *c, int *d) {
+  *c = 0;
+  *d = 0;
+  if (w >= nW) return;
+  uint32_t m = bits[w];
+  *c = __popc(m);
+  while (m) {
+    const int b = __ffs(m) - 1;
+    m &= m - 1;
+    const int v = w * 32 + b;
+    *d += csr_off[v + 1] - csr_off[v];
+  }
+}
+
+__global__ void __launch_bounds__(kNT)
+    k_q_count(const uint32_t *cbits, const int32_t *csr_off, int nW,
+              int32_t *part) {
+  int c = 0, d = 0;
+  const int w0 = blockIdx.x * kCompactBlock + threadIdx.x * kWordsPerThread;
+  for (int k = 0; k < kWordsPerThread; ++k) {
+    int cc, dd;
+    qword_stats(cbits, csr_off, nW, w0 + k, &cc, &dd);
+    c += cc;
+    d += dd;
+  }
+  int tc, td;
+  cta_excl_sum(c, &tc);
+  cta_excl_sum(d, &td);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = tc;
+    part[2 * blockIdx.x + 1] = td;
+  }
+}
+
+__global__ void __launch_bounds__(kNT)
+    k_q_spine(int32_t *part, int nb, gas_counters *cnt) {
+  __shared__ int s_carry[2];
+  if (threadIdx.x < 2) s_carry[threadIdx.x] = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += kNT) {
+    const int i = base + threadIdx.x;
+    const int vc = i < nb ? part[2 * i] : 0;
+    const int vd = i < nb ? part[2 * i + 1] : 0;
+    int tc, td;
+    const int ec = cta_excl_sum(vc, &tc);
+    const int ed = cta_excl_sum(vd, &td);
+    const int cc = s_carry[0], cd = s_carry[1];
+    if (i < nb) {
+      part[2 * i] = cc + ec;
+      part[2 * i + 1] = cd + ed;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_carry[0] = cc + tc;
+      s_carry[1] = cd + td;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    cnt->n_changed = s_carry[0];
+    cnt->n_scatter_edges = s_carry[1];
+  }
+}
+
+__global__ void __launch_bounds__(kNT)
+    k_q_write(uint32_t *cbits, uint32_t *mbits, const int32_t *csr_off, int nW,
+              const int32_t *part, const int32_t *vd, int32_t *q_ids,
+              int32_t *q_vals, int32_t *q_scan, int32_t *snap,
+              const gas_counters *cnt) {
+  const int w0 = blockIdx.x * kCompactBlock + threadIdx.x * kWordsPerThread;
+  int c = 0, d = 0;
+  for (int k = 0; k < kWordsPerThread; ++k) {
+    int cc, dd;
+    qword_stats(cbits, csr_off, nW, w0 + k, &cc, &dd);
+    c += cc;
+    d += dd;
+  }
+  int tc, td;
+  int pc = cta_excl_sum(c, &tc) + part[2 * blockIdx.x];
+  int pd = cta_excl_sum(d, &td) + part[2 * blockIdx.x + 1];
+  for (int k = 0; k < kWordsPerThread; ++k) {
+    const int w = w0 + k;
+    if (w >= nW) break;
+    uint32_t m = cbits[w];
+    mbits[w] = m;
+    if (!m) continue;
+    cbits[w] = 0;
+    while (m) {
+      const int bit = __ffs(m) - 1;
+      m &= m - 1;
+      const int v = w * 32 + bit;
+      const int val = vd[v];
+      q_ids[pc] = v;
+      q_vals[pc] = val;
+      q_scan[pc] = pd;
+      snap[v] = val;
+      ++pc;
+      pd += csr_off[v + 1] - csr_off[v];
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) q_scan[cnt->n_changed] = cnt->n_scatter_edges;
+}
+
+// ---------------------------------------------------------------------------
+// push (SSSP / CC) and BFS push
+// ---------------------------------------------------------------------------
+template <bool kWeighted>
+struct PushPol {
+  typedef int32_t Val;
+  const int32_t *csr_dst;
+  const int32_t *csr_w;
+  const int32_t *q_vals;
+  int32_t *vd;
+  uint32_t *cbits;
+  int32_t zero_cap;  // Program::gatherZero: gather results never exceed it
+  __device__ Val zero() const { return 0; }
+  __device__ Val reduce(Val a, Val) const { return a; }
+  __device__ Val map(int, int, int) const { return 0; }
+  __device__ void emit(int, int, Val) const {}
+  __device__ __forceinline__ void visit(int a, int, int pos) const {
+    const int v = __ldg(csr_dst + pos);
+    int cand = __ldg(q_vals + a);
+    if (kWeighted) cand += __ldg(csr_w + pos);
+    if (cand > zero_cap) cand = zero_cap;
+    if (cand < *(volatile const int32_t *)(vd + v)) {
+      const int old = atomicMin(vd + v, cand);
+      if (cand < old) atomicOr(cbits + ((uint32_t)v >> 5), 1u << (v & 31));
+    }
+  }
+};
+
+struct BfsPushPol {
+  typedef int32_t Val;
+  const int32_t *csr_dst;
+  int32_t *depth;
+  uint32_t *cbits;
+  int32_t level;
+  __device__ Val zero() const { return 0; }
+  __device__ Val reduce(Val a, Val) const { return a; }
+  __device__ Val map(int, int, int) const { return 0; }
+  __device__ void emit(int, int, Val) const {}
+  __device__ __forceinline__ void visit(int, int, int pos) const {
+    const int v = __ldg(csr_dst + pos);
+    if (*(volatile const int32_t *)(depth + v) == -1 &&
+        atomicCAS(depth + v, -1, level) == -1)
+      atomicOr(cbits + ((uint32_t)v >> 5), 1u << (v & 31));
+  }
+};
+
+template <class Pol>
+__global__ void __launch_bounds__(kNT)
+    k_push(Pol pol, SegSource src, const gas_counters *cnt) {
+  if (cnt->mode != kModePush) return;
+  gasdev::tile_loop<Pol, false, false>(pol, src, nullptr, nullptr, nullptr);
+}
+
+__global__ void __launch_bounds__(kNT)
+    k_bfs_push(BfsPushPol pol, SegSource src, const gas_counters *cnt) {
+  if (cnt->mode != kModePush) return;
+  pol.level = cnt->iteration;
+  gasdev::tile_loop<BfsPushPol, false, false>(pol, src, nullptr, nullptr, nullptr);
+}
+
+// Tile boundaries of the frontier queue, only when this iteration pushes.
+__global__ void __launch_bounds__(256)
+    k_push_partition(SegSource src, int32_t *part, const gas_counters *cnt) {
+  if (cnt->mode != kModePush) return;
+  constexpr int kTile = gasdev::TileShape<sizeof(int32_t)>::kTile;
+  int nA, E;
+  gasdev::seg_sizes(src, nA, E);
+  const int64_t M = (int64_t)nA + E;
+  const int ntiles = (int)((M + kTile - 1) / kTile);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles;
+       t += gridDim.x * blockDim.x) {
+    const int64_t d = (int64_t)t * kTile < M ? (int64_t)t * kTile : M;
+    part[t] = gasdev::merge_path(src.scan + 1, nA, E, (int)d);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dense pull (SSSP / CC): every vertex folds the in-edges from C_k
+// ---------------------------------------------------------------------------
+template <bool kWeighted>
+struct PullPol {
+  typedef int32_t Val;
+  const int32_t *csc_src;
+  const int32_t *csc_w;
+  const uint32_t *mbits;
+  const int32_t *snap;
+  int32_t *vd;
+  uint32_t *cbits;
+  int32_t zero_cap;
+  __device__ Val zero() const { return INT_MAX; }
+  __device__ __forceinline__ Val reduce(Val a, Val b) const { return a < b ? a : b; }
+  __device__ __forceinline__ Val map(int, int, int pos) const {
+    const uint32_t u = (uint32_t)__ldg(csc_src + pos);
+    if (!((__ldg(mbits + (u >> 5)) >> (u & 31)) & 1u)) return INT_MAX;
+    int c = __ldg(snap + u);
+    if (kWeighted) c += __ldg(csc_w + pos);
+    return c > zero_cap ? zero_cap : c;
+  }
+  __device__ __forceinline__ void emit(int, int v, Val g) const {
+    if (g < vd[v]) {
+      vd[v] = g;
+      atomicOr(cbits + ((uint32_t)v >> 5), 1u << (v & 31));
+    }
+  }
+};
+
+template <class Pol>
+__global__ void __launch_bounds__(kNT)
+    k_pull(Pol pol, SegSource src, int32_t *tf, int32_t *tc, int32_t *ta0,
+           const gas_counters *cnt) {
+  if (cnt->mode != kModePull) return;
+  gasdev::tile_loop<Pol, true, true>(pol, src, tf, tc, ta0);
+}
+
+template <class Pol>
+__global__ void __launch_bounds__(kNT)
+    k_pull_fixup(Pol pol, SegSource src, const int32_t *tf, const int32_t *tc,
+                 const int32_t *ta0, const gas_counters *cnt) {
+  if (cnt->mode != kModePull) return;
+  gasdev::fixup_loop<Pol, true>(pol, src, tf, tc, ta0);
+}
+
+// ---------------------------------------------------------------------------
+// loop control
+// ---------------------------------------------------------------------------
+// Mode of the next iteration: AUTO pulls when the frontier's out-edges are
+// more than 1/pull_div of all edges.
+__device__ __forceinline__ void pick_mode(gas_counters *cnt, int nE) {
+  const int forced = cnt->pad[0];  // 0 auto, 1 push, 2 pull
+  int mode;
+  if (forced == 1)
+    mode = kModePush;
+  else if (forced == 2)
+    mode = kModePull;
+  else
+    mode = ((long long)cnt->n_scatter_edges * cnt->pull_div > (long long)nE)
+               ? kModePull : kModePush;
+  cnt->mode = mode;
+}
+
+__global__ void k_fast_precond(gas_counters *cnt, cudaGraphConditionalHandle h,
+                               int nE) {
+  cnt->iteration = 1;  // iteration 0 ran in the prologue
+  const bool more = cnt->n_scatter_edges > 0;
+  if (more && 1 >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
+  cnt->cond = (more && 1 < cnt->max_iter) ? 1 : 0;
+  pick_mode(cnt, nE);
+  cudaGraphSetConditional(h, cnt->cond);
+}
+
+__global__ void k_fast_cond(gas_counters *cnt, cudaGraphConditionalHandle h,
+                            int nE) {
+  if (cnt->mode == kModePush)
+    ++cnt->n_push;
+  else
+    ++cnt->n_pull;
+  const int it = ++cnt->iteration;
+  const bool more = cnt->n_scatter_edges > 0;
+  if (more && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
+  cnt->cond = (more && it < cnt->max_iter) ? 1 : 0;
+  pick_mode(cnt, nE);
+  cudaGraphSetConditional(h, cnt->cond);
+}
+
+__global__ void k_fast_reset(gas_counters *cnt, int max_iter, int forced,
+                             int pull_div) {
+  cnt->iteration = 0;
+  cnt->error = 0;
+  cnt->max_iter = max_iter;
+  cnt->n_push = 0;
+  cnt->n_pull = 0;
+  cnt->pad[0] = forced;
+  cnt->pull_div = pull_div;
+  cnt->mode = kModePush;
+}
+
+__global__ void k_fast_finish(gas_counters *cnt) {
+  // the reference's active set is empty after run()
+  if (!cnt->error) cnt->n_active = 0;
+}
+
+struct FastCtx {
+  int nW;
+  int n_qblocks;
+};
+
+gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c) {
+  k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart);
+  k_q_spine<<<1, kNT, 0, cs>>>(e->qpart, c.n_qblocks, e->cnt);
+  k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->mbits, e->csr_off, c.nW,
+                                         e->qpart, (const int32_t *)e->vd,
+                                         e->q_ids, e->q_vals, e->q_scan,
+                                         e->snap, e->cnt);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t prologue(gas_engine *e, cudaStream_t cs, void *vctx) {
+  const FastCtx &c = *static_cast<const FastCtx *>(vctx);
+  // iteration 0: the generic kernels on the caller's active set
+  e->level_from_counters = true;
+  if (e->prog == GAS_PROG_BFS) {
+    GAS_TRY(gas::engine_apply_only(e, cs));
+  } else {
+    GAS_TRY(gas::engine_gather_apply(e, cs));
+    GAS_TRY(gas::engine_commit(e, cs));
+  }
+  e->level_from_counters = false;
+  k_seed_changed<<<8 * e->num_sms, kNT, 0, cs>>>(e->act, e->ret, e->cnt, e->cbits);
+  CUDA_TRY(cudaGetLastError());
+  if (e->prog != GAS_PROG_BFS) {  // tile boundaries of the dense pull
+    constexpr int kTile = gasdev::TileShape<sizeof(int32_t)>::kTile;
+    gasdev::k_partition<kTile, true><<<2 * e->num_sms, 256, 0, cs>>>(
+        gasdev::dense_source(e->csc_off, e->nV, e->nE, e->dpart), e->dpart);
+  }
+  return compaction(e, cs, c);
+}
+
+gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
+                  void *vctx) {
+  const FastCtx &c = *static_cast<const FastCtx *>(vctx);
+  const SegSource qsrc = gasdev::frontier_source(
+      e->q_ids, e->q_scan, e->csr_off, &e->cnt->n_changed,
+      &e->cnt->n_scatter_edges, e->tpart);
+  k_push_partition<<<2 * e->num_sms, 256, 0, cs>>>(qsrc, e->tpart, e->cnt);
+  int per_sm = 0;
+  const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
+  if (e->prog == GAS_PROG_BFS) {
+    BfsPushPol pol{e->csr_dst, (int32_t *)e->vd, e->cbits, 0};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_push, kNT, 0);
+    k_bfs_push<<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(pol, qsrc, e->cnt);
+  } else if (e->prog == GAS_PROG_SSSP) {
+    PushPol<true> pol{e->csr_dst, (const int32_t *)e->csr_ed, e->q_vals,
+                      (int32_t *)e->vd, e->cbits, zero_cap};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_push<PushPol<true>>, kNT, 0);
+    k_push<PushPol<true>><<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(
+        pol, qsrc, e->cnt);
+    PullPol<true> pp{e->csc_src, (const int32_t *)e->csc_ed, e->mbits, e->snap,
+                     (int32_t *)e->vd, e->cbits, zero_cap};
+    const SegSource dsrc = gasdev::dense_source(e->csc_off, e->nV, e->nE, e->dpart);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<PullPol<true>>, kNT, 0);
+    k_pull<PullPol<true>><<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(
+        pp, dsrc, (int32_t *)e->tile_first, (int32_t *)e->tile_carry, e->tile_a0, e->cnt);
+    k_pull_fixup<PullPol<true>><<<4 * e->num_sms, kNT, 0, cs>>>(
+        pp, dsrc, (const int32_t *)e->tile_first, (const int32_t *)e->tile_carry,
+        e->tile_a0, e->cnt);
+  } else {
+    PushPol<false> pol{e->csr_dst, nullptr, e->q_vals, (int32_t *)e->vd, e->cbits,
+                       zero_cap};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_push<PushPol<false>>, kNT, 0);
+    k_push<PushPol<false>><<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(
+        pol, qsrc, e->cnt);
+    PullPol<false> pp{e->csc_src, nullptr, e->mbits, e->snap, (int32_t *)e->vd,
+                      e->cbits, zero_cap};
+    const SegSource dsrc = gasdev::dense_source(e->csc_off, e->nV, e->nE, e->dpart);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<PullPol<false>>, kNT, 0);
+    k_pull<PullPol<false>><<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(
+        pp, dsrc, (int32_t *)e->tile_first, (int32_t *)e->tile_carry, e->tile_a0, e->cnt);
+    k_pull_fixup<PullPol<false>><<<4 * e->num_sms, kNT, 0, cs>>>(
+        pp, dsrc, (const int32_t *)e->tile_first, (const int32_t *)e->tile_carry,
+        e->tile_a0, e->cnt);
+  }
+  CUDA_TRY(cudaGetLastError());
+  GAS_TRY(compaction(e, cs, c));
+  k_fast_cond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t ensure_fast_buffers(gas_engine *e) {
+  if (e->q_ids) return GAS_OK;
+  const size_t V = (size_t)e->nV, nW = (V + 31) / 32;
+  const size_t nqb = (nW + kCompactBlock - 1) / kCompactBlock;
+  CUDA_TRY(cudaMalloc(&e->q_ids, (V ? V : 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->q_vals, (V ? V : 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->q_scan, (V + 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->snap, (V ? V : 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->cbits, (nW ? nW : 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->mbits, (nW ? nW : 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->qpart, 2 * (nqb ? nqb : 1) * 4));
+  CUDA_TRY(cudaMemset(e->cbits, 0, (nW ? nW : 1) * 4));
+  CUDA_TRY(cudaMemset(e->mbits, 0, (nW ? nW : 1) * 4));
+  return GAS_OK;
+}
+
+}  // namespace
+
 namespace gas {
+
+// WHILE graph with a captured prologue before the loop node.
+static gas_status_t build_fast_graph(gas_engine *e, FastCtx *ctx,
+                                     cudaGraphExec_t *out) {
+  cudaGraph_t g = nullptr;
+  cudaStream_t cs = nullptr;
+  gas_status_t st = GAS_OK;
+  CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t ce = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  std::vector<cudaGraphNode_t> deps;
+  if (ce == cudaSuccess)
+    ce = cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+  if (ce != cudaSuccess) {
+    if (cs) cudaStreamDestroy(cs);
+    cudaGraphDestroy(g);
+    return fail(GAS_ERR_CUDA, "fast graph setup: %s", cudaGetErrorString(ce));
+  }
+  e->capturing = true;
+  st = prologue(e, cs, ctx);
+  if (st == GAS_OK) {
+    k_fast_precond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE);
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) st = fail(GAS_ERR_CUDA, "precond: %s", cudaGetErrorString(ce));
+  }
+  if (st == GAS_OK) {
+    cudaStreamCaptureStatus cst;
+    const cudaGraphNode_t *d = nullptr;
+    size_t nd = 0;
+    ce = cudaStreamGetCaptureInfo(cs, &cst, nullptr, nullptr, &d, nullptr, &nd);
+    if (ce == cudaSuccess) deps.assign(d, d + nd);
+    else st = fail(GAS_ERR_CUDA, "capture info: %s", cudaGetErrorString(ce));
+  }
+  e->capturing = false;
+  cudaGraph_t cap = nullptr;
+  ce = cudaStreamEndCapture(cs, &cap);
+  if (st == GAS_OK && ce != cudaSuccess)
+    st = fail(GAS_ERR_CUDA, "end capture: %s", cudaGetErrorString(ce));
+  if (st == GAS_OK) {
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    ce = cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &p);
+    if (ce != cudaSuccess) {
+      st = fail(GAS_ERR_CUDA, "add while node: %s", cudaGetErrorString(ce));
+    } else {
+      cudaGraph_t bodyg = p.conditional.phGraph_out[0];
+      ce = cudaStreamBeginCaptureToGraph(cs, bodyg, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeRelaxed);
+      if (ce != cudaSuccess) {
+        st = fail(GAS_ERR_CUDA, "body capture: %s", cudaGetErrorString(ce));
+      } else {
+        e->capturing = true;
+        st = body(e, cs, h, ctx);
+        e->capturing = false;
+        cudaGraph_t bc = nullptr;
+        ce = cudaStreamEndCapture(cs, &bc);
+        if (st == GAS_OK && ce != cudaSuccess)
+          st = fail(GAS_ERR_CUDA, "end body capture: %s", cudaGetErrorString(ce));
+      }
+    }
+  }
+  if (st == GAS_OK) {
+    ce = cudaGraphInstantiate(out, g, 0);
+    if (ce != cudaSuccess) st = fail(GAS_ERR_CUDA, "instantiate: %s", cudaGetErrorString(ce));
+  }
+  cudaStreamDestroy(cs);
+  cudaGraphDestroy(g);
+  return st;
+}
 
 gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
                       int32_t max_iterations, gas_run_stats *stats,
                       void *stream) {
-  (void)schedule;
-  return gas_engine_run_schedule(e, GAS_SCHED_GENERIC, max_iterations, stats,
-                                 stream);
+  if (e->prog == GAS_PROG_PAGERANK)  // not monotone: the generic kernels
+    return gas_engine_run_schedule(e, GAS_SCHED_GENERIC, max_iterations, stats, stream);
+  if (e->prog == GAS_PROG_BFS && schedule == GAS_SCHED_PULL) schedule = GAS_SCHED_PUSH;
+  GAS_TRY(ensure_fast_buffers(e));
+  FastCtx ctx;
+  ctx.nW = (e->nV + 31) / 32;
+  ctx.n_qblocks = (ctx.nW + kCompactBlock - 1) / kCompactBlock;
+  if (ctx.n_qblocks < 1) ctx.n_qblocks = 1;
+  const int slot = kGraphFast0;
+  if (!e->graphs[slot]) GAS_TRY(build_fast_graph(e, &ctx, &e->graphs[slot]));
+  const int forced = schedule == GAS_SCHED_PUSH ? 1 : schedule == GAS_SCHED_PULL ? 2 : 0;
+  k_fast_reset<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations, forced, e->pull_div);
+  cudaError_t ce = cudaGetLastError();
+  if (ce == cudaSuccess) ce = cudaGraphLaunch(e->graphs[slot], S(stream));
+  if (ce == cudaSuccess) {
+    k_fast_finish<<<1, 1, 0, S(stream)>>>(e->cnt);
+    ce = cudaGetLastError();
+  }
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(stream));
+  if (ce != cudaSuccess) return fail(GAS_ERR_CUDA, "fast run: %s", cudaGetErrorString(ce));
+  gas_counters c;
+  GAS_TRY(engine_sync_counts(e, stream));
+  c = *e->h_cnt;
+  if (stats) {
+    stats->iterations = c.iteration;
+    stats->push_iters = c.n_push;
+    stats->pull_iters = c.n_pull;
+    // prologue (gather/apply, fixup, commit | bfs apply; seed; 3 compaction;
+    // precond) + per iteration (push, pull, pull fixup | bfs push;
+    // 3 compaction; cond) + reset + finish
+    const int pro = e->prog == GAS_PROG_BFS ? 6 : 10;
+    const int per = e->prog == GAS_PROG_BFS ? 6 : 8;
+    stats->kernel_launches = pro + per * (c.iteration > 0 ? c.iteration - 1 : 0) + 2;
+  }
+  e->level = c.iteration;
+  return loop_status(e, c, stream);
 }
 
 }  // namespace gas

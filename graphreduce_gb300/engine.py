@@ -204,7 +204,9 @@ def run_program(program: str, el, source: int = 0, schedule: str = "step",
             eng.setActive(source, source + 1, stream)
         else:
             eng.setActive(0, el.nV, stream)
-        cap = el.nV + 2   # a correct run never needs more (Bellman-Ford bound)
+        # BFS/SSSP/CC never need more than nV + 2 iterations (Bellman-Ford
+        # bound); PageRank's |delta| >= 0.01 rule converges in tens
+        cap = el.nV + 2 if program != PAGERANK else 100000
         if schedule == "step":
             it = 0
             eng.setIterationCount(0)

@@ -227,7 +227,9 @@ typedef struct {
 /* Runs the built-in program to convergence from the engine's current
  * vertex data and active set (set_active), like run(), with the chosen
  * schedule; the iteration count and final vertex data are identical for
- * every schedule.  Vertex data stays on the device (get_results copies). */
+ * every schedule.  Vertex data stays on the device (get_results copies).
+ * max_iterations <= 0 selects nV + 2 (BFS, SSSP, CC) or 100000 (PageRank);
+ * reaching the cap returns GAS_ERR_ITER_CAP and leaves the engine usable. */
 gas_status_t gas_engine_run_schedule(gas_engine *e, gas_schedule_t schedule,
                                      int32_t max_iterations,
                                      gas_run_stats *stats, void *stream);
@@ -256,9 +258,13 @@ typedef struct {
   int32_t error;           /* non-zero: a kernel hit an error              */
   int32_t iteration;
   int32_t cond;
-  int32_t n_changed;
+  int32_t n_changed;       /* |C_k|: vertices whose apply() returned true  */
   int32_t max_iter;        /* iteration cap of the current device loop     */
-  int32_t pad[8];
+  int32_t mode;            /* fast runs: 0 push, 1 dense pull (this iter.) */
+  int32_t n_push;          /* fast runs: iterations run with push          */
+  int32_t n_pull;          /* fast runs: iterations run with dense pull    */
+  int32_t pull_div;        /* AUTO pulls when out-edges(C_k)*pull_div > E  */
+  int32_t pad[4];
 } gas_counters;
 
 typedef struct {
@@ -279,6 +285,7 @@ typedef struct {
   void *tile_first;        /* [tile_cap] gather partials (see gas_device.cuh) */
   void *tile_carry;        /* [tile_cap]                                    */
   int32_t *tile_a0;        /* [tile_cap]                                    */
+  int32_t *tile_part;      /* [tile_cap+2] merge-path tile boundaries      */
   int32_t tile_cap;
   int32_t num_sms;         /* SM count of the engine's device              */
   gas_counters *counters;  /* device                                       */

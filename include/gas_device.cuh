@@ -106,9 +106,35 @@ struct SegSource {
   const int32_t *act;
   const int32_t *scan;
   const int32_t *off;
-  int32_t n_seg;
+  int32_t n_seg;             // sizes, unless read from device counters:
   int32_t n_edge;
+  const int32_t *n_seg_p;    // device address of the segment count, or null
+  const int32_t *n_edge_p;   // device address of the edge count, or null
+  const int32_t *part;       // part[t] = segment ends before tile t (from
+                             // k_partition), or null to search in the tile
 };
+
+__device__ __forceinline__ void seg_sizes(const SegSource &s, int &nA, int &E) {
+  nA = s.n_seg_p ? *s.n_seg_p : s.n_seg;
+  E = s.n_edge_p ? *s.n_edge_p : s.n_edge;
+}
+
+// Tile boundaries of a segment source, one thread per boundary, so that the
+// binary searches of all tiles overlap instead of serialising in each CTA
+// (moderngpu's MergePathPartitions step, gpugas.h:737-739).
+template <int kTile, bool kDense>
+__global__ void __launch_bounds__(256) k_partition(SegSource src, int32_t *part) {
+  int nA, E;
+  seg_sizes(src, nA, E);
+  const int64_t M = (int64_t)nA + E;
+  const int ntiles = (int)((M + kTile - 1) / kTile);
+  const int32_t *ends = kDense ? src.off + 1 : src.scan + 1;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles;
+       t += gridDim.x * blockDim.x) {
+    const int64_t d = (int64_t)t * kTile < M ? (int64_t)t * kTile : M;
+    part[t] = merge_path(ends, nA, E, (int)d);
+  }
+}
 
 // One pass over all tiles of a segment source.  Pol provides
 //   typedef Val; zero(); reduce(a, b); map(seg, vertex, pos) -> Val;
@@ -130,8 +156,8 @@ __device__ __forceinline__ void tile_loop(Pol &pol, const SegSource src,
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
-  const int nA = src.n_seg;
-  const int E = src.n_edge;
+  int nA, E;
+  seg_sizes(src, nA, E);
   const int32_t *ends = kDense ? src.off + 1 : src.scan + 1;
   const int64_t M = (int64_t)nA + E;
   const int ntiles = (int)((M + kTile - 1) / kTile);
@@ -139,8 +165,12 @@ __device__ __forceinline__ void tile_loop(Pol &pol, const SegSource src,
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int d0 = t * kTile;
     const int d1 = (int)((int64_t)d0 + kTile < M ? (int64_t)d0 + kTile : M);
-    if (tid == 0) sm.bounds[0] = merge_path(ends, nA, E, d0);
-    if (tid == 32) sm.bounds[1] = merge_path(ends, nA, E, d1);
+    if (src.part) {
+      if (tid < 2) sm.bounds[tid] = __ldg(src.part + t + tid);
+    } else {
+      if (tid == 0) sm.bounds[0] = merge_path(ends, nA, E, d0);
+      if (tid == 32) sm.bounds[1] = merge_path(ends, nA, E, d1);
+    }
     __syncthreads();
     const int a0 = sm.bounds[0];
     const int a1 = sm.bounds[1];
@@ -201,13 +231,19 @@ __device__ __forceinline__ void tile_loop(Pol &pol, const SegSource src,
     }
     __syncthreads();
 
-    for (int j = tid; j < nY; j += kNT) {
-      const int ls = sm.seg[j];
-      const int pos = b0 + j + sm.delta[ls];
-      if constexpr (kReduce)
-        sm.val[j] = pol.map(a0 + ls, sm.vert[ls], pos);
-      else
-        pol.visit(a0 + ls, sm.vert[ls], pos);
+    // Edges of the tile, consecutive threads on consecutive edges; fully
+    // unrolled so that the kVT independent load chains of a thread overlap.
+#pragma unroll
+    for (int k = 0; k < kVT; ++k) {
+      const int j = tid + k * kNT;
+      if (j < nY) {
+        const int ls = sm.seg[j];
+        const int pos = b0 + j + sm.delta[ls];
+        if constexpr (kReduce)
+          sm.val[j] = pol.map(a0 + ls, sm.vert[ls], pos);
+        else
+          pol.visit(a0 + ls, sm.vert[ls], pos);
+      }
     }
     __syncthreads();
     if constexpr (!kReduce) continue;
@@ -289,7 +325,9 @@ __device__ __forceinline__ void fixup_loop(Pol &pol, const SegSource src,
                                            const int32_t *tile_a0) {
   using Val = typename Pol::Val;
   constexpr int kTile = TileShape<sizeof(Val)>::kTile;
-  const int64_t M = (int64_t)src.n_seg + src.n_edge;
+  int nA, E;
+  seg_sizes(src, nA, E);
+  const int64_t M = (int64_t)nA + E;
   const int ntiles = (int)((M + kTile - 1) / kTile);
   const int lane = threadIdx.x & 31;
   const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -358,14 +396,8 @@ template <class P>
 __global__ void __launch_bounds__(kNT)
     k_gather_tiles(GenericGather<P> pol, SegSource src,
                    typename P::GatherResult *tile_first,
-                   typename P::GatherResult *tile_carry, int32_t *tile_a0,
-                   const gas_counters *cnt) {
-  SegSource s = src;
-  if (cnt) {
-    s.n_seg = cnt->n_active;
-    s.n_edge = cnt->n_edges;
-  }
-  tile_loop<GenericGather<P>, false, true>(pol, s, tile_first, tile_carry,
+                   typename P::GatherResult *tile_carry, int32_t *tile_a0) {
+  tile_loop<GenericGather<P>, false, true>(pol, src, tile_first, tile_carry,
                                            tile_a0);
 }
 
@@ -374,13 +406,41 @@ __global__ void __launch_bounds__(kNT)
     k_gather_fixup(GenericGather<P> pol, SegSource src,
                    const typename P::GatherResult *tile_first,
                    const typename P::GatherResult *tile_carry,
-                   const int32_t *tile_a0, const gas_counters *cnt) {
-  SegSource s = src;
-  if (cnt) {
-    s.n_seg = cnt->n_active;
-    s.n_edge = cnt->n_edges;
-  }
-  fixup_loop<GenericGather<P>, false>(pol, s, tile_first, tile_carry, tile_a0);
+                   const int32_t *tile_a0) {
+  fixup_loop<GenericGather<P>, false>(pol, src, tile_first, tile_carry, tile_a0);
+}
+
+// A listed segment source whose sizes are the frontier counters.
+__host__ __device__ inline SegSource frontier_source(const int32_t *act,
+                                                     const int32_t *scan,
+                                                     const int32_t *off,
+                                                     const int32_t *n_seg_p,
+                                                     const int32_t *n_edge_p,
+                                                     const int32_t *part) {
+  SegSource s;
+  s.act = act;
+  s.scan = scan;
+  s.off = off;
+  s.n_seg = 0;
+  s.n_edge = 0;
+  s.n_seg_p = n_seg_p;
+  s.n_edge_p = n_edge_p;
+  s.part = part;
+  return s;
+}
+
+__host__ __device__ inline SegSource dense_source(const int32_t *off, int nV,
+                                                  int nE, const int32_t *part) {
+  SegSource s;
+  s.act = nullptr;
+  s.scan = nullptr;
+  s.off = off;
+  s.n_seg = nV;
+  s.n_edge = nE;
+  s.n_seg_p = nullptr;
+  s.n_edge_p = nullptr;
+  s.part = part;
+  return s;
 }
 
 // Parity mode: one thread per active vertex folds its in-edges sequentially

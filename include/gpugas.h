@@ -95,27 +95,27 @@ class GASEngineGPU {
     gas_counters c;
     GPUGAS_CHECK(gas_engine_read_counters(m_engine, &c, 0));
     if (c.n_active == 0) return;
-    gasdev::SegSource src;
-    src.act = m_view.active;
-    src.scan = m_view.active_scan;
-    src.off = m_view.csc_off;
-    src.n_seg = c.n_active;
-    src.n_edge = c.n_edges;
+    const gasdev::SegSource src = gasdev::frontier_source(
+        m_view.active, m_view.active_scan, m_view.csc_off,
+        &m_view.counters->n_active, &m_view.counters->n_edges, m_view.tile_part);
     typedef gasdev::TileShape<sizeof(GatherResult)> Shape;
     const long long items = (long long)c.n_active + c.n_edges;
     const long long tiles = (items + Shape::kTile - 1) / Shape::kTile;
+    const long long pblocks = (tiles + 1 + 255) / 256;
+    gasdev::k_partition<Shape::kTile, false>
+        <<<(int)(pblocks < 2 * m_view.num_sms ? pblocks : 2 * m_view.num_sms), 256>>>(
+            src, m_view.tile_part);
+    GPUGAS_CUDA(cudaGetLastError());
     const int grid = (int)(tiles < m_gatherGrid ? tiles : m_gatherGrid);
     gasdev::k_gather_tiles<Program><<<grid, gasdev::kNT>>>(
         policy(fuse), src, static_cast<GatherResult *>(m_view.tile_first),
-        static_cast<GatherResult *>(m_view.tile_carry), m_view.tile_a0,
-        m_view.counters);
+        static_cast<GatherResult *>(m_view.tile_carry), m_view.tile_a0);
     GPUGAS_CUDA(cudaGetLastError());
     const long long fix = (tiles + 7) / 8;
     const int fgrid = (int)(fix < 4 * m_view.num_sms ? fix : 4 * m_view.num_sms);
     gasdev::k_gather_fixup<Program><<<fgrid > 0 ? fgrid : 1, gasdev::kNT>>>(
         policy(fuse), src, static_cast<GatherResult *>(m_view.tile_first),
-        static_cast<GatherResult *>(m_view.tile_carry), m_view.tile_a0,
-        m_view.counters);
+        static_cast<GatherResult *>(m_view.tile_carry), m_view.tile_a0);
     GPUGAS_CUDA(cudaGetLastError());
   }
 

@@ -31,7 +31,7 @@ def golden_el(g):
     return EdgeList(int(g["nV"]), g["src"], g["dst"], g["w"])
 
 
-@pytest.mark.parametrize("schedule", ["step", "generic", "ordered"])
+@pytest.mark.parametrize("schedule", ["step", "generic", "ordered", "auto", "push", "pull"])
 @pytest.mark.parametrize("program", INT_PROGRAMS)
 @pytest.mark.parametrize("name", CASES)
 def test_integer_programs_match_reference(name, program, schedule):
@@ -74,7 +74,7 @@ def test_random_rmat_against_oracle(scale, ef, seed):
             ref, rit = oracle.sssp(el.nV, el.src, el.dst, el.weights, s)
         else:
             ref, rit = oracle.cc(el.nV, el.src, el.dst)
-        for schedule in ("step", "generic"):
+        for schedule in ("step", "generic", "auto", "push", "pull"):
             vd, it = run_program(program, el, s, schedule)
             np.testing.assert_array_equal(vd, ref, err_msg=f"{program}/{schedule}")
             assert it == rit, (program, schedule)
@@ -83,9 +83,10 @@ def test_random_rmat_against_oracle(scale, ef, seed):
 def test_cc_with_grid_islands_against_oracle():
     el = EdgeList.rmat(12, 16, seed=2).with_grid_islands(16, 32)
     ref, rit = oracle.cc(el.nV, el.src, el.dst)
-    vd, it = run_program("cc", el, 0, "generic")
-    np.testing.assert_array_equal(vd, ref)
-    assert it == rit and it >= 62      # a 32x32 grid needs 62 label hops
+    for schedule in ("generic", "auto", "push", "pull"):
+        vd, it = run_program("cc", el, 0, schedule)
+        np.testing.assert_array_equal(vd, ref)
+        assert it == rit and it >= 62      # a 32x32 grid needs 62 label hops
 
 
 @pytest.mark.parametrize("scale,seed", [(12, 4), (14, 4)])
@@ -141,18 +142,25 @@ def test_setgraph_recall_and_empty_active_set():
     assert eng.run_schedule("generic").iterations == 0
 
 
-def test_iteration_cap_reports_error_without_fault():
+@pytest.mark.parametrize("schedule", ["generic", "auto", "push"])
+def test_iteration_cap_reports_error_without_fault(schedule):
     el = EdgeList.rmat(10, 16, seed=1).with_grid_islands(2, 16)
     eng = GASEngineGPU("cc")
     vd = initial_vertex_data("cc", el.nV)
     eng.setGraph(el.nV, vd, el.nE, None, el.src, el.dst)
     eng.setActive(0, el.nV)
     with pytest.raises(GasError) as ei:
-        eng.run_schedule("generic", max_iterations=3)
+        eng.run_schedule(schedule, max_iterations=3)
     assert ei.value.status == 4
-    # the context stays usable
+    # the context stays usable and the next run converges
+    vd2 = initial_vertex_data("cc", el.nV)
+    eng.upload_vertex_data(vd2)
     eng.setActive(0, el.nV)
-    eng.run_schedule("generic")
+    st = eng.run_schedule(schedule, max_iterations=el.nV + 2)
+    eng.getResults()
+    ref, rit = oracle.cc(el.nV, el.src, el.dst)
+    np.testing.assert_array_equal(vd, ref)
+    assert st.iterations == rit
 
 
 def test_invalid_arguments_raise():
