@@ -86,7 +86,8 @@ struct gas_engine {
   int32_t level = 0;
   int num_sms = 0;
   bool has_graph = false;
-  bool capturing = false;            // launches go into a CUDA graph
+  bool capturing = false;            // fixed grids (graph capture / host loop)
+  bool in_graph = false;             // loop kernels set a graph condition
   cudaGraphExec_t graphs[kGraphSlots] = {};
   bool level_from_counters = false;  // BFS level = counters.iteration
 };
@@ -105,6 +106,10 @@ gas_status_t engine_sync_counts(gas_engine *e, void *stream);
 int engine_grid(int64_t work_items, int per_block, int cap);
 // grid of a k_partition launch (fixed while capturing)
 int engine_partition_grid(gas_engine *e, int64_t items, int tile);
+// GAS_HOST_LOOP=1: device loops run as direct launches with one host read
+// of the condition per iteration (the kernels are the same; ncu cannot
+// profile kernels inside graphs with conditional nodes).
+bool host_loop_requested();
 }  // namespace gas
 
 #endif  // GAS_ENGINE_IMPL_H_

@@ -11,6 +11,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 
 #include "gas.h"
 #include "gas_device.cuh"
@@ -27,13 +28,14 @@ inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
 
 // Loop condition: one more iteration while the frontier is non-empty and the
 // cap is not reached; hitting the cap with work left raises the error word.
-__global__ void k_loop_cond(gas_counters *cnt, cudaGraphConditionalHandle h) {
+__global__ void k_loop_cond(gas_counters *cnt, cudaGraphConditionalHandle h,
+                            int in_graph) {
   const int max_iter = cnt->max_iter;
   const int it = ++cnt->iteration;
   const bool more = cnt->n_active > 0;
   if (more && it >= max_iter) cnt->error = GAS_ERR_ITER_CAP;
   cnt->cond = (more && it < max_iter) ? 1 : 0;
-  cudaGraphSetConditional(h, cnt->cond);
+  if (in_graph) cudaGraphSetConditional(h, cnt->cond);
 }
 
 __global__ void k_reset_loop(gas_counters *cnt, int32_t max_iter) {
@@ -80,8 +82,10 @@ gas_status_t build_while_graph(
                                      cudaStreamCaptureModeRelaxed);
   if (ce == cudaSuccess) {
     e->capturing = true;
+    e->in_graph = true;
     st = body(e, cs, h, ctx);
     e->capturing = false;
+    e->in_graph = false;
     cudaGraph_t captured = nullptr;
     cudaError_t ce2 = cudaStreamEndCapture(cs, &captured);
     if (st == GAS_OK && ce2 != cudaSuccess)
@@ -97,6 +101,38 @@ gas_status_t build_while_graph(
   cudaStreamDestroy(cs);
   cudaGraphDestroy(g);
   if (st == GAS_OK) *out = x;
+  return st;
+}
+
+bool host_loop_requested() {
+  const char *v = getenv("GAS_HOST_LOOP");
+  return v && v[0] == '1';
+}
+
+// The same loop without a graph: body launches on the stream, the host
+// reads the condition word after every iteration.
+gas_status_t run_host_loop(
+    gas_engine *e,
+    gas_status_t (*body)(gas_engine *, cudaStream_t, cudaGraphConditionalHandle,
+                         void *),
+    void *ctx, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  gas_status_t st = GAS_OK;
+  e->capturing = true;
+  e->in_graph = false;
+  for (;;) {
+    cudaError_t ce = cudaMemcpyAsync(e->h_cnt, e->cnt, sizeof(gas_counters),
+                                     cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) {
+      st = fail(GAS_ERR_CUDA, "host loop: %s", cudaGetErrorString(ce));
+      break;
+    }
+    if (!e->h_cnt->cond) break;
+    st = body(e, s, 0, ctx);
+    if (st != GAS_OK) break;
+  }
+  e->capturing = false;
   return st;
 }
 
@@ -125,7 +161,7 @@ gas_status_t generic_body(gas_engine *e, cudaStream_t cs,
                           cudaGraphConditionalHandle h, void *ctx) {
   const GenericCtx *c = static_cast<const GenericCtx *>(ctx);
   GAS_TRY(gas::engine_generic_iteration(e, c->ordered, cs));
-  k_loop_cond<<<1, 1, 0, cs>>>(e->cnt, h);
+  k_loop_cond<<<1, 1, 0, cs>>>(e->cnt, h, e->in_graph ? 1 : 0);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -155,6 +191,14 @@ extern "C" gas_status_t gas_engine_run_schedule(gas_engine *e,
 
   GenericCtx ctx{schedule == GAS_SCHED_ORDERED};
   const int slot = ctx.ordered ? kGraphOrdered : kGraphGeneric;
+  if (gas::host_loop_requested()) {
+    k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
+    CUDA_TRY(cudaGetLastError());
+    e->level_from_counters = true;
+    gas_status_t st = gas::run_host_loop(e, generic_body, &ctx, stream);
+    e->level_from_counters = false;
+    if (st != GAS_OK) return st;
+  } else {
   if (!e->graphs[slot]) {
     e->level_from_counters = true;
     gas_status_t st = gas::build_while_graph(e, generic_body, &ctx, &e->graphs[slot]);
@@ -167,6 +211,7 @@ extern "C" gas_status_t gas_engine_run_schedule(gas_engine *e,
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(stream));
   if (ce != cudaSuccess)
     return gas::fail(GAS_ERR_CUDA, "generic run: %s", cudaGetErrorString(ce));
+  }
   gas_counters c;
   GAS_TRY(gas_engine_read_counters(e, &c, stream));
   if (stats) {
@@ -273,7 +318,7 @@ __global__ void __launch_bounds__(kNT)
 __global__ void __launch_bounds__(kNT)
     k_pr_finish(const double *l1_part, int n, const double *tol_p,
                 gas_counters *cnt, double *residual,
-                cudaGraphConditionalHandle h) {
+                cudaGraphConditionalHandle h, int in_graph) {
   __shared__ double s[kNT];
   double v = 0.0;
   for (int i = threadIdx.x; i < n; i += kNT) v += l1_part[i];
@@ -292,7 +337,7 @@ __global__ void __launch_bounds__(kNT)
     const bool more = !(l1 <= tol);
     if (more && it >= max_iter) cnt->error = GAS_ERR_ITER_CAP;
     cnt->cond = (more && it < max_iter) ? 1 : 0;
-    cudaGraphSetConditional(h, cnt->cond);
+    if (in_graph) cudaGraphSetConditional(h, cnt->cond);
   }
 }
 
@@ -326,7 +371,8 @@ gas_status_t pr_body(gas_engine *e, cudaStream_t cs,
       (const PrVal *)e->tile_carry, e->tile_a0, e->cnt,
       e->pr_l1 + c->tiles_grid);
   k_pr_finish<<<1, kNT, 0, cs>>>(e->pr_l1, c->tiles_grid + c->fix_grid,
-                                 c->residual + 1, e->cnt, c->residual, h);
+                                 c->residual + 1, e->cnt, c->residual, h,
+                                 e->in_graph ? 1 : 0);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -378,7 +424,8 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
     cudaGraphExecDestroy(e->graphs[kGraphPagerank]);
     e->graphs[kGraphPagerank] = nullptr;
   }
-  if (!e->graphs[kGraphPagerank]) {
+  const bool host_loop = gas::host_loop_requested();
+  if (!host_loop && !e->graphs[kGraphPagerank]) {
     GAS_TRY(gas::build_while_graph(e, pr_body, &c, &e->graphs[kGraphPagerank]));
     e->pr_damping = damping;
   }
@@ -394,7 +441,11 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
       e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV));
   k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
   cudaError_t ce = cudaGetLastError();
-  if (ce == cudaSuccess) ce = cudaGraphLaunch(e->graphs[kGraphPagerank], S(stream));
+  if (host_loop) {
+    if (ce == cudaSuccess) GAS_TRY(gas::run_host_loop(e, pr_body, &c, stream));
+  } else if (ce == cudaSuccess) {
+    ce = cudaGraphLaunch(e->graphs[kGraphPagerank], S(stream));
+  }
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(stream));
   if (ce != cudaSuccess)
     return gas::fail(GAS_ERR_CUDA, "pagerank: %s", cudaGetErrorString(ce));

@@ -337,17 +337,17 @@ __device__ __forceinline__ void pick_mode(gas_counters *cnt, int nE) {
 }
 
 __global__ void k_fast_precond(gas_counters *cnt, cudaGraphConditionalHandle h,
-                               int nE) {
+                               int nE, int in_graph) {
   cnt->iteration = 1;  // iteration 0 ran in the prologue
   const bool more = cnt->n_scatter_edges > 0;
   if (more && 1 >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
   cnt->cond = (more && 1 < cnt->max_iter) ? 1 : 0;
   pick_mode(cnt, nE);
-  cudaGraphSetConditional(h, cnt->cond);
+  if (in_graph) cudaGraphSetConditional(h, cnt->cond);
 }
 
 __global__ void k_fast_cond(gas_counters *cnt, cudaGraphConditionalHandle h,
-                            int nE) {
+                            int nE, int in_graph) {
   if (cnt->mode == kModePush)
     ++cnt->n_push;
   else
@@ -357,7 +357,7 @@ __global__ void k_fast_cond(gas_counters *cnt, cudaGraphConditionalHandle h,
   if (more && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
   cnt->cond = (more && it < cnt->max_iter) ? 1 : 0;
   pick_mode(cnt, nE);
-  cudaGraphSetConditional(h, cnt->cond);
+  if (in_graph) cudaGraphSetConditional(h, cnt->cond);
 }
 
 __global__ void k_fast_reset(gas_counters *cnt, int max_iter, int forced,
@@ -460,7 +460,7 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   }
   CUDA_TRY(cudaGetLastError());
   GAS_TRY(compaction(e, cs, c));
-  k_fast_cond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE);
+  k_fast_cond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE, e->in_graph ? 1 : 0);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -504,9 +504,10 @@ static gas_status_t build_fast_graph(gas_engine *e, FastCtx *ctx,
     return fail(GAS_ERR_CUDA, "fast graph setup: %s", cudaGetErrorString(ce));
   }
   e->capturing = true;
+  e->in_graph = true;
   st = prologue(e, cs, ctx);
   if (st == GAS_OK) {
-    k_fast_precond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE);
+    k_fast_precond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE, e->in_graph ? 1 : 0);
     ce = cudaGetLastError();
     if (ce != cudaSuccess) st = fail(GAS_ERR_CUDA, "precond: %s", cudaGetErrorString(ce));
   }
@@ -519,6 +520,7 @@ static gas_status_t build_fast_graph(gas_engine *e, FastCtx *ctx,
     else st = fail(GAS_ERR_CUDA, "capture info: %s", cudaGetErrorString(ce));
   }
   e->capturing = false;
+  e->in_graph = false;
   cudaGraph_t cap = nullptr;
   ce = cudaStreamEndCapture(cs, &cap);
   if (st == GAS_OK && ce != cudaSuccess)
@@ -541,8 +543,10 @@ static gas_status_t build_fast_graph(gas_engine *e, FastCtx *ctx,
         st = fail(GAS_ERR_CUDA, "body capture: %s", cudaGetErrorString(ce));
       } else {
         e->capturing = true;
+        e->in_graph = true;
         st = body(e, cs, h, ctx);
         e->capturing = false;
+        e->in_graph = false;
         cudaGraph_t bc = nullptr;
         ce = cudaStreamEndCapture(cs, &bc);
         if (st == GAS_OK && ce != cudaSuccess)
@@ -564,18 +568,35 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
                       void *stream) {
   if (e->prog == GAS_PROG_PAGERANK)  // not monotone: the generic kernels
     return gas_engine_run_schedule(e, GAS_SCHED_GENERIC, max_iterations, stats, stream);
-  if (e->prog == GAS_PROG_BFS && schedule == GAS_SCHED_PULL) schedule = GAS_SCHED_PUSH;
+  // BFS has the top-down push only: every schedule pushes
+  if (e->prog == GAS_PROG_BFS) schedule = GAS_SCHED_PUSH;
   GAS_TRY(ensure_fast_buffers(e));
   FastCtx ctx;
   ctx.nW = (e->nV + 31) / 32;
   ctx.n_qblocks = (ctx.nW + kCompactBlock - 1) / kCompactBlock;
   if (ctx.n_qblocks < 1) ctx.n_qblocks = 1;
   const int slot = kGraphFast0;
-  if (!e->graphs[slot]) GAS_TRY(build_fast_graph(e, &ctx, &e->graphs[slot]));
+  const bool host_loop = host_loop_requested();
+  if (!host_loop && !e->graphs[slot]) GAS_TRY(build_fast_graph(e, &ctx, &e->graphs[slot]));
   const int forced = schedule == GAS_SCHED_PUSH ? 1 : schedule == GAS_SCHED_PULL ? 2 : 0;
   k_fast_reset<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations, forced, e->pull_div);
   cudaError_t ce = cudaGetLastError();
-  if (ce == cudaSuccess) ce = cudaGraphLaunch(e->graphs[slot], S(stream));
+  if (host_loop) {
+    if (ce == cudaSuccess) {
+      e->capturing = true;
+      e->in_graph = false;
+      gas_status_t pst = prologue(e, S(stream), &ctx);
+      if (pst == GAS_OK) {
+        k_fast_precond<<<1, 1, 0, S(stream)>>>(e->cnt, 0, e->nE, 0);
+        ce = cudaGetLastError();
+      }
+      e->capturing = false;
+      if (pst != GAS_OK) return pst;
+      if (ce == cudaSuccess) GAS_TRY(run_host_loop(e, body, &ctx, stream));
+    }
+  } else if (ce == cudaSuccess) {
+    ce = cudaGraphLaunch(e->graphs[slot], S(stream));
+  }
   if (ce == cudaSuccess) {
     k_fast_finish<<<1, 1, 0, S(stream)>>>(e->cnt);
     ce = cudaGetLastError();

@@ -25,6 +25,13 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
                       int32_t max_iterations, gas_run_stats *stats,
                       void *stream);
 
+// The loop of build_while_graph as direct launches (GAS_HOST_LOOP=1).
+gas_status_t run_host_loop(
+    gas_engine *e,
+    gas_status_t (*body)(gas_engine *, cudaStream_t, cudaGraphConditionalHandle,
+                         void *),
+    void *ctx, void *stream);
+
 // Status of a finished device loop from its counters (clears the error word).
 gas_status_t loop_status(gas_engine *e, const gas_counters &c, void *stream);
 

@@ -176,3 +176,25 @@ def test_invalid_arguments_raise():
     e2 = GASEngineGPU("sssp")
     with pytest.raises(GasError):
         e2.setGraph(el.nV, initial_vertex_data("sssp", el.nV, 0), el.nE, None, el.src, el.dst)
+
+
+@pytest.mark.parametrize("schedule", ["generic", "auto", "push", "pull"])
+def test_host_loop_mode_matches(schedule, monkeypatch):
+    """GAS_HOST_LOOP=1 runs the same kernels as direct launches (the form
+    ncu can profile); results and iteration counts must not change."""
+    monkeypatch.setenv("GAS_HOST_LOOP", "1")
+    el = EdgeList.rmat(12, 16, seed=7).with_uniform_weights(1, 64, 3).with_grid_islands(4, 8)
+    s = int(el.sample_sources(1, 7)[0])
+    for program, ref in (("sssp", oracle.sssp(el.nV, el.src, el.dst, el.weights, s)),
+                         ("cc", oracle.cc(el.nV, el.src, el.dst)),
+                         ("bfs", oracle.bfs(el.nV, el.src, el.dst, s))):
+        vd, it = run_program(program, el, s, schedule)
+        np.testing.assert_array_equal(vd, ref[0])
+        assert it == ref[1]
+    d = EdgeList.rmat(11, 16, seed=4, symmetrize=False)
+    r64, rit, _ = oracle.pagerank_fp64(d.nV, d.src, d.dst, 0.85, 1e-6)
+    eng = GASEngineGPU("pagerank")
+    vd = initial_vertex_data("pagerank", d.nV, 0, d.out_degree())
+    eng.setGraph(d.nV, vd, d.nE, None, d.src, d.dst)
+    ranks, st = eng.pagerank_precision(0.85, 1e-6)
+    assert np.abs(ranks.astype(np.float64) - r64).sum() <= 1e-6
