@@ -96,6 +96,8 @@ _SIGS = {
     "gas_engine_run_schedule": ("status", [c_vp, c_i32, c_i32, C.POINTER(RunStats), c_vp]),
     "gas_engine_pagerank_precision": ("status", [c_vp, c_dbl, c_dbl, c_i32, c_vp,
                                                  C.POINTER(RunStats), c_vp]),
+    "gas_pagerank_step_noalloc": ("status", [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                             c_dbl, c_vp, c_vp]),
     "gas_engine_view_get": ("status", [c_vp, c_vp]),
     "gas_engine_note_applied": ("status", [c_vp, c_i32]),
     "gas_engine_read_counters": ("status", [c_vp, C.POINTER(Counters), c_vp]),

@@ -28,7 +28,8 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fPIC,-fopenmp,-fvisibility=default",
     f"-I{INCLUDE}", f"-I{CSRC}",
 ]
-SOURCES = ["gas_engine.cu", "gas_runs.cu", "gas_sched.cu", "gas_host_graph.cpp"]
+SOURCES = ["gas_engine.cu", "gas_runs.cu", "gas_sched.cu", "gas_noalloc.cu",
+           "gas_host_graph.cpp"]
 
 
 def nvcc() -> str:

@@ -246,6 +246,29 @@ gas_status_t gas_engine_pagerank_precision(gas_engine *e, double damping,
                                            float *ranks, gas_run_stats *stats,
                                            void *stream);
 
+/* One precision-form PageRank step for callers that cannot allocate device
+ * memory -- code whose memory pool or arena owns every byte of the device,
+ * or a request path that must not call cudaMalloc (it synchronises the device
+ * and can fail under fragmentation).  No counterpart in the reference.
+ *   rank_out[v] = (1-d)/N + d * sum_{u->v} rank_in[u] / out_degree[u]
+ * over a CSC graph in device memory (csc_off[nV+1], csc_src[nE]); *l1_out
+ * (device) receives the FP64 residual sum_v |rank_out[v] - rank_in[v]|.
+ * All pointers are caller-owned device memory; the kernels' scratch is a
+ * fixed file-scope device array (about 6.3 MB, resident on every device that
+ * loads the library), so no allocation happens.  Graphs with
+ * nV + nE > GAS_NOALLOC_MAX_ITEMS return GAS_ERR_TOO_LARGE.  Every call
+ * shares that array: calls whose kernels overlap on the GPU race, so issue
+ * them on one stream.  The first call on a device looks the array up with
+ * that device current; make it before capturing work into a CUDA graph. */
+#define GAS_NOALLOC_MAX_ITEMS (1LL << 29)
+gas_status_t gas_pagerank_step_noalloc(int32_t nV, int32_t nE,
+                                       const int32_t *csc_off,
+                                       const int32_t *csc_src,
+                                       const int32_t *out_degree,
+                                       const float *rank_in, float *rank_out,
+                                       double damping, double *l1_out,
+                                       void *stream);
+
 /* ======================================================================= */
 /* Views used by include/gpugas.h to launch its Program-typed kernels.     */
 /* ======================================================================= */
