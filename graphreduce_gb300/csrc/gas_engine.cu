@@ -463,8 +463,12 @@ void free_graph(gas_engine *e) {
   dfree(e->ppart); dfree(e->cpart); dfree(e->cnt);
   for (int i = 0; i < 2; ++i) { dfree(e->pr_rank[i]); dfree(e->pr_contrib[i]); }
   dfree(e->pr_inv_deg); dfree(e->pr_l1);
-  dfree(e->q_ids); dfree(e->q_vals); dfree(e->q_scan); dfree(e->snap);
+  dfree(e->q_ids); dfree(e->q_vals); dfree(e->q_end); dfree(e->q_delta); dfree(e->snap);
   dfree(e->qpart); dfree(e->cbits); dfree(e->mbits);
+  dfree(e->ne_vid); dfree(e->ne_end); dfree(e->zero_vid);
+  dfree(e->slab_dpart); dfree(e->slab_qpart); dfree(e->slab_a0);
+  dfree(e->slab_first); dfree(e->slab_carry);
+  e->n_ne = e->n_zero = e->slab_cap = 0;
   for (int i = 0; i < kGraphSlots; ++i) {
     if (e->graphs[i]) cudaGraphExecDestroy(e->graphs[i]);
     e->graphs[i] = nullptr;
@@ -627,6 +631,7 @@ gas_status_t scatter_common(gas_engine *e, void *stream) {
   CUDA_TRY(cudaGetLastError());
   e->counts_dirty = true;
   e->have_gres = false;
+  e->active_full = false;
   return GAS_OK;
 }
 
@@ -796,7 +801,42 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   GAS_TRY(dalloc(&e->cpart, 2 * (size_t)e->n_cblocks));
   GAS_TRY(dalloc(&e->cnt, 1));
 
+  // rows of the CSC with / without in-edges, for the dense slab passes
+  std::vector<int32_t> ne_vid, ne_end, zero_vid;
+  try {
+    ne_vid.reserve(V);
+    ne_end.reserve(V);
+    for (int32_t v = 0; v < nV; ++v) {
+      if (e->h_csc_off[v + 1] > e->h_csc_off[v]) {
+        ne_vid.push_back(v);
+        ne_end.push_back(e->h_csc_off[v + 1]);
+      } else {
+        zero_vid.push_back(v);
+      }
+    }
+  } catch (...) {
+    return gas::fail(GAS_ERR_NOMEM, "set_graph: row lists");
+  }
+  e->n_ne = (int32_t)ne_vid.size();
+  e->n_zero = (int32_t)zero_vid.size();
+  GAS_TRY(dalloc(&e->ne_vid, ne_vid.size()));
+  GAS_TRY(dalloc(&e->ne_end, ne_end.size()));
+  GAS_TRY(dalloc(&e->zero_vid, zero_vid.size()));
+  e->slab_cap = (int32_t)((E + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk + 1);
+  GAS_TRY(dalloc(&e->slab_dpart, (size_t)e->slab_cap));
+  GAS_TRY(dalloc(&e->slab_qpart, (size_t)e->slab_cap));
+  GAS_TRY(dalloc(&e->slab_a0, (size_t)e->slab_cap));
+  GAS_TRY(dalloc((uint8_t **)&e->slab_first, (size_t)e->slab_cap * 8));
+  GAS_TRY(dalloc((uint8_t **)&e->slab_carry, (size_t)e->slab_cap * 8));
+
   cudaStream_t st = S(stream);
+  if (!ne_vid.empty()) {
+    CUDA_TRY(cudaMemcpyAsync(e->ne_vid, ne_vid.data(), ne_vid.size() * 4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(e->ne_end, ne_end.data(), ne_end.size() * 4, cudaMemcpyHostToDevice, st));
+  }
+  if (!zero_vid.empty())
+    CUDA_TRY(cudaMemcpyAsync(e->zero_vid, zero_vid.data(), zero_vid.size() * 4,
+                             cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(e->csc_off, e->h_csc_off.data(), (V + 1) * 4, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(e->csr_off, csr_off.data(), (V + 1) * 4, cudaMemcpyHostToDevice, st));
   if (E) {
@@ -843,6 +883,7 @@ gas_status_t gas_engine_set_active(gas_engine *e, int32_t start, int32_t end,
   e->n_active = n;
   e->n_edges = e->h_csc_off[end] - e->h_csc_off[start];
   e->counts_dirty = false;
+  e->active_full = start == 0 && end == e->nV;
   return GAS_OK;
 }
 

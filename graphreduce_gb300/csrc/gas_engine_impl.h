@@ -72,10 +72,19 @@ struct gas_engine {
   // fast-schedule state (lazily allocated): frontier queue of C_k with the
   // values its members had at the end of iteration k, out-degree scan,
   // changed bitmap (being built), membership bitmap of C_k, snapshots
-  int32_t *q_ids = nullptr, *q_vals = nullptr, *q_scan = nullptr;
+  int32_t *q_ids = nullptr, *q_vals = nullptr, *q_end = nullptr, *q_delta = nullptr;
   int32_t *snap = nullptr, *qpart = nullptr;
   uint32_t *cbits = nullptr, *mbits = nullptr;
   int32_t pull_div = 4;
+
+  // non-empty in-edge rows of the CSC (dense slab passes) and the rest
+  int32_t *ne_vid = nullptr, *ne_end = nullptr, *zero_vid = nullptr;
+  int32_t n_ne = 0, n_zero = 0;
+  // warp-slab chunk state: partitions of the dense CSC and of the push
+  // queue, per-chunk carries (8-byte values) and fixup rows
+  int32_t *slab_dpart = nullptr, *slab_qpart = nullptr, *slab_a0 = nullptr;
+  void *slab_first = nullptr, *slab_carry = nullptr;
+  int32_t slab_cap = 0;
 
   // host view of the step API state
   int32_t n_active = 0, n_edges = 0;
@@ -86,6 +95,7 @@ struct gas_engine {
   int32_t level = 0;
   int num_sms = 0;
   bool has_graph = false;
+  bool active_full = false;          // active set is [0, nV) from set_active
   bool capturing = false;            // fixed grids (graph capture / host loop)
   bool in_graph = false;             // loop kernels set a graph condition
   cudaGraphExec_t graphs[kGraphSlots] = {};

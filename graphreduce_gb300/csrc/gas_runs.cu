@@ -221,6 +221,7 @@ extern "C" gas_status_t gas_engine_run_schedule(gas_engine *e,
     stats->kernel_launches = c.iteration * (e->prog == GAS_PROG_BFS ? 9 : 11) + 1;
   }
   e->level = c.iteration;
+  e->active_full = false;
   return gas::loop_status(e, c, stream);
 }
 
@@ -298,19 +299,30 @@ __device__ __forceinline__ void block_sum_store(double v, double *out) {
 }
 
 __global__ void __launch_bounds__(kNT)
-    k_pr_tiles(PrPol pol, PrBufs bufs, SegSource src, PrVal *tf, PrVal *tc,
-               int32_t *ta0, const gas_counters *cnt, double *l1_part) {
+    k_pr_slab(PrPol pol, PrBufs bufs, gasdev::SlabSource src, PrVal *cf, PrVal *cc,
+              int32_t *ca0, const gas_counters *cnt, double *l1_part) {
   pr_bind(pol, bufs, cnt);
-  gasdev::tile_loop<PrPol, true, true>(pol, src, tf, tc, ta0);
+  gasdev::slab_loop<PrPol, true>(pol, src, cf, cc, ca0);
   block_sum_store(pol.l1, l1_part + blockIdx.x);
 }
 
 __global__ void __launch_bounds__(kNT)
-    k_pr_fixup(PrPol pol, PrBufs bufs, SegSource src, const PrVal *tf,
-               const PrVal *tc, const int32_t *ta0, const gas_counters *cnt,
+    k_pr_fixup(PrPol pol, PrBufs bufs, gasdev::SlabSource src, const PrVal *cf,
+               const PrVal *cc, const int32_t *ca0, const gas_counters *cnt,
                double *l1_part) {
   pr_bind(pol, bufs, cnt);
-  gasdev::fixup_loop<PrPol, true>(pol, src, tf, tc, ta0);
+  gasdev::slab_fixup_loop<PrPol>(pol, src, cf, cc, ca0);
+  block_sum_store(pol.l1, l1_part + blockIdx.x);
+}
+
+// Vertices without in-edges: rank = (1-d)/N.
+__global__ void __launch_bounds__(kNT)
+    k_pr_empty(PrPol pol, PrBufs bufs, const int32_t *zero_vid, int n_zero,
+               const gas_counters *cnt, double *l1_part) {
+  pr_bind(pol, bufs, cnt);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_zero;
+       i += gridDim.x * blockDim.x)
+    pol.emit(0, zero_vid[i], pol.zero());
   block_sum_store(pol.l1, l1_part + blockIdx.x);
 }
 
@@ -354,23 +366,26 @@ __global__ void k_pr_init(float *rank, float *contrib, const int32_t *csr_off,
 struct PrCtx {
   PrPol pol;
   PrBufs bufs;
-  SegSource src;
+  gasdev::SlabSource src;
   int tiles_grid;
   int fix_grid;
+  int empty_grid;
   double *residual;
 };
 
 gas_status_t pr_body(gas_engine *e, cudaStream_t cs,
                      cudaGraphConditionalHandle h, void *vctx) {
   PrCtx *c = static_cast<PrCtx *>(vctx);
-  k_pr_tiles<<<c->tiles_grid, kNT, 0, cs>>>(
-      c->pol, c->bufs, c->src, (PrVal *)e->tile_first, (PrVal *)e->tile_carry,
-      e->tile_a0, e->cnt, e->pr_l1);
+  k_pr_slab<<<c->tiles_grid, kNT, 0, cs>>>(
+      c->pol, c->bufs, c->src, (PrVal *)e->slab_first, (PrVal *)e->slab_carry,
+      e->slab_a0, e->cnt, e->pr_l1);
   k_pr_fixup<<<c->fix_grid, kNT, 0, cs>>>(
-      c->pol, c->bufs, c->src, (const PrVal *)e->tile_first,
-      (const PrVal *)e->tile_carry, e->tile_a0, e->cnt,
-      e->pr_l1 + c->tiles_grid);
-  k_pr_finish<<<1, kNT, 0, cs>>>(e->pr_l1, c->tiles_grid + c->fix_grid,
+      c->pol, c->bufs, c->src, (const PrVal *)e->slab_first,
+      (const PrVal *)e->slab_carry, e->slab_a0, e->cnt, e->pr_l1 + c->tiles_grid);
+  k_pr_empty<<<c->empty_grid, kNT, 0, cs>>>(c->pol, c->bufs, e->zero_vid, e->n_zero,
+                                            e->cnt,
+                                            e->pr_l1 + c->tiles_grid + c->fix_grid);
+  k_pr_finish<<<1, kNT, 0, cs>>>(e->pr_l1, c->tiles_grid + c->fix_grid + c->empty_grid,
                                  c->residual + 1, e->cnt, c->residual, h,
                                  e->in_graph ? 1 : 0);
   CUDA_TRY(cudaGetLastError());
@@ -393,21 +408,20 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
     if (!e->pr_rank[i]) CUDA_TRY(cudaMalloc(&e->pr_rank[i], (size_t)nV * 4));
     if (!e->pr_contrib[i]) CUDA_TRY(cudaMalloc(&e->pr_contrib[i], (size_t)nV * 4));
   }
-  int per_sm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pr_tiles, kNT, 0));
-  if (per_sm < 1) per_sm = 1;
   PrCtx c;
-  c.tiles_grid = e->num_sms * per_sm;
+  c.tiles_grid = 8 * e->num_sms;  // 64 resident warps per SM
   c.fix_grid = 2 * e->num_sms;
-  if (!e->pr_l1 || e->pr_l1_cap < c.tiles_grid + c.fix_grid + 2) {
+  c.empty_grid = 2 * e->num_sms;
+  const int nparts = c.tiles_grid + c.fix_grid + c.empty_grid;
+  if (!e->pr_l1 || e->pr_l1_cap < nparts + 2) {
     if (e->pr_l1) cudaFree(e->pr_l1);
     e->pr_l1 = nullptr;
     if (e->graphs[kGraphPagerank]) cudaGraphExecDestroy(e->graphs[kGraphPagerank]);
     e->graphs[kGraphPagerank] = nullptr;
-    e->pr_l1_cap = c.tiles_grid + c.fix_grid + 2;
+    e->pr_l1_cap = nparts + 2;
     CUDA_TRY(cudaMalloc(&e->pr_l1, sizeof(double) * (size_t)e->pr_l1_cap));
   }
-  c.residual = e->pr_l1 + c.tiles_grid + c.fix_grid;
+  c.residual = e->pr_l1 + nparts;
   c.pol.csc_src = e->csc_src;
   c.pol.csr_off = e->csr_off;
   c.pol.base = (float)((1.0 - damping) / (double)nV);
@@ -417,7 +431,8 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
   c.bufs.rank[1] = e->pr_rank[1];
   c.bufs.contrib[0] = e->pr_contrib[0];
   c.bufs.contrib[1] = e->pr_contrib[1];
-  c.src = gasdev::dense_source(e->csc_off, nV, e->nE, e->dpart);
+  c.src = gasdev::slab_source(e->ne_end, e->ne_vid, nullptr, e->n_ne, e->nE, nullptr,
+                              nullptr, e->slab_dpart);
 
   // damping is baked into the captured policy: rebuild when it changes
   if (e->graphs[kGraphPagerank] && e->pr_damping != damping) {
@@ -431,12 +446,7 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
   }
   CUDA_TRY(cudaMemcpyAsync(c.residual + 1, &tol, sizeof(double),
                            cudaMemcpyHostToDevice, S(stream)));
-  {
-    constexpr int kTile = gasdev::TileShape<sizeof(PrVal)>::kTile;
-    const int64_t items = (int64_t)nV + e->nE;
-    gasdev::k_partition<kTile, true>
-        <<<gas::engine_partition_grid(e, items, kTile), 256, 0, S(stream)>>>(c.src, e->dpart);
-  }
+  gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, S(stream)>>>(c.src, e->slab_dpart);
   k_pr_init<<<gas::engine_grid(nV, kNT, 8 * e->num_sms), kNT, 0, S(stream)>>>(
       e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV));
   k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
@@ -464,7 +474,7 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
   if (stats) {
     stats->iterations = cnt.iteration;
     stats->pull_iters = cnt.iteration;
-    stats->kernel_launches = 3 * cnt.iteration + 2;
+    stats->kernel_launches = 4 * cnt.iteration + 3;
     stats->edges_processed = (int64_t)cnt.iteration * e->nE;
     stats->residual = resid;
   }

@@ -87,42 +87,89 @@ __global__ void k_seed_changed(const int32_t *act, const uint8_t *ret,
   }
 }
 
-// ---------------------------------------------------------------------------
-// frontier compaction: changed bitmap -> queue (id, value), out-degree scan;
-// the bitmap moves to mbits (membership of C_k for the dense pull)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void qword_stats(const uint32_t *bits,
-                                            const int32_t *csr_off, int nW,
-                                            int w, int *c, int *d) {
-  *c = 0;
-  *d = 0;
-  if (w >= nW) return;
-  uint32_t m = bits[w];
-  *c = __popc(m);
-  while (m) {
-    const int b = __ffs(m) - 1;
-    m &= m - 1;
-    const int v = w * 32 + b;
-    *d += csr_off[v + 1] - csr_off[v];
+// Iteration 0 from the full vertex range, without folding every in-edge:
+// with A_0 = V, a vertex u whose value is not below Program::gatherZero
+// contributes min(gatherZero, d_u + w) = gatherZero >= d_v to every
+// out-neighbour, so only S = {u : d_u < gatherZero} can change anything.
+// Pushing (or dense-pulling) from S is iteration 0 exactly; for SSSP from
+// one source S = {source}.
+__global__ void k_seed_finite(const int32_t *vd, int nV, int32_t zero_cap,
+                              uint32_t *cbits) {
+  const int nW = (nV + 31) / 32;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nW;
+       w += gridDim.x * blockDim.x) {
+    uint32_t m = 0;
+    const int v0 = w * 32;
+    const int n = nV - v0 < 32 ? nV - v0 : 32;
+    for (int b = 0; b < n; ++b)
+      if (vd[v0 + b] < zero_cap) m |= 1u << b;
+    cbits[w] = m;
   }
+}
+
+// ---------------------------------------------------------------------------
+// frontier compaction: changed bitmap -> queue of the members with out-edges
+// (id, value at the end of the iteration, end of its out-edge range in the
+// queue's edge space, CSR position offset), membership bitmap + snapshots of
+// all members for the dense pull.  One lane per vertex: each warp takes 32
+// bitmap words; a word's 32 lanes read their out-degrees coalesced, a ballot
+// gives queue positions, a warp scan gives edge offsets.
+// ---------------------------------------------------------------------------
+constexpr int kQWordsPerWarp = 32;
+constexpr int kQWordsPerBlock = kQWordsPerWarp * (kNT / 32);  // 256 words
+
+__device__ __forceinline__ int warp_incl_sum_i(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int o = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= d) v += o;
+  }
+  return v;
+}
+
+// per-warp (queue entries, out-edges) of its 32 words
+__device__ __forceinline__ void q_warp_counts(const uint32_t *cbits,
+                                              const int32_t *csr_off, int nW,
+                                              int w0, int *cq, int *cd) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t mine = (w0 + lane < nW) ? cbits[w0 + lane] : 0u;
+  int q = 0, d = 0;
+  for (int i = 0; i < kQWordsPerWarp; ++i) {
+    const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
+    if (!word) continue;
+    const int v = (w0 + i) * 32 + lane;
+    int deg = 0;
+    if ((word >> lane) & 1u) deg = csr_off[v + 1] - csr_off[v];
+    q += __popc(__ballot_sync(0xffffffffu, deg > 0));
+    d += deg;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  *cq = q;
+  *cd = d;
 }
 
 __global__ void __launch_bounds__(kNT)
     k_q_count(const uint32_t *cbits, const int32_t *csr_off, int nW,
               int32_t *part) {
-  int c = 0, d = 0;
-  const int w0 = blockIdx.x * kCompactBlock + threadIdx.x * kWordsPerThread;
-  for (int k = 0; k < kWordsPerThread; ++k) {
-    int cc, dd;
-    qword_stats(cbits, csr_off, nW, w0 + k, &cc, &dd);
-    c += cc;
-    d += dd;
+  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int cq, cd;
+  q_warp_counts(cbits, csr_off, nW, blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp,
+                &cq, &cd);
+  if (lane == 0) {
+    s_q[warp] = cq;
+    s_d[warp] = cd;
   }
-  int tc, td;
-  cta_excl_sum(c, &tc);
-  cta_excl_sum(d, &td);
+  __syncthreads();
   if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = tc;
+    int tq = 0, td = 0;
+    for (int w = 0; w < kNT / 32; ++w) {
+      tq += s_q[w];
+      td += s_d[w];
+    }
+    part[2 * blockIdx.x] = tq;
     part[2 * blockIdx.x + 1] = td;
   }
 }
@@ -152,48 +199,60 @@ __global__ void __launch_bounds__(kNT)
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    cnt->n_changed = s_carry[0];
-    cnt->n_scatter_edges = s_carry[1];
+    cnt->n_changed = s_carry[0];       // queue length (members with out-edges)
+    cnt->n_scatter_edges = s_carry[1]; // their out-edges
   }
 }
 
 __global__ void __launch_bounds__(kNT)
     k_q_write(uint32_t *cbits, uint32_t *mbits, const int32_t *csr_off, int nW,
               const int32_t *part, const int32_t *vd, int32_t *q_ids,
-              int32_t *q_vals, int32_t *q_scan, int32_t *snap,
-              const gas_counters *cnt) {
-  const int w0 = blockIdx.x * kCompactBlock + threadIdx.x * kWordsPerThread;
-  int c = 0, d = 0;
-  for (int k = 0; k < kWordsPerThread; ++k) {
-    int cc, dd;
-    qword_stats(cbits, csr_off, nW, w0 + k, &cc, &dd);
-    c += cc;
-    d += dd;
+              int32_t *q_vals, int32_t *q_end, int32_t *q_delta, int32_t *snap) {
+  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
+  int cq, cd;
+  q_warp_counts(cbits, csr_off, nW, w0, &cq, &cd);
+  if (lane == 0) {
+    s_q[warp] = cq;
+    s_d[warp] = cd;
   }
-  int tc, td;
-  int pc = cta_excl_sum(c, &tc) + part[2 * blockIdx.x];
-  int pd = cta_excl_sum(d, &td) + part[2 * blockIdx.x + 1];
-  for (int k = 0; k < kWordsPerThread; ++k) {
-    const int w = w0 + k;
-    if (w >= nW) break;
-    uint32_t m = cbits[w];
-    mbits[w] = m;
-    if (!m) continue;
-    cbits[w] = 0;
-    while (m) {
-      const int bit = __ffs(m) - 1;
-      m &= m - 1;
-      const int v = w * 32 + bit;
-      const int val = vd[v];
-      q_ids[pc] = v;
-      q_vals[pc] = val;
-      q_scan[pc] = pd;
+  __syncthreads();
+  int bq = part[2 * blockIdx.x], bd = part[2 * blockIdx.x + 1];
+  for (int w = 0; w < warp; ++w) {
+    bq += s_q[w];
+    bd += s_d[w];
+  }
+  const uint32_t mine = (w0 + lane < nW) ? cbits[w0 + lane] : 0u;
+  if (w0 + lane < nW) {
+    mbits[w0 + lane] = mine;
+    if (mine) cbits[w0 + lane] = 0u;
+  }
+  for (int i = 0; i < kQWordsPerWarp; ++i) {
+    const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
+    if (!word) continue;
+    const int v = (w0 + i) * 32 + lane;
+    const bool member = (word >> lane) & 1u;
+    int deg = 0, val = 0, off = 0;
+    if (member) {
+      off = csr_off[v];
+      deg = csr_off[v + 1] - off;
+      val = vd[v];
       snap[v] = val;
-      ++pc;
-      pd += csr_off[v + 1] - csr_off[v];
     }
+    const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
+    const int incl = warp_incl_sum_i(deg);
+    if (deg > 0) {
+      const int pos = bq + __popc(qb & ((1u << lane) - 1u));
+      const int end = bd + incl;
+      q_ids[pos] = v;
+      q_vals[pos] = val;
+      q_end[pos] = end;
+      q_delta[pos] = off - (end - deg);
+    }
+    bq += __popc(qb);
+    bd += __shfl_sync(0xffffffffu, incl, 31);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) q_scan[cnt->n_changed] = cnt->n_scatter_edges;
 }
 
 // ---------------------------------------------------------------------------
@@ -244,31 +303,37 @@ struct BfsPushPol {
 
 template <class Pol>
 __global__ void __launch_bounds__(kNT)
-    k_push(Pol pol, SegSource src, const gas_counters *cnt) {
+    k_push(Pol pol, gasdev::SlabSource src, const gas_counters *cnt) {
   if (cnt->mode != kModePush) return;
-  gasdev::tile_loop<Pol, false, false>(pol, src, nullptr, nullptr, nullptr);
+  gasdev::slab_loop<Pol, false>(pol, src, nullptr, nullptr, nullptr);
 }
 
 __global__ void __launch_bounds__(kNT)
-    k_bfs_push(BfsPushPol pol, SegSource src, const gas_counters *cnt) {
+    k_bfs_push(BfsPushPol pol, gasdev::SlabSource src, const gas_counters *cnt) {
   if (cnt->mode != kModePush) return;
   pol.level = cnt->iteration;
-  gasdev::tile_loop<BfsPushPol, false, false>(pol, src, nullptr, nullptr, nullptr);
+  gasdev::slab_loop<BfsPushPol, false>(pol, src, nullptr, nullptr, nullptr);
 }
 
-// Tile boundaries of the frontier queue, only when this iteration pushes.
+// Chunk partitions of the frontier queue, only when this iteration pushes.
 __global__ void __launch_bounds__(256)
-    k_push_partition(SegSource src, int32_t *part, const gas_counters *cnt) {
+    k_push_partition(gasdev::SlabSource src, int32_t *part, const gas_counters *cnt) {
   if (cnt->mode != kModePush) return;
-  constexpr int kTile = gasdev::TileShape<sizeof(int32_t)>::kTile;
-  int nA, E;
-  gasdev::seg_sizes(src, nA, E);
-  const int64_t M = (int64_t)nA + E;
-  const int ntiles = (int)((M + kTile - 1) / kTile);
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles;
-       t += gridDim.x * blockDim.x) {
-    const int64_t d = (int64_t)t * kTile < M ? (int64_t)t * kTile : M;
-    part[t] = gasdev::merge_path(src.scan + 1, nA, E, (int)d);
+  int nS, E;
+  gasdev::slab_sizes(src, nS, E);
+  const int nchunks = (E + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks;
+       c += gridDim.x * blockDim.x) {
+    const int e = c * gasdev::kSlabChunk;
+    int lo = 0, hi = nS;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (src.ends[mid] <= e)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    part[c] = lo;
   }
 }
 
@@ -304,18 +369,18 @@ struct PullPol {
 
 template <class Pol>
 __global__ void __launch_bounds__(kNT)
-    k_pull(Pol pol, SegSource src, int32_t *tf, int32_t *tc, int32_t *ta0,
+    k_pull(Pol pol, gasdev::SlabSource src, int32_t *cf, int32_t *cc, int32_t *ca0,
            const gas_counters *cnt) {
   if (cnt->mode != kModePull) return;
-  gasdev::tile_loop<Pol, true, true>(pol, src, tf, tc, ta0);
+  gasdev::slab_loop<Pol, true>(pol, src, cf, cc, ca0);
 }
 
 template <class Pol>
 __global__ void __launch_bounds__(kNT)
-    k_pull_fixup(Pol pol, SegSource src, const int32_t *tf, const int32_t *tc,
-                 const int32_t *ta0, const gas_counters *cnt) {
+    k_pull_fixup(Pol pol, gasdev::SlabSource src, const int32_t *cf, const int32_t *cc,
+                 const int32_t *ca0, const gas_counters *cnt) {
   if (cnt->mode != kModePull) return;
-  gasdev::fixup_loop<Pol, true>(pol, src, tf, tc, ta0);
+  gasdev::slab_fixup_loop<Pol>(pol, src, cf, cc, ca0);
 }
 
 // ---------------------------------------------------------------------------
@@ -336,12 +401,15 @@ __device__ __forceinline__ void pick_mode(gas_counters *cnt, int nE) {
   cnt->mode = mode;
 }
 
+// seeded: the prologue only built the iteration-0 sender set, iteration 0
+// itself runs in the loop (and always exists: A_0 = V is not empty).
 __global__ void k_fast_precond(gas_counters *cnt, cudaGraphConditionalHandle h,
-                               int nE, int in_graph) {
-  cnt->iteration = 1;  // iteration 0 ran in the prologue
-  const bool more = cnt->n_scatter_edges > 0;
-  if (more && 1 >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
-  cnt->cond = (more && 1 < cnt->max_iter) ? 1 : 0;
+                               int nE, int in_graph, int seeded) {
+  const int done = seeded ? 0 : 1;  // iterations run by the prologue
+  cnt->iteration = done;
+  const bool more = seeded ? true : cnt->n_scatter_edges > 0;
+  if (more && done >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
+  cnt->cond = (more && done < cnt->max_iter) ? 1 : 0;
   pick_mode(cnt, nE);
   if (in_graph) cudaGraphSetConditional(h, cnt->cond);
 }
@@ -380,6 +448,7 @@ __global__ void k_fast_finish(gas_counters *cnt) {
 struct FastCtx {
   int nW;
   int n_qblocks;
+  bool seeded;  // iteration 0 from the full range via the finite-value seed
 };
 
 gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c) {
@@ -387,14 +456,27 @@ gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c) {
   k_q_spine<<<1, kNT, 0, cs>>>(e->qpart, c.n_qblocks, e->cnt);
   k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->mbits, e->csr_off, c.nW,
                                          e->qpart, (const int32_t *)e->vd,
-                                         e->q_ids, e->q_vals, e->q_scan,
-                                         e->snap, e->cnt);
+                                         e->q_ids, e->q_vals, e->q_end, e->q_delta,
+                                         e->snap);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
 
+gasdev::SlabSource dense_csc(const gas_engine *e) {
+  return gasdev::slab_source(e->ne_end, e->ne_vid, nullptr, e->n_ne, e->nE, nullptr,
+                             nullptr, e->slab_dpart);
+}
+
 gas_status_t prologue(gas_engine *e, cudaStream_t cs, void *vctx) {
   const FastCtx &c = *static_cast<const FastCtx *>(vctx);
+  if (c.seeded) {
+    const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
+    k_seed_finite<<<2 * e->num_sms, kNT, 0, cs>>>((const int32_t *)e->vd, e->nV,
+                                                  zero_cap, e->cbits);
+    CUDA_TRY(cudaGetLastError());
+    gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, cs>>>(dense_csc(e), e->slab_dpart);
+    return compaction(e, cs, c);
+  }
   // iteration 0: the generic kernels on the caller's active set
   e->level_from_counters = true;
   if (e->prog == GAS_PROG_BFS) {
@@ -406,57 +488,43 @@ gas_status_t prologue(gas_engine *e, cudaStream_t cs, void *vctx) {
   e->level_from_counters = false;
   k_seed_changed<<<8 * e->num_sms, kNT, 0, cs>>>(e->act, e->ret, e->cnt, e->cbits);
   CUDA_TRY(cudaGetLastError());
-  if (e->prog != GAS_PROG_BFS) {  // tile boundaries of the dense pull
-    constexpr int kTile = gasdev::TileShape<sizeof(int32_t)>::kTile;
-    gasdev::k_partition<kTile, true><<<2 * e->num_sms, 256, 0, cs>>>(
-        gasdev::dense_source(e->csc_off, e->nV, e->nE, e->dpart), e->dpart);
-  }
+  if (e->prog != GAS_PROG_BFS)  // chunk boundaries of the dense pull
+    gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, cs>>>(dense_csc(e), e->slab_dpart);
   return compaction(e, cs, c);
 }
 
 gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
                   void *vctx) {
   const FastCtx &c = *static_cast<const FastCtx *>(vctx);
-  const SegSource qsrc = gasdev::frontier_source(
-      e->q_ids, e->q_scan, e->csr_off, &e->cnt->n_changed,
-      &e->cnt->n_scatter_edges, e->tpart);
-  k_push_partition<<<2 * e->num_sms, 256, 0, cs>>>(qsrc, e->tpart, e->cnt);
-  int per_sm = 0;
+  const gasdev::SlabSource qsrc = gasdev::slab_source(
+      e->q_end, e->q_ids, e->q_delta, 0, 0, &e->cnt->n_changed,
+      &e->cnt->n_scatter_edges, e->slab_qpart);
+  k_push_partition<<<2 * e->num_sms, 256, 0, cs>>>(qsrc, e->slab_qpart, e->cnt);
+  const int grid = 8 * e->num_sms;  // 64 warps per SM
   const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
+  const gasdev::SlabSource dsrc = dense_csc(e);
+  int32_t *cf = (int32_t *)e->slab_first, *cc = (int32_t *)e->slab_carry;
   if (e->prog == GAS_PROG_BFS) {
     BfsPushPol pol{e->csr_dst, (int32_t *)e->vd, e->cbits, 0};
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_push, kNT, 0);
-    k_bfs_push<<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(pol, qsrc, e->cnt);
+    k_bfs_push<<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
   } else if (e->prog == GAS_PROG_SSSP) {
     PushPol<true> pol{e->csr_dst, (const int32_t *)e->csr_ed, e->q_vals,
                       (int32_t *)e->vd, e->cbits, zero_cap};
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_push<PushPol<true>>, kNT, 0);
-    k_push<PushPol<true>><<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(
-        pol, qsrc, e->cnt);
+    k_push<PushPol<true>><<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
     PullPol<true> pp{e->csc_src, (const int32_t *)e->csc_ed, e->mbits, e->snap,
                      (int32_t *)e->vd, e->cbits, zero_cap};
-    const SegSource dsrc = gasdev::dense_source(e->csc_off, e->nV, e->nE, e->dpart);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<PullPol<true>>, kNT, 0);
-    k_pull<PullPol<true>><<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(
-        pp, dsrc, (int32_t *)e->tile_first, (int32_t *)e->tile_carry, e->tile_a0, e->cnt);
-    k_pull_fixup<PullPol<true>><<<4 * e->num_sms, kNT, 0, cs>>>(
-        pp, dsrc, (const int32_t *)e->tile_first, (const int32_t *)e->tile_carry,
-        e->tile_a0, e->cnt);
+    k_pull<PullPol<true>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->cnt);
+    k_pull_fixup<PullPol<true>><<<2 * e->num_sms, kNT, 0, cs>>>(pp, dsrc, cf, cc,
+                                                                e->slab_a0, e->cnt);
   } else {
     PushPol<false> pol{e->csr_dst, nullptr, e->q_vals, (int32_t *)e->vd, e->cbits,
                        zero_cap};
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_push<PushPol<false>>, kNT, 0);
-    k_push<PushPol<false>><<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(
-        pol, qsrc, e->cnt);
+    k_push<PushPol<false>><<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
     PullPol<false> pp{e->csc_src, nullptr, e->mbits, e->snap, (int32_t *)e->vd,
                       e->cbits, zero_cap};
-    const SegSource dsrc = gasdev::dense_source(e->csc_off, e->nV, e->nE, e->dpart);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<PullPol<false>>, kNT, 0);
-    k_pull<PullPol<false>><<<e->num_sms * (per_sm > 0 ? per_sm : 1), kNT, 0, cs>>>(
-        pp, dsrc, (int32_t *)e->tile_first, (int32_t *)e->tile_carry, e->tile_a0, e->cnt);
-    k_pull_fixup<PullPol<false>><<<4 * e->num_sms, kNT, 0, cs>>>(
-        pp, dsrc, (const int32_t *)e->tile_first, (const int32_t *)e->tile_carry,
-        e->tile_a0, e->cnt);
+    k_pull<PullPol<false>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->cnt);
+    k_pull_fixup<PullPol<false>><<<2 * e->num_sms, kNT, 0, cs>>>(pp, dsrc, cf, cc,
+                                                                 e->slab_a0, e->cnt);
   }
   CUDA_TRY(cudaGetLastError());
   GAS_TRY(compaction(e, cs, c));
@@ -468,10 +536,11 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
 gas_status_t ensure_fast_buffers(gas_engine *e) {
   if (e->q_ids) return GAS_OK;
   const size_t V = (size_t)e->nV, nW = (V + 31) / 32;
-  const size_t nqb = (nW + kCompactBlock - 1) / kCompactBlock;
+  const size_t nqb = (nW + kQWordsPerBlock - 1) / kQWordsPerBlock;
   CUDA_TRY(cudaMalloc(&e->q_ids, (V ? V : 1) * 4));
   CUDA_TRY(cudaMalloc(&e->q_vals, (V ? V : 1) * 4));
-  CUDA_TRY(cudaMalloc(&e->q_scan, (V + 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->q_end, (V ? V : 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->q_delta, (V ? V : 1) * 4));
   CUDA_TRY(cudaMalloc(&e->snap, (V ? V : 1) * 4));
   CUDA_TRY(cudaMalloc(&e->cbits, (nW ? nW : 1) * 4));
   CUDA_TRY(cudaMalloc(&e->mbits, (nW ? nW : 1) * 4));
@@ -507,7 +576,8 @@ static gas_status_t build_fast_graph(gas_engine *e, FastCtx *ctx,
   e->in_graph = true;
   st = prologue(e, cs, ctx);
   if (st == GAS_OK) {
-    k_fast_precond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE, e->in_graph ? 1 : 0);
+    k_fast_precond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE, e->in_graph ? 1 : 0,
+                                    ctx->seeded ? 1 : 0);
     ce = cudaGetLastError();
     if (ce != cudaSuccess) st = fail(GAS_ERR_CUDA, "precond: %s", cudaGetErrorString(ce));
   }
@@ -573,9 +643,11 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
   GAS_TRY(ensure_fast_buffers(e));
   FastCtx ctx;
   ctx.nW = (e->nV + 31) / 32;
-  ctx.n_qblocks = (ctx.nW + kCompactBlock - 1) / kCompactBlock;
+  ctx.n_qblocks = (ctx.nW + kQWordsPerBlock - 1) / kQWordsPerBlock;
   if (ctx.n_qblocks < 1) ctx.n_qblocks = 1;
-  const int slot = kGraphFast0;
+  ctx.seeded = e->prog != GAS_PROG_BFS && e->active_full && !e->counts_dirty &&
+               e->n_active == e->nV;
+  const int slot = kGraphFast0 + (ctx.seeded ? 1 : 0);
   const bool host_loop = host_loop_requested();
   if (!host_loop && !e->graphs[slot]) GAS_TRY(build_fast_graph(e, &ctx, &e->graphs[slot]));
   const int forced = schedule == GAS_SCHED_PUSH ? 1 : schedule == GAS_SCHED_PULL ? 2 : 0;
@@ -587,7 +659,7 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
       e->in_graph = false;
       gas_status_t pst = prologue(e, S(stream), &ctx);
       if (pst == GAS_OK) {
-        k_fast_precond<<<1, 1, 0, S(stream)>>>(e->cnt, 0, e->nE, 0);
+        k_fast_precond<<<1, 1, 0, S(stream)>>>(e->cnt, 0, e->nE, 0, ctx.seeded ? 1 : 0);
         ce = cudaGetLastError();
       }
       e->capturing = false;
@@ -613,11 +685,13 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     // prologue (gather/apply, fixup, commit | bfs apply; seed; 3 compaction;
     // precond) + per iteration (push, pull, pull fixup | bfs push;
     // 3 compaction; cond) + reset + finish
-    const int pro = e->prog == GAS_PROG_BFS ? 6 : 10;
+    const int pro = e->prog == GAS_PROG_BFS ? 6 : (ctx.seeded ? 6 : 10);
     const int per = e->prog == GAS_PROG_BFS ? 6 : 8;
-    stats->kernel_launches = pro + per * (c.iteration > 0 ? c.iteration - 1 : 0) + 2;
+    const int loop_iters = ctx.seeded ? c.iteration : (c.iteration > 0 ? c.iteration - 1 : 0);
+    stats->kernel_launches = pro + per * loop_iters + 2;
   }
   e->level = c.iteration;
+  e->active_full = false;
   return loop_status(e, c, stream);
 }
 

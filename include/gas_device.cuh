@@ -26,6 +26,7 @@
 #define GAS_DEVICE_CUH_
 
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -474,6 +475,211 @@ __global__ void __launch_bounds__(kNT)
     const typename P::GatherResult g = gres ? gres[i] : P::gatherZero;
     ret[i] = P::apply(vd + act[i], g) ? 1 : 0;
   }
+}
+
+
+// ---------------------------------------------------------------------------
+// Warp-slab segmented passes (dense CSC pulls, PageRank, frontier pushes).
+//
+// The segments here are never empty (vertices without edges are handled
+// apart), so a 32-edge slab contains at most 31 segment boundaries.  Each
+// warp streams a contiguous chunk of kSlabChunk edges, 32 at a time: one
+// coalesced load of the next 32 segment ends gives, through
+// __reduce_or_sync + popc, the segment of every lane's edge; a 5-step
+// shuffle segmented scan folds the slab; the last lane of each segment that
+// ends in the slab emits it; a segment that runs past the slab is carried in
+// registers.  No shared memory and no CTA barriers.  Segments split across
+// chunks leave a per-chunk carry folded by slab_fixup_loop in chunk order.
+// ---------------------------------------------------------------------------
+constexpr int kSlabChunk = 32 * 16;  // edges per warp chunk
+
+struct SlabSource {
+  const int32_t *ends;     // [n_seg] exclusive end of segment k in the virtual
+                           // edge range, strictly increasing
+  const int32_t *vid;      // [n_seg] vertex of segment k (null: k itself)
+  const int32_t *delta;    // [n_seg] array position - virtual index (null: 0)
+  int32_t n_seg;
+  int32_t n_edge;
+  const int32_t *n_seg_p;  // device counters, or null
+  const int32_t *n_edge_p;
+  const int32_t *part;     // [n_chunks] segment holding each chunk's first edge
+};
+
+__device__ __forceinline__ void slab_sizes(const SlabSource &s, int &nS, int &E) {
+  nS = s.n_seg_p ? *s.n_seg_p : s.n_seg;
+  E = s.n_edge_p ? *s.n_edge_p : s.n_edge;
+}
+
+// Segment of each chunk's first edge: the first k with ends[k] > e.
+template <int kChunk = kSlabChunk>
+__global__ void __launch_bounds__(256) k_slab_partition(SlabSource src, int32_t *part) {
+  int nS, E;
+  slab_sizes(src, nS, E);
+  const int nchunks = (E + kChunk - 1) / kChunk;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks;
+       c += gridDim.x * blockDim.x) {
+    const int e = c * kChunk;
+    int lo = 0, hi = nS;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(src.ends + mid) <= e)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    part[c] = lo;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ T shfl_any(const T &v, int src_lane) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  int w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int k = 0; k < W; ++k) w[k] = __shfl_sync(0xffffffffu, w[k], src_lane);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+// Pol as for tile_loop: Val, zero(), reduce(), map(seg, vertex, pos),
+// emit(seg, vertex, Val) when kReduce; visit(seg, vertex, pos) otherwise.
+template <class Pol, bool kReduce>
+__device__ __forceinline__ void slab_loop(Pol &pol, const SlabSource src,
+                                          typename Pol::Val *ch_first,
+                                          typename Pol::Val *ch_carry,
+                                          int32_t *ch_a0) {
+  using Val = typename Pol::Val;
+  constexpr unsigned FULL = 0xffffffffu;
+  int nS, E;
+  slab_sizes(src, nS, E);
+  const int nchunks = (E + kSlabChunk - 1) / kSlabChunk;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int c = gwarp; c < nchunks; c += nwarps) {
+    const int e0 = c * kSlabChunk;
+    const int e1 = e0 + kSlabChunk < E ? e0 + kSlabChunk : E;
+    int r = __ldg(src.part + c);
+    const int r_first = r;
+    bool open_first = false;
+    if (kReduce) open_first = (r > 0 ? __ldg(src.ends + r - 1) : 0) < e0;
+    int wbase = r;
+    int b = (r + lane < nS) ? __ldg(src.ends + r + lane) : INT_MAX;
+    Val carry = pol.zero();
+    bool have_carry = false;
+    bool first_done = false;
+    for (int s = e0; s < e1; s += 32) {
+      int shift = r - wbase;
+      const int b31 = __shfl_sync(FULL, b, 31);
+      if (shift > 0 && b31 <= s + 31) {  // window used up: reload at r
+        wbase = r;
+        shift = 0;
+        b = (r + lane < nS) ? __ldg(src.ends + r + lane) : INT_MAX;
+      }
+      const int k = b - s;
+      const unsigned bit = (lane >= shift && k >= 1 && k <= 31) ? (1u << k) : 0u;
+      const unsigned mask = __reduce_or_sync(FULL, bit);
+      const unsigned upto = mask & ((2u << lane) - 1u);
+      const int row = r + __popc(upto);
+      const int e = s + lane;
+      const bool valid = e < e1;
+      int v = row, pos = e;
+      if (valid) {
+        if (src.vid) v = __ldg(src.vid + row);
+        if (src.delta) pos = e + __ldg(src.delta + row);
+      }
+      const int row_end = __shfl_sync(FULL, b, row - wbase);
+      const bool ends_here = valid && row_end == e + 1;
+      const int last = e1 - s - 1 < 31 ? e1 - s - 1 : 31;
+      const int row_last = __shfl_sync(FULL, row, last);
+      const bool end_last = __shfl_sync(FULL, (int)ends_here, last) != 0;
+      if constexpr (!kReduce) {
+        if (valid) pol.visit(row, v, pos);
+      } else {
+        Val val = valid ? pol.map(row, v, pos) : pol.zero();
+        if (lane == 0 && have_carry) val = pol.reduce(carry, val);
+        const unsigned hb = (mask | 1u) & ((2u << lane) - 1u);
+        const int seg_start = 31 - __clz(hb);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const Val t = shfl_up_any(val, d);
+          if (lane - d >= seg_start) val = pol.reduce(t, val);
+        }
+        const bool to_first = ends_here && open_first && row == r_first;
+        if (ends_here) {
+          if (to_first)
+            ch_first[c] = val;
+          else
+            pol.emit(row, v, val);
+        }
+        first_done = first_done || __any_sync(FULL, to_first);
+        const Val v_last = shfl_any(val, last);
+        have_carry = !end_last;
+        if (have_carry) carry = v_last;
+      }
+      r = end_last ? row_last + 1 : row_last;
+    }
+    if constexpr (kReduce) {
+      if (lane == 0) {
+        ch_carry[c] = have_carry ? carry : pol.zero();
+        ch_a0[c] = (open_first && first_done) ? r_first : -1;
+      }
+    }
+  }
+}
+
+// Completes segments split across chunks (one warp per chunk, ordered fold).
+template <class Pol>
+__device__ __forceinline__ void slab_fixup_loop(Pol &pol, const SlabSource src,
+                                                const typename Pol::Val *ch_first,
+                                                const typename Pol::Val *ch_carry,
+                                                const int32_t *ch_a0) {
+  using Val = typename Pol::Val;
+  int nS, E;
+  slab_sizes(src, nS, E);
+  const int nchunks = (E + kSlabChunk - 1) / kSlabChunk;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int c = gwarp; c < nchunks; c += nwarps) {
+    const int row = ch_a0[c];
+    if (row < 0) continue;
+    const int start = row > 0 ? __ldg(src.ends + row - 1) : 0;
+    const int c_first = start / kSlabChunk;
+    Val acc = pol.zero();
+    for (int q = c_first; q < c; q += 32) {
+      Val x = (q + lane < c) ? ch_carry[q + lane] : pol.zero();
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const Val y = shfl_down_any(x, d);
+        if (lane + d < 32) x = pol.reduce(x, y);
+      }
+      acc = pol.reduce(acc, x);
+    }
+    if (lane == 0) {
+      const int v = src.vid ? __ldg(src.vid + row) : row;
+      pol.emit(row, v, pol.reduce(acc, ch_first[c]));
+    }
+  }
+}
+
+__host__ __device__ inline SlabSource slab_source(const int32_t *ends, const int32_t *vid,
+                                                  const int32_t *delta, int n_seg,
+                                                  int n_edge, const int32_t *n_seg_p,
+                                                  const int32_t *n_edge_p,
+                                                  const int32_t *part) {
+  SlabSource s;
+  s.ends = ends;
+  s.vid = vid;
+  s.delta = delta;
+  s.n_seg = n_seg;
+  s.n_edge = n_edge;
+  s.n_seg_p = n_seg_p;
+  s.n_edge_p = n_edge_p;
+  s.part = part;
+  return s;
 }
 
 }  // namespace gasdev
