@@ -258,7 +258,7 @@ def run_ours(args, rank, world):
     # per-algorithm split and the dominant kernel's roofline (untimed pass)
     split = per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources,
                            args.schedule, sp, stream)
-    roof = gather_roofline(e_s, dev_s[0], ssp, sp, stream)
+    roof = kernel_roofline(e_s, e_c, dev_s, dev_c, ssp, ccg, args.schedule, sp)
     peak, peak_kind = measured_peaks()
     roof["peak"] = peak
     roof["frac"] = roof["achieved"] / peak
@@ -321,36 +321,44 @@ def per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources, 
     return out
 
 
-def gather_roofline(e_s, dev_init, ssp, sp, stream):
-    """Times every launch of the load-balanced gather (+ fused apply) of one
-    SSSP run with CUDA events on its stream; algorithmic bytes per launch:
-    per active vertex 20 B (id, in-degree scan entry, row offset, own state
-    read, state write) and per in-edge 12 B (source id, source state,
-    weight)."""
+def kernel_roofline(e_s, e_c, dev_s, dev_c, ssp, ccg, schedule, sp):
+    """One extra pass of the step's runs with kernel profiling on: the engine
+    brackets every push / dense-pull launch with CUDA events on the run's
+    stream and accumulates its algorithmic bytes (per edge: index, weight for
+    SSSP, and the state or membership word it reads; per frontier entry or
+    row: 16 B).  The dominant kernel is the one with the larger total time."""
     import torch
-    e_s.upload_vertex_data_ptr(dev_init.data_ptr(), sp)
-    e_s.setActive(0, ssp.nV, sp)
-    total_ms, total_bytes, launches = 0.0, 0, 0
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    while e_s.countActive():
-        c = e_s.counters()
-        e_s.gather(True, sp)
-        a.record(stream)
-        e_s.apply(sp)
-        b.record(stream)
-        torch.cuda.synchronize()
-        total_ms += a.elapsed_time(b)
-        total_bytes += 20 * c.n_active + 12 * c.n_edges
-        launches += 1
-        e_s.scatterActivate(True, sp)
-        e_s.nextIter(sp)
-    achieved = total_bytes / (total_ms * 1e-3) / 1e9
-    return {"kernel": "k_gather_tiles+k_gather_fixup (SSSP pull, apply fused)",
-            "bound": "hbm", "achieved": round(achieved, 1), "unit": "GB/s",
-            "traffic": None, "launches": launches,
-            "algorithmic_bytes_per_launch": int(total_bytes / max(1, launches)),
-            "avg_launch_ms": round(total_ms / max(1, launches), 4)}
+    for e in (e_s, e_c):
+        e.set_profiling(True)
+        e.profile(reset=True)
+    for k in range(len(dev_s)):
+        e_s.upload_vertex_data_ptr(dev_s[k].data_ptr(), sp)
+        e_s.setActive(0, ssp.nV, sp)
+        e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
+    e_c.upload_vertex_data_ptr(dev_c.data_ptr(), sp)
+    e_c.setActive(0, ccg.nV, sp)
+    e_c.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
+    torch.cuda.synchronize()
+    ps, pc = e_s.profile(), e_c.profile()
+    for e in (e_s, e_c):
+        e.set_profiling(False)
+    kinds = {}
+    for name in ("push", "pull"):
+        ms = getattr(ps, f"{name}_ms") + getattr(pc, f"{name}_ms")
+        by = getattr(ps, f"{name}_bytes") + getattr(pc, f"{name}_bytes")
+        n = getattr(ps, f"{name}_launches") + getattr(pc, f"{name}_launches")
+        kinds[name] = {"ms": ms, "bytes": by, "launches": n,
+                       "achieved_gbs": (by / (ms * 1e-3) / 1e9) if ms > 0 else 0.0}
+    dom = max(kinds, key=lambda k: kinds[k]["ms"])
+    d = kinds[dom]
+    return {"kernel": {"pull": "k_pull (dense pull, warp-slab)",
+                       "push": "k_push (frontier push, warp-slab)"}[dom],
+            "bound": "hbm", "achieved": round(d["achieved_gbs"], 1), "unit": "GB/s",
+            "traffic": None, "launches": d["launches"],
+            "algorithmic_bytes_per_launch": int(d["bytes"] / max(1, d["launches"])),
+            "avg_launch_ms": round(d["ms"] / max(1, d["launches"]), 4),
+            "by_kernel": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv)
+                              for kk, vv in v.items()} for k, v in kinds.items()}}
 
 
 # ---------------------------------------------------------------------------

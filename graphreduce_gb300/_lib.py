@@ -48,6 +48,13 @@ class RunStats(C.Structure):
                 ("residual", c_dbl)]
 
 
+class KernelProfile(C.Structure):
+    _fields_ = [("push_ms", c_dbl), ("pull_ms", c_dbl), ("pagerank_ms", c_dbl),
+                ("push_bytes", c_i64), ("pull_bytes", c_i64), ("pagerank_bytes", c_i64),
+                ("push_launches", c_i32), ("pull_launches", c_i32),
+                ("pagerank_launches", c_i32), ("pad", c_i32)]
+
+
 class Counters(C.Structure):
     _fields_ = [("n_active", c_i32), ("n_edges", c_i32), ("n_scatter_edges", c_i32),
                 ("error", c_i32), ("iteration", c_i32), ("cond", c_i32),
@@ -98,6 +105,8 @@ _SIGS = {
                                                  C.POINTER(RunStats), c_vp]),
     "gas_pagerank_step_noalloc": ("status", [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,
                                              c_dbl, c_vp, c_vp]),
+    "gas_engine_set_profiling": ("status", [c_vp, c_i32]),
+    "gas_engine_get_profile": ("status", [c_vp, C.POINTER(KernelProfile), c_i32]),
     "gas_engine_view_get": ("status", [c_vp, c_vp]),
     "gas_engine_note_applied": ("status", [c_vp, c_i32]),
     "gas_engine_read_counters": ("status", [c_vp, C.POINTER(Counters), c_vp]),

@@ -467,7 +467,7 @@ void free_graph(gas_engine *e) {
   dfree(e->qpart); dfree(e->cbits); dfree(e->mbits);
   dfree(e->ne_vid); dfree(e->ne_end); dfree(e->zero_vid);
   dfree(e->slab_dpart); dfree(e->slab_qpart); dfree(e->slab_a0);
-  dfree(e->slab_first); dfree(e->slab_carry);
+  dfree(e->slab_first); dfree(e->slab_carry); dfree(e->slab_fix); dfree(e->slab_fix_n);
   e->n_ne = e->n_zero = e->slab_cap = 0;
   for (int i = 0; i < kGraphSlots; ++i) {
     if (e->graphs[i]) cudaGraphExecDestroy(e->graphs[i]);
@@ -706,6 +706,8 @@ gas_status_t gas_engine_create_user(size_t vertex_bytes, size_t gather_bytes,
 void gas_engine_destroy(gas_engine *e) {
   if (!e) return;
   free_graph(e);
+  for (int i = 0; i < 2; ++i)
+    if (e->prof_ev[i]) cudaEventDestroy(e->prof_ev[i]);
   if (e->h_cnt) cudaFreeHost(e->h_cnt);
   delete e;
 }
@@ -828,6 +830,8 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   GAS_TRY(dalloc(&e->slab_a0, (size_t)e->slab_cap));
   GAS_TRY(dalloc((uint8_t **)&e->slab_first, (size_t)e->slab_cap * 8));
   GAS_TRY(dalloc((uint8_t **)&e->slab_carry, (size_t)e->slab_cap * 8));
+  GAS_TRY(dalloc(&e->slab_fix, (size_t)e->slab_cap));
+  GAS_TRY(dalloc(&e->slab_fix_n, 1));
 
   cudaStream_t st = S(stream);
   if (!ne_vid.empty()) {
@@ -850,6 +854,7 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   if (V)
     CUDA_TRY(cudaMemcpyAsync(e->vd, vertex_data, V * e->vbytes, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemsetAsync(e->bits, 0, nW * 4, st));
+  CUDA_TRY(cudaMemsetAsync(e->slab_fix_n, 0, sizeof(int32_t), st));
   CUDA_TRY(cudaMemsetAsync(e->cnt, 0, sizeof(gas_counters), st));
   CUDA_TRY(cudaMemsetAsync(e->ret, 0, V ? V : 1, st));
   // the host vectors are released at return: wait for the copies
@@ -1031,6 +1036,24 @@ gas_status_t gas_engine_note_applied(gas_engine *e, int32_t wrote_slots) {
   return GAS_OK;
 }
 
+gas_status_t gas_engine_set_profiling(gas_engine *e, int32_t on) {
+  if (!e) return gas::fail(GAS_ERR_INVALID, "null engine");
+  if (on) {
+    for (int i = 0; i < 2; ++i)
+      if (!e->prof_ev[i]) CUDA_TRY(cudaEventCreate(&e->prof_ev[i]));
+  }
+  e->profiling = on != 0;
+  return GAS_OK;
+}
+
+gas_status_t gas_engine_get_profile(gas_engine *e, gas_kernel_profile *out,
+                                    int32_t reset) {
+  if (!e || !out) return gas::fail(GAS_ERR_INVALID, "null argument");
+  *out = e->prof;
+  if (reset) e->prof = gas_kernel_profile{};
+  return GAS_OK;
+}
+
 gas_status_t gas_engine_read_counters(gas_engine *e, gas_counters *out,
                                       void *stream) {
   if (!e || !out || !e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
@@ -1046,6 +1069,35 @@ gas_status_t gas_engine_read_counters(gas_engine *e, gas_counters *out,
 // gas_runs.cu; they reach the engine through these accessors.
 // ---------------------------------------------------------------------------
 namespace gas {
+
+void prof_begin(gas_engine *e, cudaStream_t s, int kind, int64_t bytes) {
+  if (!e->profiling || e->in_graph || !e->prof_ev[0]) return;
+  cudaEventRecord(e->prof_ev[0], s);
+  e->prof_kind = kind;
+  e->prof_bytes_pending = bytes;
+}
+
+void prof_end(gas_engine *e, cudaStream_t s) {
+  if (e->prof_kind < 0) return;
+  cudaEventRecord(e->prof_ev[1], s);
+}
+
+void prof_collect(gas_engine *e) {
+  if (e->prof_kind < 0) return;
+  float ms = 0.f;
+  if (cudaEventSynchronize(e->prof_ev[1]) == cudaSuccess &&
+      cudaEventElapsedTime(&ms, e->prof_ev[0], e->prof_ev[1]) == cudaSuccess) {
+    gas_kernel_profile &p = e->prof;
+    if (e->prof_kind == kProfPush) {
+      p.push_ms += ms; p.push_bytes += e->prof_bytes_pending; ++p.push_launches;
+    } else if (e->prof_kind == kProfPull) {
+      p.pull_ms += ms; p.pull_bytes += e->prof_bytes_pending; ++p.pull_launches;
+    } else {
+      p.pagerank_ms += ms; p.pagerank_bytes += e->prof_bytes_pending; ++p.pagerank_launches;
+    }
+  }
+  e->prof_kind = -1;
+}
 
 gas_status_t engine_scatter(gas_engine *e, void *stream) {
   return scatter_common(e, stream);

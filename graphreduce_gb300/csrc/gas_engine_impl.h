@@ -83,6 +83,8 @@ struct gas_engine {
   // warp-slab chunk state: partitions of the dense CSC and of the push
   // queue, per-chunk carries (8-byte values) and fixup rows
   int32_t *slab_dpart = nullptr, *slab_qpart = nullptr, *slab_a0 = nullptr;
+  int32_t *slab_fix = nullptr;      // chunks needing a fixup, [slab_cap]
+  int32_t *slab_fix_n = nullptr;    // their count (reset after each fixup)
   void *slab_first = nullptr, *slab_carry = nullptr;
   int32_t slab_cap = 0;
 
@@ -95,6 +97,12 @@ struct gas_engine {
   int32_t level = 0;
   int num_sms = 0;
   bool has_graph = false;
+  // kernel profiling (gas_engine_set_profiling)
+  bool profiling = false;
+  cudaEvent_t prof_ev[2] = {nullptr, nullptr};
+  int prof_kind = -1;           // kernel bracketed in the current iteration
+  int64_t prof_bytes_pending = 0;
+  gas_kernel_profile prof = {};
   bool active_full = false;          // active set is [0, nV) from set_active
   bool capturing = false;            // fixed grids (graph capture / host loop)
   bool in_graph = false;             // loop kernels set a graph condition
@@ -120,6 +128,12 @@ int engine_partition_grid(gas_engine *e, int64_t items, int tile);
 // of the condition per iteration (the kernels are the same; ncu cannot
 // profile kernels inside graphs with conditional nodes).
 bool host_loop_requested();
+// Profiling hooks: bracket one kernel of the current iteration (host loop
+// only) and fold its time into the profile once the iteration has run.
+enum { kProfPush = 0, kProfPull = 1, kProfPagerank = 2 };
+void prof_begin(gas_engine *e, cudaStream_t s, int kind, int64_t bytes);
+void prof_end(gas_engine *e, cudaStream_t s);
+void prof_collect(gas_engine *e);
 }  // namespace gas
 
 #endif  // GAS_ENGINE_IMPL_H_

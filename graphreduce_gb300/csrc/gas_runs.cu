@@ -109,6 +109,10 @@ bool host_loop_requested() {
   return v && v[0] == '1';
 }
 
+bool host_loop_for(const gas_engine *e) {
+  return e->profiling || host_loop_requested();
+}
+
 // The same loop without a graph: body launches on the stream, the host
 // reads the condition word after every iteration.
 gas_status_t run_host_loop(
@@ -131,6 +135,7 @@ gas_status_t run_host_loop(
     if (!e->h_cnt->cond) break;
     st = body(e, s, 0, ctx);
     if (st != GAS_OK) break;
+    prof_collect(e);
   }
   e->capturing = false;
   return st;
@@ -191,7 +196,7 @@ extern "C" gas_status_t gas_engine_run_schedule(gas_engine *e,
 
   GenericCtx ctx{schedule == GAS_SCHED_ORDERED};
   const int slot = ctx.ordered ? kGraphOrdered : kGraphGeneric;
-  if (gas::host_loop_requested()) {
+  if (gas::host_loop_for(e)) {
     k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
     CUDA_TRY(cudaGetLastError());
     e->level_from_counters = true;
@@ -245,6 +250,7 @@ __device__ __forceinline__ PrVal two_sum_add(const PrVal &a, const PrVal &b) {
 
 struct PrPol {
   typedef PrVal Val;
+  static constexpr bool kMapNeedsVertex = false;
   const int32_t *csc_src;
   const int32_t *csr_off;
   const float *contrib;
@@ -300,18 +306,19 @@ __device__ __forceinline__ void block_sum_store(double v, double *out) {
 
 __global__ void __launch_bounds__(kNT)
     k_pr_slab(PrPol pol, PrBufs bufs, gasdev::SlabSource src, PrVal *cf, PrVal *cc,
-              int32_t *ca0, const gas_counters *cnt, double *l1_part) {
+              int32_t *ca0, int32_t *fix, int32_t *fix_n, const gas_counters *cnt,
+              double *l1_part) {
   pr_bind(pol, bufs, cnt);
-  gasdev::slab_loop<PrPol, true>(pol, src, cf, cc, ca0);
+  gasdev::slab_loop<PrPol, true>(pol, src, cf, cc, ca0, fix, fix_n);
   block_sum_store(pol.l1, l1_part + blockIdx.x);
 }
 
 __global__ void __launch_bounds__(kNT)
     k_pr_fixup(PrPol pol, PrBufs bufs, gasdev::SlabSource src, const PrVal *cf,
-               const PrVal *cc, const int32_t *ca0, const gas_counters *cnt,
-               double *l1_part) {
+               const PrVal *cc, const int32_t *ca0, const int32_t *fix,
+               const int32_t *fix_n, const gas_counters *cnt, double *l1_part) {
   pr_bind(pol, bufs, cnt);
-  gasdev::slab_fixup_loop<PrPol>(pol, src, cf, cc, ca0);
+  gasdev::slab_fixup_loop<PrPol>(pol, src, cf, cc, ca0, fix, fix_n);
   block_sum_store(pol.l1, l1_part + blockIdx.x);
 }
 
@@ -329,7 +336,7 @@ __global__ void __launch_bounds__(kNT)
 // Deterministic sum of the per-CTA residuals; sets the loop condition.
 __global__ void __launch_bounds__(kNT)
     k_pr_finish(const double *l1_part, int n, const double *tol_p,
-                gas_counters *cnt, double *residual,
+                gas_counters *cnt, double *residual, int32_t *fix_n,
                 cudaGraphConditionalHandle h, int in_graph) {
   __shared__ double s[kNT];
   double v = 0.0;
@@ -343,6 +350,7 @@ __global__ void __launch_bounds__(kNT)
   if (threadIdx.x == 0) {
     const double l1 = s[0];
     const double tol = *tol_p;
+    *fix_n = 0;  // the fixup of this iteration has run
     const int max_iter = cnt->max_iter;
     *residual = l1;
     const int it = ++cnt->iteration;
@@ -376,17 +384,23 @@ struct PrCtx {
 gas_status_t pr_body(gas_engine *e, cudaStream_t cs,
                      cudaGraphConditionalHandle h, void *vctx) {
   PrCtx *c = static_cast<PrCtx *>(vctx);
+  // algorithmic bytes of one iteration: per edge its source index and the
+  // source's contribution; per vertex offsets, old and new rank, new
+  // contribution
+  gas::prof_begin(e, cs, gas::kProfPagerank, 8LL * e->nE + 16LL * e->nV);
   k_pr_slab<<<c->tiles_grid, kNT, 0, cs>>>(
       c->pol, c->bufs, c->src, (PrVal *)e->slab_first, (PrVal *)e->slab_carry,
-      e->slab_a0, e->cnt, e->pr_l1);
+      e->slab_a0, e->slab_fix, e->slab_fix_n, e->cnt, e->pr_l1);
   k_pr_fixup<<<c->fix_grid, kNT, 0, cs>>>(
       c->pol, c->bufs, c->src, (const PrVal *)e->slab_first,
-      (const PrVal *)e->slab_carry, e->slab_a0, e->cnt, e->pr_l1 + c->tiles_grid);
+      (const PrVal *)e->slab_carry, e->slab_a0, e->slab_fix, e->slab_fix_n, e->cnt,
+      e->pr_l1 + c->tiles_grid);
+  gas::prof_end(e, cs);
   k_pr_empty<<<c->empty_grid, kNT, 0, cs>>>(c->pol, c->bufs, e->zero_vid, e->n_zero,
                                             e->cnt,
                                             e->pr_l1 + c->tiles_grid + c->fix_grid);
   k_pr_finish<<<1, kNT, 0, cs>>>(e->pr_l1, c->tiles_grid + c->fix_grid + c->empty_grid,
-                                 c->residual + 1, e->cnt, c->residual, h,
+                                 c->residual + 1, e->cnt, c->residual, e->slab_fix_n, h,
                                  e->in_graph ? 1 : 0);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
@@ -409,7 +423,9 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
     if (!e->pr_contrib[i]) CUDA_TRY(cudaMalloc(&e->pr_contrib[i], (size_t)nV * 4));
   }
   PrCtx c;
-  c.tiles_grid = 8 * e->num_sms;  // 64 resident warps per SM
+  int per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pr_slab, kNT, 0));
+  c.tiles_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);  // resident CTAs only
   c.fix_grid = 2 * e->num_sms;
   c.empty_grid = 2 * e->num_sms;
   const int nparts = c.tiles_grid + c.fix_grid + c.empty_grid;
@@ -439,7 +455,7 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
     cudaGraphExecDestroy(e->graphs[kGraphPagerank]);
     e->graphs[kGraphPagerank] = nullptr;
   }
-  const bool host_loop = gas::host_loop_requested();
+  const bool host_loop = gas::host_loop_for(e);
   if (!host_loop && !e->graphs[kGraphPagerank]) {
     GAS_TRY(gas::build_while_graph(e, pr_body, &c, &e->graphs[kGraphPagerank]));
     e->pr_damping = damping;

@@ -128,36 +128,75 @@ __device__ __forceinline__ int warp_incl_sum_i(int v) {
   return v;
 }
 
+// A warp owns 32 bitmap words.  Sparse warps (few set bits) give each lane
+// one word and walk its set bits; dense warps walk the words one at a time
+// with one lane per vertex, so the out-degree loads are coalesced.
+constexpr int kQDenseBits = 96;
+
+struct QLane {
+  uint32_t word;  // this lane's bitmap word
+  bool dense;     // warp-uniform
+};
+
+__device__ __forceinline__ QLane q_lane(const uint32_t *cbits, int nW, int w0) {
+  const int lane = threadIdx.x & 31;
+  QLane q;
+  q.word = (w0 + lane < nW) ? cbits[w0 + lane] : 0u;
+  q.dense = __reduce_add_sync(0xffffffffu, (unsigned)__popc(q.word)) > kQDenseBits;
+  return q;
+}
+
 // per-warp (queue entries, out-edges) of its 32 words
-__device__ __forceinline__ void q_warp_counts(const uint32_t *cbits,
-                                              const int32_t *csr_off, int nW,
+__device__ __forceinline__ void q_warp_counts(const QLane &ql, const int32_t *csr_off,
                                               int w0, int *cq, int *cd) {
   const int lane = threadIdx.x & 31;
-  const uint32_t mine = (w0 + lane < nW) ? cbits[w0 + lane] : 0u;
   int q = 0, d = 0;
-  for (int i = 0; i < kQWordsPerWarp; ++i) {
-    const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
-    if (!word) continue;
-    const int v = (w0 + i) * 32 + lane;
-    int deg = 0;
-    if ((word >> lane) & 1u) deg = csr_off[v + 1] - csr_off[v];
-    q += __popc(__ballot_sync(0xffffffffu, deg > 0));
-    d += deg;
+  if (ql.dense) {
+    for (int i = 0; i < kQWordsPerWarp; ++i) {
+      const uint32_t word = __shfl_sync(0xffffffffu, ql.word, i);
+      if (!word) continue;
+      const int v = (w0 + i) * 32 + lane;
+      int deg = 0;
+      if ((word >> lane) & 1u) deg = csr_off[v + 1] - csr_off[v];
+      q += deg > 0;
+      d += deg;
+    }
+  } else {
+    uint32_t m = ql.word;
+    while (m) {
+      const int bit = __ffs(m) - 1;
+      m &= m - 1;
+      const int v = (w0 + lane) * 32 + bit;
+      const int deg = csr_off[v + 1] - csr_off[v];
+      q += deg > 0;
+      d += deg;
+    }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    q += __shfl_xor_sync(0xffffffffu, q, o);
+    d += __shfl_xor_sync(0xffffffffu, d, o);
+  }
   *cq = q;
   *cd = d;
 }
 
+// Counts per block; first resets the snapshots of the previous queue (its
+// length is still in the counters) to Program::gatherZero.
 __global__ void __launch_bounds__(kNT)
     k_q_count(const uint32_t *cbits, const int32_t *csr_off, int nW,
-              int32_t *part) {
+              int32_t *part, const int32_t *q_ids, int32_t *snap, int32_t zero,
+              const gas_counters *cnt) {
+  const int n_old = cnt->n_changed;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old;
+       i += gridDim.x * blockDim.x)
+    snap[q_ids[i]] = zero;
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
+  const QLane ql = q_lane(cbits, nW, w0);
   int cq, cd;
-  q_warp_counts(cbits, csr_off, nW, blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp,
-                &cq, &cd);
+  q_warp_counts(ql, csr_off, w0, &cq, &cd);
   if (lane == 0) {
     s_q[warp] = cq;
     s_d[warp] = cd;
@@ -205,14 +244,15 @@ __global__ void __launch_bounds__(kNT)
 }
 
 __global__ void __launch_bounds__(kNT)
-    k_q_write(uint32_t *cbits, uint32_t *mbits, const int32_t *csr_off, int nW,
-              const int32_t *part, const int32_t *vd, int32_t *q_ids,
-              int32_t *q_vals, int32_t *q_end, int32_t *q_delta, int32_t *snap) {
+    k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int32_t *part,
+              const int32_t *vd, int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
+              int32_t *q_delta, int32_t *snap) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
+  const QLane ql = q_lane(cbits, nW, w0);
   int cq, cd;
-  q_warp_counts(cbits, csr_off, nW, w0, &cq, &cd);
+  q_warp_counts(ql, csr_off, w0, &cq, &cd);
   if (lane == 0) {
     s_q[warp] = cq;
     s_d[warp] = cd;
@@ -223,35 +263,64 @@ __global__ void __launch_bounds__(kNT)
     bq += s_q[w];
     bd += s_d[w];
   }
-  const uint32_t mine = (w0 + lane < nW) ? cbits[w0 + lane] : 0u;
-  if (w0 + lane < nW) {
-    mbits[w0 + lane] = mine;
-    if (mine) cbits[w0 + lane] = 0u;
-  }
-  for (int i = 0; i < kQWordsPerWarp; ++i) {
-    const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
-    if (!word) continue;
-    const int v = (w0 + i) * 32 + lane;
-    const bool member = (word >> lane) & 1u;
-    int deg = 0, val = 0, off = 0;
-    if (member) {
-      off = csr_off[v];
-      deg = csr_off[v + 1] - off;
-      val = vd[v];
-      snap[v] = val;
+  if (ql.word) cbits[w0 + lane] = 0u;
+  if (ql.dense) {
+    for (int i = 0; i < kQWordsPerWarp; ++i) {
+      const uint32_t word = __shfl_sync(0xffffffffu, ql.word, i);
+      if (!word) continue;
+      const int v = (w0 + i) * 32 + lane;
+      int deg = 0, off = 0;
+      if ((word >> lane) & 1u) {
+        off = csr_off[v];
+        deg = csr_off[v + 1] - off;
+      }
+      const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
+      const int incl = warp_incl_sum_i(deg);
+      if (deg > 0) {
+        const int val = vd[v];
+        const int pos = bq + __popc(qb & ((1u << lane) - 1u));
+        const int end = bd + incl;
+        q_ids[pos] = v;
+        q_vals[pos] = val;
+        q_end[pos] = end;
+        q_delta[pos] = off - (end - deg);
+        snap[v] = val;
+      }
+      bq += __popc(qb);
+      bd += __shfl_sync(0xffffffffu, incl, 31);
     }
-    const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
-    const int incl = warp_incl_sum_i(deg);
-    if (deg > 0) {
-      const int pos = bq + __popc(qb & ((1u << lane) - 1u));
-      const int end = bd + incl;
-      q_ids[pos] = v;
-      q_vals[pos] = val;
-      q_end[pos] = end;
-      q_delta[pos] = off - (end - deg);
+  } else {
+    // lane-local counts first, then a warp scan gives each lane its offsets
+    int lq = 0, ld = 0;
+    uint32_t m = ql.word;
+    while (m) {
+      const int bit = __ffs(m) - 1;
+      m &= m - 1;
+      const int v = (w0 + lane) * 32 + bit;
+      const int deg = csr_off[v + 1] - csr_off[v];
+      lq += deg > 0;
+      ld += deg;
     }
-    bq += __popc(qb);
-    bd += __shfl_sync(0xffffffffu, incl, 31);
+    int pq = warp_incl_sum_i(lq) - lq + bq;
+    int pd = warp_incl_sum_i(ld) - ld + bd;
+    m = ql.word;
+    while (m) {
+      const int bit = __ffs(m) - 1;
+      m &= m - 1;
+      const int v = (w0 + lane) * 32 + bit;
+      const int off = csr_off[v];
+      const int deg = csr_off[v + 1] - off;
+      if (deg > 0) {
+        const int val = vd[v];
+        pd += deg;
+        q_ids[pq] = v;
+        q_vals[pq] = val;
+        q_end[pq] = pd;
+        q_delta[pq] = off - (pd - deg);
+        snap[v] = val;
+        ++pq;
+      }
+    }
   }
 }
 
@@ -261,6 +330,7 @@ __global__ void __launch_bounds__(kNT)
 template <bool kWeighted>
 struct PushPol {
   typedef int32_t Val;
+  static constexpr bool kMapNeedsVertex = false;
   const int32_t *csr_dst;
   const int32_t *csr_w;
   const int32_t *q_vals;
@@ -285,6 +355,7 @@ struct PushPol {
 
 struct BfsPushPol {
   typedef int32_t Val;
+  static constexpr bool kMapNeedsVertex = false;
   const int32_t *csr_dst;
   int32_t *depth;
   uint32_t *cbits;
@@ -305,14 +376,15 @@ template <class Pol>
 __global__ void __launch_bounds__(kNT)
     k_push(Pol pol, gasdev::SlabSource src, const gas_counters *cnt) {
   if (cnt->mode != kModePush) return;
-  gasdev::slab_loop<Pol, false>(pol, src, nullptr, nullptr, nullptr);
+  gasdev::slab_loop<Pol, false>(pol, src, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
 __global__ void __launch_bounds__(kNT)
     k_bfs_push(BfsPushPol pol, gasdev::SlabSource src, const gas_counters *cnt) {
   if (cnt->mode != kModePush) return;
   pol.level = cnt->iteration;
-  gasdev::slab_loop<BfsPushPol, false>(pol, src, nullptr, nullptr, nullptr);
+  gasdev::slab_loop<BfsPushPol, false>(pol, src, nullptr, nullptr, nullptr, nullptr,
+                                       nullptr);
 }
 
 // Chunk partitions of the frontier queue, only when this iteration pushes.
@@ -343,20 +415,21 @@ __global__ void __launch_bounds__(256)
 template <bool kWeighted>
 struct PullPol {
   typedef int32_t Val;
+  static constexpr bool kMapNeedsVertex = false;
+  static constexpr bool kIntMin = true;  // reduce is min over int
   const int32_t *csc_src;
   const int32_t *csc_w;
-  const uint32_t *mbits;
-  const int32_t *snap;
+  const int32_t *snap;   // value of u at the end of iteration k if u is in
+                         // C_k (and has out-edges), else Program::gatherZero
   int32_t *vd;
   uint32_t *cbits;
   int32_t zero_cap;
   __device__ Val zero() const { return INT_MAX; }
   __device__ __forceinline__ Val reduce(Val a, Val b) const { return a < b ? a : b; }
   __device__ __forceinline__ Val map(int, int, int pos) const {
-    const uint32_t u = (uint32_t)__ldg(csc_src + pos);
-    if (!((__ldg(mbits + (u >> 5)) >> (u & 31)) & 1u)) return INT_MAX;
-    int c = __ldg(snap + u);
-    if (kWeighted) c += __ldg(csc_w + pos);
+    const int u = __ldg(csc_src + pos);
+    int c = kWeighted ? __ldg(csc_w + pos) : 0;
+    c += snap[u];  // a non-member gives gatherZero (+w), which changes nothing
     return c > zero_cap ? zero_cap : c;
   }
   __device__ __forceinline__ void emit(int, int v, Val g) const {
@@ -370,17 +443,18 @@ struct PullPol {
 template <class Pol>
 __global__ void __launch_bounds__(kNT)
     k_pull(Pol pol, gasdev::SlabSource src, int32_t *cf, int32_t *cc, int32_t *ca0,
-           const gas_counters *cnt) {
+           int32_t *fix, int32_t *fix_n, const gas_counters *cnt) {
   if (cnt->mode != kModePull) return;
-  gasdev::slab_loop<Pol, true>(pol, src, cf, cc, ca0);
+  gasdev::slab_loop<Pol, true>(pol, src, cf, cc, ca0, fix, fix_n);
 }
 
 template <class Pol>
 __global__ void __launch_bounds__(kNT)
     k_pull_fixup(Pol pol, gasdev::SlabSource src, const int32_t *cf, const int32_t *cc,
-                 const int32_t *ca0, const gas_counters *cnt) {
+                 const int32_t *ca0, const int32_t *fix, const int32_t *fix_n,
+                 const gas_counters *cnt) {
   if (cnt->mode != kModePull) return;
-  gasdev::slab_fixup_loop<Pol>(pol, src, cf, cc, ca0);
+  gasdev::slab_fixup_loop<Pol>(pol, src, cf, cc, ca0, fix, fix_n);
 }
 
 // ---------------------------------------------------------------------------
@@ -415,7 +489,8 @@ __global__ void k_fast_precond(gas_counters *cnt, cudaGraphConditionalHandle h,
 }
 
 __global__ void k_fast_cond(gas_counters *cnt, cudaGraphConditionalHandle h,
-                            int nE, int in_graph) {
+                            int nE, int in_graph, int32_t *fix_n) {
+  *fix_n = 0;  // the pull fixup of this iteration has run
   if (cnt->mode == kModePush)
     ++cnt->n_push;
   else
@@ -438,6 +513,7 @@ __global__ void k_fast_reset(gas_counters *cnt, int max_iter, int forced,
   cnt->pad[0] = forced;
   cnt->pull_div = pull_div;
   cnt->mode = kModePush;
+  cnt->n_changed = 0;  // no previous queue whose snapshots need resetting
 }
 
 __global__ void k_fast_finish(gas_counters *cnt) {
@@ -448,16 +524,21 @@ __global__ void k_fast_finish(gas_counters *cnt) {
 struct FastCtx {
   int nW;
   int n_qblocks;
+  int slab_grid;  // resident CTAs of the slab kernels
   bool seeded;  // iteration 0 from the full range via the finite-value seed
 };
 
+int32_t snap_zero(const gas_engine *e) {
+  return e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
+}
+
 gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c) {
-  k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart);
+  k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart,
+                                         e->q_ids, e->snap, snap_zero(e), e->cnt);
   k_q_spine<<<1, kNT, 0, cs>>>(e->qpart, c.n_qblocks, e->cnt);
-  k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->mbits, e->csr_off, c.nW,
-                                         e->qpart, (const int32_t *)e->vd,
-                                         e->q_ids, e->q_vals, e->q_end, e->q_delta,
-                                         e->snap);
+  k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart,
+                                         (const int32_t *)e->vd, e->q_ids, e->q_vals,
+                                         e->q_end, e->q_delta, e->snap);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -467,8 +548,14 @@ gasdev::SlabSource dense_csc(const gas_engine *e) {
                              nullptr, e->slab_dpart);
 }
 
+__global__ void k_fill(int32_t *p, int32_t v, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
 gas_status_t prologue(gas_engine *e, cudaStream_t cs, void *vctx) {
   const FastCtx &c = *static_cast<const FastCtx *>(vctx);
+  k_fill<<<2 * e->num_sms, kNT, 0, cs>>>(e->snap, snap_zero(e), e->nV);
   if (c.seeded) {
     const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
     k_seed_finite<<<2 * e->num_sms, kNT, 0, cs>>>((const int32_t *)e->vd, e->nV,
@@ -500,10 +587,22 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
       e->q_end, e->q_ids, e->q_delta, 0, 0, &e->cnt->n_changed,
       &e->cnt->n_scatter_edges, e->slab_qpart);
   k_push_partition<<<2 * e->num_sms, 256, 0, cs>>>(qsrc, e->slab_qpart, e->cnt);
-  const int grid = 8 * e->num_sms;  // 64 warps per SM
+  const int grid = c.slab_grid;  // resident CTAs only (persistent warps)
   const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
   const gasdev::SlabSource dsrc = dense_csc(e);
   int32_t *cf = (int32_t *)e->slab_first, *cc = (int32_t *)e->slab_carry;
+  // profiling (host loop only): the mode of this iteration was read back
+  // with the counters before the launch
+  const bool prof_pull = e->profiling && !e->in_graph && e->h_cnt->mode == kModePull;
+  const int64_t wbytes = e->prog == GAS_PROG_SSSP ? 4 : 0;
+  if (e->profiling && !e->in_graph) {
+    if (prof_pull)  // per edge index (+ weight) + state or bitmap; per row 16 B
+      gas::prof_begin(e, cs, gas::kProfPull, (8 + wbytes) * e->nE + 16LL * e->n_ne);
+    else  // per pushed edge dst (+ weight) + state; per queue entry 16 B
+      gas::prof_begin(e, cs, gas::kProfPush,
+                      (8 + wbytes) * (int64_t)e->h_cnt->n_scatter_edges +
+                          16LL * e->h_cnt->n_changed);
+  }
   if (e->prog == GAS_PROG_BFS) {
     BfsPushPol pol{e->csr_dst, (int32_t *)e->vd, e->cbits, 0};
     k_bfs_push<<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
@@ -511,24 +610,26 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
     PushPol<true> pol{e->csr_dst, (const int32_t *)e->csr_ed, e->q_vals,
                       (int32_t *)e->vd, e->cbits, zero_cap};
     k_push<PushPol<true>><<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
-    PullPol<true> pp{e->csc_src, (const int32_t *)e->csc_ed, e->mbits, e->snap,
-                     (int32_t *)e->vd, e->cbits, zero_cap};
-    k_pull<PullPol<true>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->cnt);
-    k_pull_fixup<PullPol<true>><<<2 * e->num_sms, kNT, 0, cs>>>(pp, dsrc, cf, cc,
-                                                                e->slab_a0, e->cnt);
+    PullPol<true> pp{e->csc_src, (const int32_t *)e->csc_ed, e->snap, (int32_t *)e->vd,
+                     e->cbits, zero_cap};
+    k_pull<PullPol<true>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->slab_fix,
+                                                e->slab_fix_n, e->cnt);
+    k_pull_fixup<PullPol<true>><<<2 * e->num_sms, kNT, 0, cs>>>(
+        pp, dsrc, cf, cc, e->slab_a0, e->slab_fix, e->slab_fix_n, e->cnt);
   } else {
     PushPol<false> pol{e->csr_dst, nullptr, e->q_vals, (int32_t *)e->vd, e->cbits,
                        zero_cap};
     k_push<PushPol<false>><<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
-    PullPol<false> pp{e->csc_src, nullptr, e->mbits, e->snap, (int32_t *)e->vd,
-                      e->cbits, zero_cap};
-    k_pull<PullPol<false>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->cnt);
-    k_pull_fixup<PullPol<false>><<<2 * e->num_sms, kNT, 0, cs>>>(pp, dsrc, cf, cc,
-                                                                 e->slab_a0, e->cnt);
+    PullPol<false> pp{e->csc_src, nullptr, e->snap, (int32_t *)e->vd, e->cbits, zero_cap};
+    k_pull<PullPol<false>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->slab_fix,
+                                                 e->slab_fix_n, e->cnt);
+    k_pull_fixup<PullPol<false>><<<2 * e->num_sms, kNT, 0, cs>>>(
+        pp, dsrc, cf, cc, e->slab_a0, e->slab_fix, e->slab_fix_n, e->cnt);
   }
   CUDA_TRY(cudaGetLastError());
+  gas::prof_end(e, cs);
   GAS_TRY(compaction(e, cs, c));
-  k_fast_cond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE, e->in_graph ? 1 : 0);
+  k_fast_cond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE, e->in_graph ? 1 : 0, e->slab_fix_n);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -645,10 +746,15 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
   ctx.nW = (e->nV + 31) / 32;
   ctx.n_qblocks = (ctx.nW + kQWordsPerBlock - 1) / kQWordsPerBlock;
   if (ctx.n_qblocks < 1) ctx.n_qblocks = 1;
+  {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<PullPol<true>>, kNT, 0);
+    ctx.slab_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);
+  }
   ctx.seeded = e->prog != GAS_PROG_BFS && e->active_full && !e->counts_dirty &&
                e->n_active == e->nV;
   const int slot = kGraphFast0 + (ctx.seeded ? 1 : 0);
-  const bool host_loop = host_loop_requested();
+  const bool host_loop = host_loop_for(e);
   if (!host_loop && !e->graphs[slot]) GAS_TRY(build_fast_graph(e, &ctx, &e->graphs[slot]));
   const int forced = schedule == GAS_SCHED_PUSH ? 1 : schedule == GAS_SCHED_PULL ? 2 : 0;
   k_fast_reset<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations, forced, e->pull_div);
@@ -685,7 +791,7 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     // prologue (gather/apply, fixup, commit | bfs apply; seed; 3 compaction;
     // precond) + per iteration (push, pull, pull fixup | bfs push;
     // 3 compaction; cond) + reset + finish
-    const int pro = e->prog == GAS_PROG_BFS ? 6 : (ctx.seeded ? 6 : 10);
+    const int pro = e->prog == GAS_PROG_BFS ? 7 : (ctx.seeded ? 7 : 11);
     const int per = e->prog == GAS_PROG_BFS ? 6 : 8;
     const int loop_iters = ctx.seeded ? c.iteration : (c.iteration > 0 ? c.iteration - 1 : 0);
     stats->kernel_launches = pro + per * loop_iters + 2;

@@ -25,6 +25,8 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
                       int32_t max_iterations, gas_run_stats *stats,
                       void *stream);
 
+bool host_loop_for(const gas_engine *e);
+
 // The loop of build_while_graph as direct launches (GAS_HOST_LOOP=1).
 gas_status_t run_host_loop(
     gas_engine *e,

@@ -163,6 +163,15 @@ class GASEngineGPU:
         (synchronises the stream)."""
         L.call("gas_engine_download_vertex_data", self._h, ptr, _stream_ptr(stream))
 
+    def set_profiling(self, on: bool) -> None:
+        """Kernel-level timing of later runs (direct launches, CUDA events)."""
+        L.call("gas_engine_set_profiling", self._h, int(on))
+
+    def profile(self, reset: bool = True) -> L.KernelProfile:
+        p = L.KernelProfile()
+        L.call("gas_engine_get_profile", self._h, C.byref(p), int(reset))
+        return p
+
     def counters(self) -> L.Counters:
         c = L.Counters()
         L.call("gas_engine_read_counters", self._h, C.byref(c), None)

@@ -269,6 +269,23 @@ gas_status_t gas_pagerank_step_noalloc(int32_t nV, int32_t nE,
                                        double damping, double *l1_out,
                                        void *stream);
 
+/* Kernel-level measurement of the fast runs.  With profiling on, runs use
+ * direct launches (one host read per iteration) and bracket the dominant
+ * kernels with CUDA events on the run's stream; times and algorithmic bytes
+ * (the bytes the work itself must move: per edge its index, weight and the
+ * state it reads; per vertex its offsets and state) accumulate until
+ * reset.  No reference counterpart. */
+typedef struct {
+  double push_ms, pull_ms, pagerank_ms;        /* summed kernel time        */
+  int64_t push_bytes, pull_bytes, pagerank_bytes;
+  int32_t push_launches, pull_launches, pagerank_launches;
+  int32_t pad;
+} gas_kernel_profile;
+
+gas_status_t gas_engine_set_profiling(gas_engine *e, int32_t on);
+gas_status_t gas_engine_get_profile(gas_engine *e, gas_kernel_profile *out,
+                                    int32_t reset);
+
 /* ======================================================================= */
 /* Views used by include/gpugas.h to launch its Program-typed kernels.     */
 /* ======================================================================= */

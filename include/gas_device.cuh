@@ -543,15 +543,109 @@ __device__ __forceinline__ T shfl_any(const T &v, int src_lane) {
   return r;
 }
 
+// Policy traits of the slab passes (defaults: vertex ids loaded for map /
+// visit, ordered shuffle scan).  A policy may declare
+//   static constexpr bool kMapNeedsVertex = false;  // map/visit ignore it
+//   static constexpr bool kIntMin = true;           // Val is int, reduce is min
+template <class Pol, class = void>
+struct NeedsVertex { static constexpr bool value = true; };
+template <class Pol>
+struct NeedsVertex<Pol, decltype((void)Pol::kMapNeedsVertex, void())> {
+  static constexpr bool value = Pol::kMapNeedsVertex;
+};
+template <class Pol, class = void>
+struct IntMin { static constexpr bool value = false; };
+template <class Pol>
+struct IntMin<Pol, decltype((void)Pol::kIntMin, void())> {
+  static constexpr bool value = Pol::kIntMin;
+};
+
+// Segment of every lane's edge in one 32-edge slab starting at s.
+struct SlabRows {
+  int row;
+  bool valid;
+  bool ends_here;  // this lane holds the last edge of its segment
+  unsigned mask;   // bit l: lane l starts a new segment (l >= 1)
+  int r_next;      // segment of the next slab's first edge
+  bool end_last;   // the slab's last edge ends its segment
+};
+
+__device__ __forceinline__ SlabRows slab_rows(const SlabSource &src, int nS, int s,
+                                              int e1, int r, int &wbase, int &b,
+                                              int lane) {
+  constexpr unsigned FULL = 0xffffffffu;
+  int shift = r - wbase;
+  const int b31 = __shfl_sync(FULL, b, 31);
+  if (shift > 0 && b31 <= s + 31) {  // window used up: reload at r
+    wbase = r;
+    shift = 0;
+    b = (r + lane < nS) ? __ldg(src.ends + r + lane) : INT_MAX;
+  }
+  SlabRows o;
+  const int last = e1 - s - 1 < 31 ? e1 - s - 1 : 31;
+  const int end_r = __shfl_sync(FULL, b, shift);  // end of segment r
+  if (end_r > s + last) {
+    // the whole slab lies in segment r (most slabs of high-degree rows)
+    o.mask = 0u;
+    o.row = r;
+    o.valid = s + lane < e1;
+    o.ends_here = o.valid && end_r == s + lane + 1;
+    o.end_last = end_r == s + last + 1;
+    o.r_next = o.end_last ? r + 1 : r;
+    return o;
+  }
+  const int k = b - s;
+  const unsigned bit = (lane >= shift && k >= 1 && k <= 31) ? (1u << k) : 0u;
+  o.mask = __reduce_or_sync(FULL, bit);
+  o.row = r + __popc(o.mask & ((2u << lane) - 1u));
+  const int e = s + lane;
+  o.valid = e < e1;
+  const int row_end = __shfl_sync(FULL, b, o.row - wbase);
+  o.ends_here = o.valid && row_end == e + 1;
+  const int row_last = __shfl_sync(FULL, o.row, last);
+  o.end_last = __shfl_sync(FULL, (int)o.ends_here, last) != 0;
+  o.r_next = o.end_last ? row_last + 1 : row_last;
+  return o;
+}
+
+// Inclusive fold of each segment's lanes (segment heads: lane 0 and the
+// bits of mask); the last lane of a segment holds the segment's fold.
+template <class Pol>
+__device__ __forceinline__ typename Pol::Val slab_fold(const Pol &pol,
+                                                       typename Pol::Val val,
+                                                       unsigned mask, int lane) {
+  const unsigned heads = mask | 1u;
+  const int seg_start = 31 - __clz(heads & ((2u << lane) - 1u));
+  if constexpr (IntMin<Pol>::value) {
+    const unsigned above = heads & ~((2u << lane) - 1u);
+    const int seg_end = above ? __ffs(above) - 2 : 31;
+    const unsigned hi = seg_end == 31 ? 0xffffffffu : ((2u << seg_end) - 1u);
+    const unsigned group = hi & ~((1u << seg_start) - 1u);
+    return __reduce_min_sync(group, val);
+  } else {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const typename Pol::Val t = shfl_up_any(val, d);
+      if (lane - d >= seg_start) val = pol.reduce(t, val);
+    }
+    return val;
+  }
+}
+
 // Pol as for tile_loop: Val, zero(), reduce(), map(seg, vertex, pos),
 // emit(seg, vertex, Val) when kReduce; visit(seg, vertex, pos) otherwise.
+// Two slabs are in flight per iteration so that their load chains overlap.
+// Chunks whose first segment started in an earlier chunk and ends here are
+// appended to fix_list (row in ch_a0[c]) for slab_fixup_loop.
 template <class Pol, bool kReduce>
 __device__ __forceinline__ void slab_loop(Pol &pol, const SlabSource src,
                                           typename Pol::Val *ch_first,
                                           typename Pol::Val *ch_carry,
-                                          int32_t *ch_a0) {
+                                          int32_t *ch_a0, int32_t *fix_list,
+                                          int32_t *fix_count) {
   using Val = typename Pol::Val;
   constexpr unsigned FULL = 0xffffffffu;
+  constexpr bool kVert = NeedsVertex<Pol>::value;
   int nS, E;
   slab_sizes(src, nS, E);
   const int nchunks = (E + kSlabChunk - 1) / kSlabChunk;
@@ -564,88 +658,104 @@ __device__ __forceinline__ void slab_loop(Pol &pol, const SlabSource src,
     int r = __ldg(src.part + c);
     const int r_first = r;
     bool open_first = false;
-    if (kReduce) open_first = (r > 0 ? __ldg(src.ends + r - 1) : 0) < e0;
+    if constexpr (kReduce) open_first = (r > 0 ? __ldg(src.ends + r - 1) : 0) < e0;
     int wbase = r;
     int b = (r + lane < nS) ? __ldg(src.ends + r + lane) : INT_MAX;
     Val carry = pol.zero();
     bool have_carry = false;
     bool first_done = false;
-    for (int s = e0; s < e1; s += 32) {
-      int shift = r - wbase;
-      const int b31 = __shfl_sync(FULL, b, 31);
-      if (shift > 0 && b31 <= s + 31) {  // window used up: reload at r
-        wbase = r;
-        shift = 0;
-        b = (r + lane < nS) ? __ldg(src.ends + r + lane) : INT_MAX;
+    for (int s = e0; s < e1; s += 64) {
+      const bool two = s + 32 < e1;
+      const SlabRows A = slab_rows(src, nS, s, e1, r, wbase, b, lane);
+      SlabRows B = A;
+      if (two) B = slab_rows(src, nS, s + 32, e1, A.r_next, wbase, b, lane);
+      // positions and the (independent) loads of both slabs
+      const int eA = s + lane, eB = s + 32 + lane;
+      int posA = eA, posB = eB, vA = A.row, vB = B.row;
+      if (A.valid) {
+        if (src.delta) posA += __ldg(src.delta + A.row);
+        if (kVert && src.vid) vA = __ldg(src.vid + A.row);
       }
-      const int k = b - s;
-      const unsigned bit = (lane >= shift && k >= 1 && k <= 31) ? (1u << k) : 0u;
-      const unsigned mask = __reduce_or_sync(FULL, bit);
-      const unsigned upto = mask & ((2u << lane) - 1u);
-      const int row = r + __popc(upto);
-      const int e = s + lane;
-      const bool valid = e < e1;
-      int v = row, pos = e;
-      if (valid) {
-        if (src.vid) v = __ldg(src.vid + row);
-        if (src.delta) pos = e + __ldg(src.delta + row);
+      if (two && B.valid) {
+        if (src.delta) posB += __ldg(src.delta + B.row);
+        if (kVert && src.vid) vB = __ldg(src.vid + B.row);
       }
-      const int row_end = __shfl_sync(FULL, b, row - wbase);
-      const bool ends_here = valid && row_end == e + 1;
-      const int last = e1 - s - 1 < 31 ? e1 - s - 1 : 31;
-      const int row_last = __shfl_sync(FULL, row, last);
-      const bool end_last = __shfl_sync(FULL, (int)ends_here, last) != 0;
       if constexpr (!kReduce) {
-        if (valid) pol.visit(row, v, pos);
+        if (A.valid) pol.visit(A.row, vA, posA);
+        if (two && B.valid) pol.visit(B.row, vB, posB);
+        r = two ? B.r_next : A.r_next;
       } else {
-        Val val = valid ? pol.map(row, v, pos) : pol.zero();
-        if (lane == 0 && have_carry) val = pol.reduce(carry, val);
-        const unsigned hb = (mask | 1u) & ((2u << lane) - 1u);
-        const int seg_start = 31 - __clz(hb);
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const Val t = shfl_up_any(val, d);
-          if (lane - d >= seg_start) val = pol.reduce(t, val);
+        Val valA = A.valid ? pol.map(A.row, vA, posA) : pol.zero();
+        Val valB = (two && B.valid) ? pol.map(B.row, vB, posB) : pol.zero();
+        // slab A
+        if (lane == 0 && have_carry) valA = pol.reduce(carry, valA);
+        valA = slab_fold(pol, valA, A.mask, lane);
+        {
+          const bool to_first = A.ends_here && open_first && A.row == r_first;
+          if (A.ends_here) {
+            if (to_first) {
+              ch_first[c] = valA;
+            } else {
+              const int v = (!kVert && src.vid) ? __ldg(src.vid + A.row) : vA;
+              pol.emit(A.row, v, valA);
+            }
+          }
+          first_done = first_done || __any_sync(FULL, to_first);
+          const int last = e1 - s - 1 < 31 ? e1 - s - 1 : 31;
+          const Val v_last = shfl_any(valA, last);
+          have_carry = !A.end_last;
+          if (have_carry) carry = v_last;
         }
-        const bool to_first = ends_here && open_first && row == r_first;
-        if (ends_here) {
-          if (to_first)
-            ch_first[c] = val;
-          else
-            pol.emit(row, v, val);
+        if (two) {
+          if (lane == 0 && have_carry) valB = pol.reduce(carry, valB);
+          valB = slab_fold(pol, valB, B.mask, lane);
+          const bool to_first = B.ends_here && open_first && B.row == r_first;
+          if (B.ends_here) {
+            if (to_first) {
+              ch_first[c] = valB;
+            } else {
+              const int v = (!kVert && src.vid) ? __ldg(src.vid + B.row) : vB;
+              pol.emit(B.row, v, valB);
+            }
+          }
+          first_done = first_done || __any_sync(FULL, to_first);
+          const int last = e1 - s - 33 < 31 ? e1 - s - 33 : 31;
+          const Val v_last = shfl_any(valB, last);
+          have_carry = !B.end_last;
+          if (have_carry) carry = v_last;
         }
-        first_done = first_done || __any_sync(FULL, to_first);
-        const Val v_last = shfl_any(val, last);
-        have_carry = !end_last;
-        if (have_carry) carry = v_last;
+        r = two ? B.r_next : A.r_next;
       }
-      r = end_last ? row_last + 1 : row_last;
     }
     if constexpr (kReduce) {
       if (lane == 0) {
         ch_carry[c] = have_carry ? carry : pol.zero();
-        ch_a0[c] = (open_first && first_done) ? r_first : -1;
+        if (open_first && first_done) {
+          ch_a0[c] = r_first;
+          fix_list[atomicAdd(fix_count, 1)] = c;
+        }
       }
     }
   }
 }
 
-// Completes segments split across chunks (one warp per chunk, ordered fold).
+// Completes segments split across chunks: one warp per listed chunk folds
+// the carries of the chunks the segment spans, in chunk order.
 template <class Pol>
 __device__ __forceinline__ void slab_fixup_loop(Pol &pol, const SlabSource src,
                                                 const typename Pol::Val *ch_first,
                                                 const typename Pol::Val *ch_carry,
-                                                const int32_t *ch_a0) {
+                                                const int32_t *ch_a0,
+                                                const int32_t *fix_list,
+                                                const int32_t *fix_count) {
   using Val = typename Pol::Val;
-  int nS, E;
-  slab_sizes(src, nS, E);
-  const int nchunks = (E + kSlabChunk - 1) / kSlabChunk;
+  const int n = *fix_count;
   const int lane = threadIdx.x & 31;
   const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-  for (int c = gwarp; c < nchunks; c += nwarps) {
+  for (int i = gwarp; i < n; i += nwarps) {
+    const int c = fix_list[i];
     const int row = ch_a0[c];
-    if (row < 0) continue;
     const int start = row > 0 ? __ldg(src.ends + row - 1) : 0;
     const int c_first = start / kSlabChunk;
     Val acc = pol.zero();

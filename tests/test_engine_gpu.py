@@ -198,3 +198,30 @@ def test_host_loop_mode_matches(schedule, monkeypatch):
     eng.setGraph(d.nV, vd, d.nE, None, d.src, d.dst)
     ranks, st = eng.pagerank_precision(0.85, 1e-6)
     assert np.abs(ranks.astype(np.float64) - r64).sum() <= 1e-6
+
+
+def test_profiling_mode_counts_kernels_and_keeps_results():
+    el = EdgeList.rmat(13, 16, seed=8).with_uniform_weights(1, 64, 3)
+    s = int(el.sample_sources(1, 8)[0])
+    ref, rit = oracle.sssp(el.nV, el.src, el.dst, el.weights, s)
+    eng = GASEngineGPU("sssp")
+    vd = initial_vertex_data("sssp", el.nV, s)
+    eng.setGraph(el.nV, vd, el.nE, el.weights, el.src, el.dst)
+    eng.set_profiling(True)
+    eng.setActive(0, el.nV)
+    st = eng.run_schedule("auto", max_iterations=el.nV + 2)
+    eng.getResults()
+    p = eng.profile()
+    np.testing.assert_array_equal(vd, ref)
+    assert st.iterations == rit
+    assert p.push_launches + p.pull_launches == st.iterations
+    assert p.push_launches == st.push_iters and p.pull_launches == st.pull_iters
+    assert p.push_ms + p.pull_ms > 0 and p.push_bytes + p.pull_bytes > 0
+    d = EdgeList.rmat(11, 16, seed=4, symmetrize=False)
+    e2 = GASEngineGPU("pagerank")
+    vd2 = initial_vertex_data("pagerank", d.nV, 0, d.out_degree())
+    e2.setGraph(d.nV, vd2, d.nE, None, d.src, d.dst)
+    e2.set_profiling(True)
+    ranks, pst = e2.pagerank_precision(0.85, 1e-6)
+    pp = e2.profile()
+    assert pp.pagerank_launches == pst.iterations and pp.pagerank_ms > 0
