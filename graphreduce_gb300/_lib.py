@@ -39,7 +39,11 @@ STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA err
 
 GAS_PROG_USER, GAS_PROG_BFS, GAS_PROG_SSSP, GAS_PROG_CC, GAS_PROG_PAGERANK = range(5)
 (GAS_SCHED_AUTO, GAS_SCHED_GENERIC, GAS_SCHED_PUSH, GAS_SCHED_PULL,
- GAS_SCHED_ORDERED) = range(5)
+ GAS_SCHED_ORDERED, GAS_SCHED_LEARNED) = range(6)
+GAS_SCHED_FEATURES = 16
+GAS_WARM_FEATURES = 4
+GAS_TRACE_CAP = 4096
+P_f32 = C.POINTER(C.c_float)
 
 
 class RunStats(C.Structure):
@@ -53,6 +57,12 @@ class KernelProfile(C.Structure):
                 ("push_bytes", c_i64), ("pull_bytes", c_i64), ("pagerank_bytes", c_i64),
                 ("push_launches", c_i32), ("pull_launches", c_i32),
                 ("pagerank_launches", c_i32), ("pad", c_i32)]
+
+
+class TraceRecord(C.Structure):
+    _fields_ = [("iteration", c_i32), ("mode", c_i32), ("n_queue", c_i32),
+                ("n_edges_out", c_i32), ("hist", c_i32 * 8), ("t_start_ns", c_i64),
+                ("t_end_ns", c_i64)]
 
 
 class Counters(C.Structure):
@@ -107,6 +117,22 @@ _SIGS = {
                                              c_dbl, c_vp, c_vp]),
     "gas_engine_set_profiling": ("status", [c_vp, c_i32]),
     "gas_engine_get_profile": ("status", [c_vp, C.POINTER(KernelProfile), c_i32]),
+    "gas_mlp_create": ("status", [c_i32, c_i32, c_u64, C.POINTER(c_vp)]),
+    "gas_mlp_destroy": (None, [c_vp]),
+    "gas_mlp_num_params": (c_i64, [c_vp]),
+    "gas_mlp_get_params": ("status", [c_vp, c_vp]),
+    "gas_mlp_set_params": ("status", [c_vp, c_vp]),
+    "gas_mlp_gradients": ("status", [c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
+    "gas_mlp_train_step": ("status", [c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, C.c_float, c_vp,
+                                      c_vp]),
+    "gas_mlp_forward": ("status", [c_vp, c_vp, c_i32, c_vp, c_vp]),
+    "gas_engine_set_trace": ("status", [c_vp, c_i32]),
+    "gas_engine_get_trace": ("status", [c_vp, c_vp, c_i32, P_i32]),
+    "gas_schedule_features": (None, [c_vp, c_i32, c_i64, c_i32, c_vp]),
+    "gas_engine_set_schedule_model": ("status", [c_vp, c_vp]),
+    "gas_engine_pagerank_warm_start": ("status", [c_vp, c_vp, c_vp, c_vp]),
+    "gas_engine_pagerank_precision_from": ("status", [c_vp, c_dbl, c_dbl, c_i32, c_vp, c_vp,
+                                                      C.POINTER(RunStats), c_vp]),
     "gas_engine_view_get": ("status", [c_vp, c_vp]),
     "gas_engine_note_applied": ("status", [c_vp, c_i32]),
     "gas_engine_read_counters": ("status", [c_vp, C.POINTER(Counters), c_vp]),

@@ -29,7 +29,7 @@ NVCC_FLAGS = [
     f"-I{INCLUDE}", f"-I{CSRC}",
 ]
 SOURCES = ["gas_engine.cu", "gas_runs.cu", "gas_sched.cu", "gas_noalloc.cu",
-           "gas_host_graph.cpp"]
+           "gas_learn.cu", "gas_host_graph.cpp"]
 
 
 def nvcc() -> str:

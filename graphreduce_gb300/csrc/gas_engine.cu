@@ -468,6 +468,7 @@ void free_graph(gas_engine *e) {
   dfree(e->ne_vid); dfree(e->ne_end); dfree(e->zero_vid);
   dfree(e->slab_dpart); dfree(e->slab_qpart); dfree(e->slab_a0);
   dfree(e->slab_first); dfree(e->slab_carry); dfree(e->slab_fix); dfree(e->slab_fix_n);
+  dfree(e->trace); dfree(e->hist);
   e->n_ne = e->n_zero = e->slab_cap = 0;
   for (int i = 0; i < kGraphSlots; ++i) {
     if (e->graphs[i]) cudaGraphExecDestroy(e->graphs[i]);
@@ -832,6 +833,8 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   GAS_TRY(dalloc((uint8_t **)&e->slab_carry, (size_t)e->slab_cap * 8));
   GAS_TRY(dalloc(&e->slab_fix, (size_t)e->slab_cap));
   GAS_TRY(dalloc(&e->slab_fix_n, 1));
+  GAS_TRY(dalloc(&e->trace, GAS_TRACE_CAP));
+  GAS_TRY(dalloc(&e->hist, 8));
 
   cudaStream_t st = S(stream);
   if (!ne_vid.empty()) {
@@ -855,6 +858,8 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
     CUDA_TRY(cudaMemcpyAsync(e->vd, vertex_data, V * e->vbytes, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemsetAsync(e->bits, 0, nW * 4, st));
   CUDA_TRY(cudaMemsetAsync(e->slab_fix_n, 0, sizeof(int32_t), st));
+  CUDA_TRY(cudaMemsetAsync(e->hist, 0, 8 * sizeof(int32_t), st));
+  CUDA_TRY(cudaMemsetAsync(e->trace, 0, GAS_TRACE_CAP * sizeof(gas_trace_record), st));
   CUDA_TRY(cudaMemsetAsync(e->cnt, 0, sizeof(gas_counters), st));
   CUDA_TRY(cudaMemsetAsync(e->ret, 0, V ? V : 1, st));
   // the host vectors are released at return: wait for the copies

@@ -83,6 +83,11 @@ struct gas_engine {
   // warp-slab chunk state: partitions of the dense CSC and of the push
   // queue, per-chunk carries (8-byte values) and fixup rows
   int32_t *slab_dpart = nullptr, *slab_qpart = nullptr, *slab_a0 = nullptr;
+  // traces and the learned schedule
+  gas_trace_record *trace = nullptr;  // [GAS_TRACE_CAP] device
+  int32_t *hist = nullptr;            // [8] degree histogram of the queue
+  bool trace_on = false;
+  const void *sched_model = nullptr;  // BF16 weights of the schedule head
   int32_t *slab_fix = nullptr;      // chunks needing a fixup, [slab_cap]
   int32_t *slab_fix_n = nullptr;    // their count (reset after each fixup)
   void *slab_first = nullptr, *slab_carry = nullptr;

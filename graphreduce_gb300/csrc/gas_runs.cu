@@ -361,13 +361,15 @@ __global__ void __launch_bounds__(kNT)
   }
 }
 
+// Initial ranks: 1/N, or the caller's vector already copied into rank.
 __global__ void k_pr_init(float *rank, float *contrib, const int32_t *csr_off,
-                          int n, float r0) {
+                          int n, float r0, int have_init) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += gridDim.x * blockDim.x) {
     const int deg = csr_off[v + 1] - csr_off[v];
-    rank[v] = r0;
-    contrib[v] = deg ? __fdiv_rn(r0, (float)deg) : 0.0f;
+    const float r = have_init ? rank[v] : r0;
+    rank[v] = r;
+    contrib[v] = deg ? __fdiv_rn(r, (float)deg) : 0.0f;
   }
 }
 
@@ -411,6 +413,13 @@ gas_status_t pr_body(gas_engine *e, cudaStream_t cs,
 extern "C" gas_status_t gas_engine_pagerank_precision(
     gas_engine *e, double damping, double tol, int32_t max_iterations,
     float *ranks, gas_run_stats *stats, void *stream) {
+  return gas_engine_pagerank_precision_from(e, damping, tol, max_iterations, nullptr,
+                                            ranks, stats, stream);
+}
+
+extern "C" gas_status_t gas_engine_pagerank_precision_from(
+    gas_engine *e, double damping, double tol, int32_t max_iterations,
+    const float *init, float *ranks, gas_run_stats *stats, void *stream) {
   if (!e || !e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
   if (!(damping > 0.0 && damping < 1.0) || !(tol > 0.0))
     return gas::fail(GAS_ERR_INVALID, "damping must be in (0,1), tol > 0");
@@ -463,8 +472,11 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
   CUDA_TRY(cudaMemcpyAsync(c.residual + 1, &tol, sizeof(double),
                            cudaMemcpyHostToDevice, S(stream)));
   gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, S(stream)>>>(c.src, e->slab_dpart);
+  if (init)
+    CUDA_TRY(cudaMemcpyAsync(e->pr_rank[0], init, (size_t)nV * 4, cudaMemcpyDefault,
+                             S(stream)));
   k_pr_init<<<gas::engine_grid(nV, kNT, 8 * e->num_sms), kNT, 0, S(stream)>>>(
-      e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV));
+      e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV), init ? 1 : 0);
   k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
   cudaError_t ce = cudaGetLastError();
   if (host_loop) {

@@ -28,6 +28,7 @@
 // (each kernel returns at once when the other mode is selected), the
 // frontier compaction and the condition kernel, which also picks the next
 // iteration's mode.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -38,6 +39,8 @@
 #include "gas_engine_impl.h"
 #include "gas_internal.h"
 #include "gas_sched.h"
+#include "gas_features.h"
+#include "gas_learn.h"
 
 using gasdev::kNT;
 using gasdev::SegSource;
@@ -246,8 +249,10 @@ __global__ void __launch_bounds__(kNT)
 __global__ void __launch_bounds__(kNT)
     k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int32_t *part,
               const int32_t *vd, int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
-              int32_t *q_delta, int32_t *snap) {
+              int32_t *q_delta, int32_t *snap, int32_t *hist) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
+  __shared__ int s_hist[8];
+  if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
   const QLane ql = q_lane(cbits, nW, w0);
@@ -285,6 +290,7 @@ __global__ void __launch_bounds__(kNT)
         q_end[pos] = end;
         q_delta[pos] = off - (end - deg);
         snap[v] = val;
+        if (hist) atomicAdd(&s_hist[gasfeat::degree_bucket(deg)], 1);
       }
       bq += __popc(qb);
       bd += __shfl_sync(0xffffffffu, incl, 31);
@@ -318,9 +324,14 @@ __global__ void __launch_bounds__(kNT)
         q_end[pq] = pd;
         q_delta[pq] = off - (pd - deg);
         snap[v] = val;
+        if (hist) atomicAdd(&s_hist[gasfeat::degree_bucket(deg)], 1);
         ++pq;
       }
     }
+  }
+  if (hist) {
+    __syncthreads();
+    if (threadIdx.x < 8 && s_hist[threadIdx.x]) atomicAdd(hist + threadIdx.x, s_hist[threadIdx.x]);
   }
 }
 
@@ -460,47 +471,98 @@ __global__ void __launch_bounds__(kNT)
 // ---------------------------------------------------------------------------
 // loop control
 // ---------------------------------------------------------------------------
-// Mode of the next iteration: AUTO pulls when the frontier's out-edges are
-// more than 1/pull_div of all edges.
-__device__ __forceinline__ void pick_mode(gas_counters *cnt, int nE) {
-  const int forced = cnt->pad[0];  // 0 auto, 1 push, 2 pull
+// Loop-control state captured into the graph.
+struct LoopCtl {
+  cudaGraphConditionalHandle h;
+  int in_graph;
+  int nV;
+  int nE;
+  int weighted;
+  const __nv_bfloat16 *model;  // schedule head (LEARNED), or null
+  gas_trace_record *trace;     // per-iteration records, or null
+  int32_t *hist;               // degree histogram of the queue, or null
+  int32_t *fix_n;
+};
+
+// Mode of the next iteration (one warp): forced push / pull, the learned
+// head, or the fixed heuristic -- pull when the frontier's out-edges are
+// more than 1/pull_div of all edges.  With tracing, records the iteration.
+__device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now) {
+  const int lane = threadIdx.x & 31;
+  const int forced = cnt->pad[0];  // 0 auto, 1 push, 2 pull, 3 learned
+  const int it = cnt->iteration;   // the iteration being scheduled
   int mode;
-  if (forced == 1)
+  if (forced == 1) {
     mode = kModePush;
-  else if (forced == 2)
+  } else if (forced == 2) {
     mode = kModePull;
-  else
-    mode = ((long long)cnt->n_scatter_edges * cnt->pull_div > (long long)nE)
+  } else if (forced == 3 && c.model) {
+    float f[GAS_SCHED_FEATURES], lg[2];
+    gasfeat::schedule_features(cnt->n_changed, cnt->n_scatter_edges, c.hist, it, c.nV,
+                               c.nE, c.weighted, f);
+    gaslearn::mlp_warp_logits(c.model, GAS_SCHED_FEATURES, f, lg);
+    mode = lg[1] > lg[0] ? kModePull : kModePush;
+  } else {
+    mode = ((long long)cnt->n_scatter_edges * cnt->pull_div > (long long)c.nE)
                ? kModePull : kModePush;
-  cnt->mode = mode;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    cnt->mode = mode;
+    if (c.trace && it < GAS_TRACE_CAP && cnt->cond) {
+      gas_trace_record &r = c.trace[it];
+      r.iteration = it;
+      r.mode = mode;
+      r.n_queue = cnt->n_changed;
+      r.n_edges_out = cnt->n_scatter_edges;
+      for (int b = 0; b < 8; ++b) r.hist[b] = c.hist ? c.hist[b] : 0;
+      r.t_start_ns = now;
+      r.t_end_ns = 0;
+    }
+  }
+  __syncwarp();
+  if (lane < 8 && c.hist) c.hist[lane] = 0;
+}
+
+__device__ __forceinline__ long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return (long long)t;
 }
 
 // seeded: the prologue only built the iteration-0 sender set, iteration 0
 // itself runs in the loop (and always exists: A_0 = V is not empty).
-__global__ void k_fast_precond(gas_counters *cnt, cudaGraphConditionalHandle h,
-                               int nE, int in_graph, int seeded) {
-  const int done = seeded ? 0 : 1;  // iterations run by the prologue
-  cnt->iteration = done;
-  const bool more = seeded ? true : cnt->n_scatter_edges > 0;
-  if (more && done >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
-  cnt->cond = (more && done < cnt->max_iter) ? 1 : 0;
-  pick_mode(cnt, nE);
-  if (in_graph) cudaGraphSetConditional(h, cnt->cond);
+__global__ void k_fast_precond(gas_counters *cnt, LoopCtl c, int seeded) {
+  const long long now = global_ns();
+  if (threadIdx.x == 0) {
+    const int done = seeded ? 0 : 1;  // iterations run by the prologue
+    cnt->iteration = done;
+    const bool more = seeded ? true : cnt->n_scatter_edges > 0;
+    if (more && done >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
+    cnt->cond = (more && done < cnt->max_iter) ? 1 : 0;
+  }
+  __syncwarp();
+  schedule_next(cnt, c, now);
+  if (threadIdx.x == 0 && c.in_graph) cudaGraphSetConditional(c.h, cnt->cond);
 }
 
-__global__ void k_fast_cond(gas_counters *cnt, cudaGraphConditionalHandle h,
-                            int nE, int in_graph, int32_t *fix_n) {
-  *fix_n = 0;  // the pull fixup of this iteration has run
-  if (cnt->mode == kModePush)
-    ++cnt->n_push;
-  else
-    ++cnt->n_pull;
-  const int it = ++cnt->iteration;
-  const bool more = cnt->n_scatter_edges > 0;
-  if (more && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
-  cnt->cond = (more && it < cnt->max_iter) ? 1 : 0;
-  pick_mode(cnt, nE);
-  if (in_graph) cudaGraphSetConditional(h, cnt->cond);
+__global__ void k_fast_cond(gas_counters *cnt, LoopCtl c) {
+  const long long now = global_ns();
+  if (threadIdx.x == 0) {
+    *c.fix_n = 0;  // the pull fixup of this iteration has run
+    if (cnt->mode == kModePush)
+      ++cnt->n_push;
+    else
+      ++cnt->n_pull;
+    if (c.trace && cnt->iteration < GAS_TRACE_CAP) c.trace[cnt->iteration].t_end_ns = now;
+    const int it = ++cnt->iteration;
+    const bool more = cnt->n_scatter_edges > 0;
+    if (more && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
+    cnt->cond = (more && it < cnt->max_iter) ? 1 : 0;
+  }
+  __syncwarp();
+  schedule_next(cnt, c, now);
+  if (threadIdx.x == 0 && c.in_graph) cudaGraphSetConditional(c.h, cnt->cond);
 }
 
 __global__ void k_fast_reset(gas_counters *cnt, int max_iter, int forced,
@@ -528,6 +590,20 @@ struct FastCtx {
   bool seeded;  // iteration 0 from the full range via the finite-value seed
 };
 
+LoopCtl loop_ctl(const gas_engine *e, cudaGraphConditionalHandle h) {
+  LoopCtl c;
+  c.h = h;
+  c.in_graph = e->in_graph ? 1 : 0;
+  c.nV = e->nV;
+  c.nE = e->nE;
+  c.weighted = e->prog == GAS_PROG_SSSP ? 1 : 0;
+  c.model = static_cast<const __nv_bfloat16 *>(e->sched_model);
+  c.trace = e->trace_on ? e->trace : nullptr;
+  c.hist = (e->trace_on || e->sched_model) ? e->hist : nullptr;
+  c.fix_n = e->slab_fix_n;
+  return c;
+}
+
 int32_t snap_zero(const gas_engine *e) {
   return e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
 }
@@ -538,7 +614,8 @@ gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c) {
   k_q_spine<<<1, kNT, 0, cs>>>(e->qpart, c.n_qblocks, e->cnt);
   k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart,
                                          (const int32_t *)e->vd, e->q_ids, e->q_vals,
-                                         e->q_end, e->q_delta, e->snap);
+                                         e->q_end, e->q_delta, e->snap,
+                                         (e->trace_on || e->sched_model) ? e->hist : nullptr);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -629,7 +706,7 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   CUDA_TRY(cudaGetLastError());
   gas::prof_end(e, cs);
   GAS_TRY(compaction(e, cs, c));
-  k_fast_cond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE, e->in_graph ? 1 : 0, e->slab_fix_n);
+  k_fast_cond<<<1, 32, 0, cs>>>(e->cnt, loop_ctl(e, h));
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -677,8 +754,7 @@ static gas_status_t build_fast_graph(gas_engine *e, FastCtx *ctx,
   e->in_graph = true;
   st = prologue(e, cs, ctx);
   if (st == GAS_OK) {
-    k_fast_precond<<<1, 1, 0, cs>>>(e->cnt, h, e->nE, e->in_graph ? 1 : 0,
-                                    ctx->seeded ? 1 : 0);
+    k_fast_precond<<<1, 32, 0, cs>>>(e->cnt, loop_ctl(e, h), ctx->seeded ? 1 : 0);
     ce = cudaGetLastError();
     if (ce != cudaSuccess) st = fail(GAS_ERR_CUDA, "precond: %s", cudaGetErrorString(ce));
   }
@@ -741,6 +817,8 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     return gas_engine_run_schedule(e, GAS_SCHED_GENERIC, max_iterations, stats, stream);
   // BFS has the top-down push only: every schedule pushes
   if (e->prog == GAS_PROG_BFS) schedule = GAS_SCHED_PUSH;
+  if (schedule == GAS_SCHED_LEARNED && !e->sched_model)
+    return fail(GAS_ERR_STATE, "LEARNED schedule without a schedule model");
   GAS_TRY(ensure_fast_buffers(e));
   FastCtx ctx;
   ctx.nW = (e->nV + 31) / 32;
@@ -756,7 +834,8 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
   const int slot = kGraphFast0 + (ctx.seeded ? 1 : 0);
   const bool host_loop = host_loop_for(e);
   if (!host_loop && !e->graphs[slot]) GAS_TRY(build_fast_graph(e, &ctx, &e->graphs[slot]));
-  const int forced = schedule == GAS_SCHED_PUSH ? 1 : schedule == GAS_SCHED_PULL ? 2 : 0;
+  const int forced = schedule == GAS_SCHED_PUSH ? 1 : schedule == GAS_SCHED_PULL ? 2
+                     : schedule == GAS_SCHED_LEARNED ? 3 : 0;
   k_fast_reset<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations, forced, e->pull_div);
   cudaError_t ce = cudaGetLastError();
   if (host_loop) {
@@ -765,7 +844,7 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
       e->in_graph = false;
       gas_status_t pst = prologue(e, S(stream), &ctx);
       if (pst == GAS_OK) {
-        k_fast_precond<<<1, 1, 0, S(stream)>>>(e->cnt, 0, e->nE, 0, ctx.seeded ? 1 : 0);
+        k_fast_precond<<<1, 32, 0, S(stream)>>>(e->cnt, loop_ctl(e, 0), ctx.seeded ? 1 : 0);
         ce = cudaGetLastError();
       }
       e->capturing = false;
@@ -802,3 +881,54 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
 }
 
 }  // namespace gas
+
+// ---------------------------------------------------------------------------
+// traces and the schedule model
+// ---------------------------------------------------------------------------
+namespace {
+void drop_fast_graphs(gas_engine *e) {
+  for (int i = kGraphFast0; i < kGraphSlots; ++i) {
+    if (e->graphs[i]) cudaGraphExecDestroy(e->graphs[i]);
+    e->graphs[i] = nullptr;
+  }
+}
+}  // namespace
+
+extern "C" gas_status_t gas_engine_set_trace(gas_engine *e, int32_t on) {
+  if (!e) return gas::fail(GAS_ERR_INVALID, "null engine");
+  if ((on != 0) != e->trace_on) drop_fast_graphs(e);  // captured with the old setting
+  e->trace_on = on != 0;
+  return GAS_OK;
+}
+
+extern "C" gas_status_t gas_engine_get_trace(gas_engine *e, gas_trace_record *out,
+                                             int32_t cap, int32_t *n) {
+  if (!e || !out || !n || cap < 0) return gas::fail(GAS_ERR_INVALID, "bad arguments");
+  if (!e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
+  gas_counters c;
+  GAS_TRY(gas_engine_read_counters(e, &c, nullptr));
+  int32_t k = c.iteration < GAS_TRACE_CAP ? c.iteration : GAS_TRACE_CAP;
+  if (k > cap) k = cap;
+  if (k > 0)
+    CUDA_TRY(cudaMemcpy(out, e->trace, sizeof(gas_trace_record) * (size_t)k,
+                        cudaMemcpyDeviceToHost));
+  *n = k;
+  return GAS_OK;
+}
+
+extern "C" gas_status_t gas_engine_set_schedule_model(gas_engine *e, const gas_mlp *m) {
+  if (!e) return gas::fail(GAS_ERR_INVALID, "null engine");
+  if (m && (gaslearn::mlp_inputs(m) != GAS_SCHED_FEATURES || gaslearn::mlp_outputs(m) != 2))
+    return gas::fail(GAS_ERR_INVALID, "schedule model must be %d -> 2", GAS_SCHED_FEATURES);
+  const void *w = m ? gaslearn::mlp_bf16(m) : nullptr;
+  if (w != e->sched_model) drop_fast_graphs(e);
+  e->sched_model = w;
+  return GAS_OK;
+}
+
+extern "C" void gas_schedule_features(const gas_trace_record *rec, int32_t nV, int64_t nE,
+                                      int32_t weighted, float *out) {
+  if (!rec || !out) return;
+  gasfeat::schedule_features(rec->n_queue, rec->n_edges_out, rec->hist, rec->iteration, nV,
+                             nE, weighted, out);
+}

@@ -29,7 +29,7 @@ VERTEX_DTYPE = {BFS: np.dtype(np.int32), SSSP: np.dtype(np.int32),
 
 SCHEDULES = {"auto": L.GAS_SCHED_AUTO, "generic": L.GAS_SCHED_GENERIC,
              "push": L.GAS_SCHED_PUSH, "pull": L.GAS_SCHED_PULL,
-             "ordered": L.GAS_SCHED_ORDERED}
+             "ordered": L.GAS_SCHED_ORDERED, "learned": L.GAS_SCHED_LEARNED}
 
 BFS_UNREACHED = -1                       # bfs.cu:107
 SSSP_GATHER_ZERO = 2**31 - 1 - 100000    # sssp.cu:32-33
@@ -171,6 +171,38 @@ class GASEngineGPU:
         p = L.KernelProfile()
         L.call("gas_engine_get_profile", self._h, C.byref(p), int(reset))
         return p
+
+    def set_trace(self, on: bool) -> None:
+        """Per-iteration device records of later fast runs."""
+        L.call("gas_engine_set_trace", self._h, int(on))
+
+    def trace(self) -> list:
+        """The last run's records (list of TraceRecord)."""
+        buf = (L.TraceRecord * L.GAS_TRACE_CAP)()
+        n = C.c_int32()
+        L.call("gas_engine_get_trace", self._h, buf, L.GAS_TRACE_CAP, C.byref(n))
+        return [buf[i] for i in range(n.value)]
+
+    def set_schedule_model(self, mlp) -> None:
+        """Schedule head for run_schedule("learned") (None removes it)."""
+        L.call("gas_engine_set_schedule_model", self._h, None if mlp is None else mlp.handle)
+        self._sched_model = mlp
+
+    def pagerank_warm_start(self, mlp, out: np.ndarray | None = None) -> np.ndarray:
+        init = out if out is not None else np.zeros(self.nVertices, np.float32)
+        L.call("gas_engine_pagerank_warm_start", self._h, mlp.handle, init.ctypes.data, None)
+        return init
+
+    def pagerank_precision_from(self, init: np.ndarray | None, damping: float = 0.85,
+                                tol: float = 1e-6, max_iterations: int = 1000,
+                                stream=None):
+        ranks = np.zeros(self.nVertices, np.float32)
+        st = RunStats()
+        ip = None if init is None else np.ascontiguousarray(init, np.float32)
+        L.call("gas_engine_pagerank_precision_from", self._h, damping, tol, max_iterations,
+               None if ip is None else ip.ctypes.data, ranks.ctypes.data, C.byref(st),
+               _stream_ptr(stream))
+        return ranks, st
 
     def counters(self) -> L.Counters:
         c = L.Counters()

@@ -211,8 +211,10 @@ typedef enum {
   GAS_SCHED_GENERIC = 1,   /* the step-API kernels (pull over active set)  */
   GAS_SCHED_PUSH = 2,      /* push every iteration (SSSP, CC, BFS)         */
   GAS_SCHED_PULL = 3,      /* dense pull every iteration (SSSP, CC, BFS)   */
-  GAS_SCHED_ORDERED = 4    /* generic, but each vertex folds its in-edges  */
+  GAS_SCHED_ORDERED = 4,   /* generic, but each vertex folds its in-edges  */
                            /* sequentially in CSC order (parity mode)      */
+  GAS_SCHED_LEARNED = 5    /* push or pull per iteration from the engine's */
+                           /* schedule model (gas_engine_set_schedule_model) */
 } gas_schedule_t;
 
 typedef struct {
@@ -285,6 +287,94 @@ typedef struct {
 gas_status_t gas_engine_set_profiling(gas_engine *e, int32_t on);
 gas_status_t gas_engine_get_profile(gas_engine *e, gas_kernel_profile *out,
                                     int32_t reset);
+
+/* ======================================================================= */
+/* Learned parts: MLP, engine traces, schedule head, PageRank warm start.  */
+/* No reference counterpart.                                               */
+/* ======================================================================= */
+
+#define GAS_MLP_HIDDEN 64    /* two hidden layers of this width, ReLU      */
+#define GAS_MLP_MAX_IN 32
+#define GAS_MLP_MAX_OUT 2
+
+/* An MLP n_in -> 64 -> 64 -> n_out on the device: FP32 master weights,
+ * BF16 copies for every forward pass, FP32 accumulation, Adam state.
+ * Flat parameter layout: W1[n_in][64] b1[64] W2[64][64] b2[64]
+ * W3[64][n_out] b3[n_out]. */
+typedef struct gas_mlp gas_mlp;
+gas_status_t gas_mlp_create(int32_t n_in, int32_t n_out, uint64_t seed,
+                            gas_mlp **out);
+void gas_mlp_destroy(gas_mlp *m);
+int64_t gas_mlp_num_params(const gas_mlp *m);
+gas_status_t gas_mlp_get_params(const gas_mlp *m, float *host);
+gas_status_t gas_mlp_set_params(gas_mlp *m, const float *host);
+/* Loss and its gradient for a batch (device pointers): x[batch][n_in];
+ * y[batch] class labels (softmax cross-entropy) or t[batch] targets of
+ * output 0 (squared error); w[batch] optional sample weights.  The loss is
+ * the weighted mean over the batch; grad_host receives all parameters'
+ * gradients (may be NULL). */
+gas_status_t gas_mlp_gradients(gas_mlp *m, const float *x, const int32_t *y,
+                               const float *t, const float *w, int32_t batch,
+                               float *grad_host, float *loss_host,
+                               void *stream);
+/* One Adam step (lr; betas 0.9, 0.999) on the same loss. */
+gas_status_t gas_mlp_train_step(gas_mlp *m, const float *x, const int32_t *y,
+                                const float *t, const float *w, int32_t batch,
+                                float lr, float *loss_host, void *stream);
+/* out[n][n_out] = model(x[n][n_in]) with the BF16 weights (device). */
+gas_status_t gas_mlp_forward(const gas_mlp *m, const float *x, int32_t n,
+                             float *out, void *stream);
+
+/* One iteration of a fast run, as recorded on the device. */
+typedef struct {
+  int32_t iteration;     /* k                                            */
+  int32_t mode;          /* 0 push, 1 dense pull, used for iteration k  */
+  int32_t n_queue;       /* |C_{k-1}| restricted to vertices with out-edges */
+  int32_t n_edges_out;   /* their out-edges                              */
+  int32_t hist[8];       /* their out-degrees: bucket min(7, floor(log2 d)/2) */
+  int64_t t_start_ns;    /* %globaltimer when iteration k was scheduled  */
+  int64_t t_end_ns;      /* ... when iteration k had finished            */
+} gas_trace_record;
+
+#define GAS_SCHED_FEATURES 16
+#define GAS_TRACE_CAP 4096
+
+/* Turns per-iteration recording of later fast runs on or off, and copies
+ * the last run's records out (n = number written, at most cap). */
+gas_status_t gas_engine_set_trace(gas_engine *e, int32_t on);
+gas_status_t gas_engine_get_trace(gas_engine *e, gas_trace_record *out,
+                                  int32_t cap, int32_t *n);
+
+/* The schedule head's input for iteration rec->iteration: log-scaled
+ * frontier size and out-edge count, graph size, frontier shares, degree
+ * histogram shares, iteration index, weighted flag (the same function the
+ * device loop evaluates). */
+void gas_schedule_features(const gas_trace_record *rec, int32_t nV, int64_t nE,
+                           int32_t weighted, float *out);
+
+/* GAS_SCHED_LEARNED uses this two-output model (n_in = GAS_SCHED_FEATURES;
+ * logit 1 > logit 0 selects the dense pull); NULL removes it.  The model is
+ * read when runs launch; it must outlive them. */
+gas_status_t gas_engine_set_schedule_model(gas_engine *e, const gas_mlp *m);
+
+/* PageRank warm start: per-vertex features of in- and out-degree (log2 of
+ * 1 + degree, over 32) plus graph-level log sizes go through a one-output
+ * model (n_in = GAS_WARM_FEATURES) predicting log(N * rank); init receives
+ * exp(prediction) / N for every vertex (device or host pointer, nV
+ * floats).  The model is evaluated on a 64 x 64 grid of log-degrees and
+ * interpolated bilinearly per vertex. */
+#define GAS_WARM_FEATURES 4
+gas_status_t gas_engine_pagerank_warm_start(gas_engine *e, const gas_mlp *m,
+                                            float *init, void *stream);
+
+/* gas_engine_pagerank_precision from a given initial vector (nV floats,
+ * device or host; NULL = the uniform 1/N). */
+gas_status_t gas_engine_pagerank_precision_from(gas_engine *e, double damping,
+                                                double tol,
+                                                int32_t max_iterations,
+                                                const float *init, float *ranks,
+                                                gas_run_stats *stats,
+                                                void *stream);
 
 /* ======================================================================= */
 /* Views used by include/gpugas.h to launch its Program-typed kernels.     */

@@ -173,3 +173,19 @@ def test_gr_rejects_truncated_and_missing(tmp_path):
 def test_edge_list_create_validates_ids():
     with pytest.raises(GasError):
         EdgeList(2, np.array([0, 2], np.int32), np.array([1, 1], np.int32)).write_gr("/tmp/x")
+
+
+def test_schedule_features_host_function():
+    """gas_schedule_features (the function the device loop evaluates) against
+    a restatement in numpy."""
+    from graphreduce_gb300 import _lib as L
+    from graphreduce_gb300.learn import schedule_features
+    rec = L.TraceRecord()
+    rec.iteration, rec.mode, rec.n_queue, rec.n_edges_out = 7, 1, 1000, 50000
+    for b, v in enumerate([400, 300, 200, 50, 30, 10, 7, 3]):
+        rec.hist[b] = v
+    f = schedule_features(rec, 1 << 20, 32 << 20, True)
+    want = [np.log2(1001) / 32, np.log2(50001) / 32, np.log2(1 + (1 << 20)) / 32,
+            np.log2(1 + (32 << 20)) / 32, 50000 / (32 << 20), 1000 / (1 << 20),
+            0.4, 0.3, 0.2, 0.05, 0.03, 0.01, 0.007, 0.003, 7 / 64, 1.0]
+    np.testing.assert_allclose(f, want, rtol=1e-5, atol=1e-7)

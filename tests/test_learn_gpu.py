@@ -1,0 +1,175 @@
+"""The learned parts: MLP kernels (gradients against an FP64 numpy
+implementation), engine traces, the LEARNED schedule (outputs identical to
+the oracle by construction) and the PageRank warm start (converges to the
+same tolerance)."""
+import numpy as np
+import pytest
+
+import oracle
+from graphreduce_gb300 import GASEngineGPU, GasError, run_program
+from graphreduce_gb300 import _lib as L
+from graphreduce_gb300.engine import initial_vertex_data
+from graphreduce_gb300.graph import EdgeList
+
+pytestmark = pytest.mark.gpu
+H = 64
+
+
+def bf16(a):
+    b = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def unpack(p, n_in, n_out):
+    p = p.astype(np.float64)
+    o = 0
+    W1 = p[o:o + n_in * H].reshape(n_in, H); o += n_in * H
+    b1 = p[o:o + H]; o += H
+    W2 = p[o:o + H * H].reshape(H, H); o += H * H
+    b2 = p[o:o + H]; o += H
+    W3 = p[o:o + H * n_out].reshape(H, n_out); o += H * n_out
+    b3 = p[o:o + n_out]
+    return W1, b1, W2, b2, W3, b3
+
+
+def numpy_grads(p, x, n_out, y=None, t=None, w=None):
+    """FP64 forward/backward of the same network and loss."""
+    W1, b1, W2, b2, W3, b3 = unpack(p, x.shape[1], n_out)
+    x = x.astype(np.float64)
+    B = x.shape[0]
+    w = np.ones(B) if w is None else w.astype(np.float64)
+    a1 = x @ W1 + b1
+    h1 = np.maximum(a1, 0)
+    a2 = h1 @ W2 + b2
+    h2 = np.maximum(a2, 0)
+    o = h2 @ W3 + b3
+    if y is not None:
+        m = o.max(1, keepdims=True)
+        z = np.exp(o - m).sum(1, keepdims=True)
+        logp = o - m - np.log(z)
+        loss = float((w * -logp[np.arange(B), y]).sum() / B)
+        dout = np.exp(logp)
+        dout[np.arange(B), y] -= 1
+        dout *= (w / B)[:, None]
+    else:
+        d = o[:, 0] - t
+        loss = float((w * d * d).sum() / B)
+        dout = np.zeros_like(o)
+        dout[:, 0] = 2 * w * d / B
+    gW3 = h2.T @ dout
+    gb3 = dout.sum(0)
+    d2 = (dout @ W3.T) * (a2 > 0)
+    gW2 = h1.T @ d2
+    gb2 = d2.sum(0)
+    d1 = (d2 @ W2.T) * (a1 > 0)
+    gW1 = x.T @ d1
+    gb1 = d1.sum(0)
+    g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3])
+    return g, loss
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.mark.parametrize("kind", ["classify", "regress"])
+def test_mlp_gradients_match_fp64(torch, kind):
+    from graphreduce_gb300.learn import MLP
+    rng = np.random.default_rng(3)
+    n_in = 16 if kind == "classify" else 4
+    n_out = 2 if kind == "classify" else 1
+    m = MLP(n_in, n_out, seed=11)
+    p = bf16(rng.normal(0, 0.3, m.n_params).astype(np.float32))
+    m.set_params(p)
+    x = rng.normal(0, 1, (32, n_in)).astype(np.float32)
+    w = rng.uniform(0.5, 2.0, 32).astype(np.float32)
+    xd, wd = torch.from_numpy(x).cuda(), torch.from_numpy(w).cuda()
+    if kind == "classify":
+        y = rng.integers(0, 2, 32).astype(np.int32)
+        g, loss = m.gradients(xd, y=torch.from_numpy(y).cuda(), w=wd)
+        gr, lr = numpy_grads(p, x, n_out, y=y, w=w)
+    else:
+        t = rng.normal(0, 1, 32).astype(np.float32)
+        g, loss = m.gradients(xd, t=torch.from_numpy(t).cuda(), w=wd)
+        gr, lr = numpy_grads(p, x, n_out, t=t, w=w)
+    assert abs(loss - lr) <= 1e-4 * max(1.0, abs(lr))
+    scale = np.abs(gr).max()
+    np.testing.assert_allclose(g, gr, atol=1e-4 * scale, rtol=1e-3)
+
+
+def test_mlp_training_reduces_loss(torch):
+    from graphreduce_gb300.learn import MLP
+    rng = np.random.default_rng(0)
+    x = rng.normal(0, 1, (1024, 16)).astype(np.float32)
+    y = (x[:, 0] + 0.5 * x[:, 3] > 0).astype(np.int32)
+    m = MLP(16, 2, seed=1)
+    xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    first = m.train_step(xd, yd, lr=1e-3)
+    for _ in range(300):
+        last = m.train_step(xd, yd, lr=3e-3)
+    assert last < 0.3 * first
+    out = m.forward(xd).cpu().numpy()
+    assert ((out[:, 1] > out[:, 0]) == y).mean() > 0.95
+
+
+def test_traces_see_the_same_frontiers_under_push_and_pull():
+    from graphreduce_gb300.learn import schedule_samples
+    el = EdgeList.rmat(13, 16, seed=21).with_uniform_weights(1, 64, 3)
+    src = int(el.sample_sources(1, 2)[0])
+    for program in ("sssp", "cc"):
+        X, y, w = schedule_samples(el, program, src)   # asserts identical frontiers
+        assert X.shape[1] == L.GAS_SCHED_FEATURES and len(y) == len(w) > 2
+        assert np.all(w >= 0)
+
+
+@pytest.mark.parametrize("program", ["sssp", "cc", "bfs"])
+def test_learned_schedule_is_exact(program):
+    from graphreduce_gb300.learn import MLP
+    el = EdgeList.rmat(14, 16, seed=31).with_uniform_weights(1, 64, 3).with_grid_islands(8, 8)
+    s = int(el.sample_sources(1, 31)[0])
+    ref = {"sssp": lambda: oracle.sssp(el.nV, el.src, el.dst, el.weights, s),
+           "cc": lambda: oracle.cc(el.nV, el.src, el.dst),
+           "bfs": lambda: oracle.bfs(el.nV, el.src, el.dst, s)}[program]()
+    for seed in (1, 2):   # two arbitrary (untrained) heads: any decision is exact
+        m = MLP(L.GAS_SCHED_FEATURES, 2, seed=seed)
+        eng = GASEngineGPU(program)
+        vd = initial_vertex_data(program, el.nV, s)
+        eng.setGraph(el.nV, vd, el.nE, el.weights if program == "sssp" else None,
+                     el.src, el.dst)
+        eng.set_schedule_model(m)
+        eng.setActive(*((s, s + 1) if program == "bfs" else (0, el.nV)))
+        st = eng.run_schedule("learned", max_iterations=el.nV + 2)
+        eng.getResults()
+        np.testing.assert_array_equal(vd, ref[0])
+        assert st.iterations == ref[1]
+
+
+def test_learned_without_model_is_refused():
+    el = EdgeList.rmat(8, 8, seed=1)
+    eng = GASEngineGPU("cc")
+    vd = initial_vertex_data("cc", el.nV)
+    eng.setGraph(el.nV, vd, el.nE, None, el.src, el.dst)
+    eng.setActive(0, el.nV)
+    with pytest.raises(GasError) as ei:
+        eng.run_schedule("learned")
+    assert ei.value.status == 6
+
+
+def test_warm_start_converges_to_the_same_tolerance():
+    from graphreduce_gb300.learn import MLP
+    d = EdgeList.rmat(13, 16, seed=4, symmetrize=False)
+    r64, _, _ = oracle.pagerank_fp64(d.nV, d.src, d.dst, 0.85, 1e-6)
+    eng = GASEngineGPU("pagerank")
+    vd = initial_vertex_data("pagerank", d.nV, 0, d.out_degree())
+    eng.setGraph(d.nV, vd, d.nE, None, d.src, d.dst)
+    m = MLP(L.GAS_WARM_FEATURES, 1, seed=5)
+    init = eng.pagerank_warm_start(m)
+    assert np.all(np.isfinite(init)) and np.all(init > 0)
+    ranks, st = eng.pagerank_precision_from(init)
+    assert st.residual <= 1e-6
+    # both stop within 1e-6 of a step from the same fixed point
+    assert np.abs(ranks.astype(np.float64) - r64).sum() <= 2e-5
+    uni, su = eng.pagerank_precision_from(None)
+    assert np.abs(uni.astype(np.float64) - r64).sum() <= 1e-6
