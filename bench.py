@@ -163,6 +163,11 @@ def run_ours(args, rank, world):
     out_sssp = ssp.out_degree()
     out_cc = ccg.out_degree()
 
+    model = None
+    if args.schedule == "learned":
+        from graphreduce_gb300.learn import DATA, MLP
+        model = MLP.load(DATA / "schedule_head.npz")  # trained schedule head (required)
+
     t = time.time()
     e_s = gg.GASEngineGPU("sssp")
     vd_s = initial_vertex_data("sssp", ssp.nV, int(sources[0]))
@@ -171,6 +176,9 @@ def run_ours(args, rank, world):
     vd_c = initial_vertex_data("cc", ccg.nV)
     e_c.setGraph(ccg.nV, vd_c, ccg.nE, None, ccg.src, ccg.dst, sp)
     log(f"setGraph (host CSR/CSC build + upload) {time.time() - t:.1f}s")
+    if model is not None:
+        e_s.set_schedule_model(model)
+        e_c.set_schedule_model(model)
 
     # initial vertex states resident in HBM (value) and in pinned host memory (e2e)
     init_s = [torch.from_numpy(initial_vertex_data("sssp", ssp.nV, int(s))) for s in sources]
@@ -186,20 +194,20 @@ def run_ours(args, rank, world):
     launches = [0]
     iters = {"sssp": [], "cc": 0}
 
-    def one_step(e2e):
+    def one_step(e2e, schedule=args.schedule):
         launches[0] = 0
         iters["sssp"] = []
         for k in range(len(sources)):
             e_s.upload_vertex_data_ptr(pin_s[k].data_ptr() if e2e else dev_s[k].data_ptr(), sp)
             e_s.setActive(0, ssp.nV, sp)
-            st = e_s.run_schedule(args.schedule, max_iterations=MAX_ITERS, stream=sp)
+            st = e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
             iters["sssp"].append(st.iterations)
             launches[0] += st.kernel_launches + 1
             if e2e:
                 e_s.download_vertex_data_ptr(res_s[k].data_ptr(), sp)
         e_c.upload_vertex_data_ptr(pin_c.data_ptr() if e2e else dev_c.data_ptr(), sp)
         e_c.setActive(0, ccg.nV, sp)
-        st = e_c.run_schedule(args.schedule, max_iterations=MAX_ITERS, stream=sp)
+        st = e_c.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
         iters["cc"] = st.iterations
         launches[0] += st.kernel_launches + 1
         if e2e:
@@ -220,9 +228,9 @@ def run_ours(args, rank, world):
     ev_units += edges_visited(out_cc, res_c.numpy(), -12345)  # every CC vertex is reached
     first_sssp = res_s[0].numpy().copy()
 
-    def timed(e2e, steps, warmup):
+    def timed(e2e, steps, warmup, schedule=args.schedule):
         for _ in range(warmup):
-            one_step(e2e)
+            one_step(e2e, schedule)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -232,7 +240,7 @@ def run_ours(args, rank, world):
         t0 = time.perf_counter()
         start.record(stream)
         for _ in range(steps):
-            one_step(e2e)
+            one_step(e2e, schedule)
         end.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -249,6 +257,13 @@ def run_ours(args, rank, world):
     clocks = clk.summary()
     ms_e2e, _ = timed(True, max(1, args.steps), 1)
     launches_per_step = launches[0]
+    plain = None
+    if args.schedule != "auto":
+        # the same step under the fixed heuristic (AUTO), device-resident
+        ms_plain, _ = timed(False, args.steps, args.warmup, "auto")
+        plain = {"schedule": "auto (fixed heuristic)", "ms_per_step": round(ms_plain, 3),
+                 "value": round(world * ev_units / (ms_plain * 1e-3) / 1e9, 4),
+                 "speedup_of_headline": round(ms_plain / ms_step, 4)}
 
     value = world * ev_units / (ms_step * 1e-3) / 1e9
     e2e = world * ev_units / (ms_e2e * 1e-3) / 1e9
@@ -278,6 +293,7 @@ def run_ours(args, rank, world):
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roof,
         "algos": split,
+        "plain": plain,
         "clocks": clocks,
     }
     return result, (ssp, sources, out_sssp, first_sssp)
@@ -362,6 +378,197 @@ def kernel_roofline(e_s, e_c, dev_s, dev_c, ssp, ccg, schedule, sp):
 
 
 # ---------------------------------------------------------------------------
+# batched workload: 64 graphs x (16 BFS sources + 16 PPR seeds)
+# ---------------------------------------------------------------------------
+BATCH_GRAPHS, BATCH_LANES, BATCH_SEED = 64, 16, 6
+BATCH_METRIC = "GTEPS (batched: 64 R-MAT graphs x (16 BFS + 16 PPR))"
+PPR_DAMPING, PPR_TOL = 0.85, 1e-6
+
+
+def make_batched_workload(n_graphs=BATCH_GRAPHS):
+    """Scale U[12,20], edge factor U[8,32] per graph (seed 6), symmetrised
+    R-MAT; 16 BFS sources and 16 PPR seeds per graph, uniform over the
+    graph's largest component (seeded per graph)."""
+    from graphreduce_gb300.graph import EdgeList
+    rng = np.random.default_rng(BATCH_SEED)
+    scales = rng.integers(12, 21, n_graphs)
+    efs = rng.integers(8, 33, n_graphs)
+    t = time.time()
+    graphs, srcs, seeds = [], [], []
+    for g in range(n_graphs):
+        el = EdgeList.rmat(int(scales[g]), int(efs[g]), *RMAT_ABC, seed=1000 + g,
+                           symmetrize=True)
+        graphs.append(el)
+        srcs.append(el.sample_sources(BATCH_LANES, 2000 + g))
+        seeds.append(el.sample_sources(BATCH_LANES, 3000 + g))
+    log(f"batched workload: {n_graphs} graphs, V={sum(x.nV for x in graphs)} "
+        f"E={sum(x.nE for x in graphs)}, generated in {time.time() - t:.1f}s")
+    return graphs, np.stack(srcs).astype(np.int32), np.stack(seeds).astype(np.int32), \
+        scales, efs
+
+
+def run_batched(args):
+    import torch
+
+    import graphreduce_gb300 as gg
+    from graphreduce_gb300.engine import initial_vertex_data
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    graphs, srcs, seeds, scales, efs = make_batched_workload(args.batch_graphs)
+    G, L = len(graphs), BATCH_LANES
+    b = gg.Batch()
+    for el in graphs:
+        b.add_graph(el.nV, el.src, el.dst)
+    t = time.time()
+    b.build(sp)
+    V, E = b.num_vertices, b.num_edges
+    if args.launch_list:
+        # one batch run and nothing else (for an ncu launch list / capture)
+        r = b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, piece_edges=256, stream=sp)
+        torch.cuda.synchronize()
+        return {"launch_list": True, "gpu_launches": r.stats.kernel_launches}
+    piece, ms_iter = b.tune(L, PPR_DAMPING, 5, sp)
+    log(f"batch build {time.time() - t:.1f}s; tuned piece {piece} edges, "
+        f"{ms_iter:.3f} ms per PPR iteration")
+    depth_d = torch.empty((V, L), dtype=torch.int32, device=dev)
+    rank_d = torch.empty((V, L), dtype=torch.float32, device=dev)
+    depth_h = torch.empty((V, L), dtype=torch.int32).pin_memory()
+    rank_h = torch.empty((V, L), dtype=torch.float32).pin_memory()
+
+    def step(e2e):
+        if e2e:
+            return b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, depth_out=depth_h.data_ptr(),
+                         rank_out=rank_h.data_ptr(), stream=sp)
+        return b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, depth_out=depth_d.data_ptr(),
+                     rank_out=rank_d.data_ptr(), stream=sp)
+
+    # units: BFS per (graph, lane) the out-degrees of the reached vertices;
+    # PPR per (graph, lane) E_graph x iterations
+    r = step(True)
+    depth = depth_h.numpy()
+    bfs_units = 0
+    for g, el in enumerate(graphs):
+        od = el.out_degree().astype(np.int64)
+        d = depth[b.vertex_offset(g):b.vertex_offset(g) + el.nV]
+        bfs_units += int(((d >= 0) * od[:, None]).sum())
+    ppr_iters = r.stats.ppr_iterations
+    ppr_units = int(sum(el.nE for el in graphs)) * L * ppr_iters
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        z = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        z.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(z) / steps
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms = timed(lambda: step(False), args.steps, args.warmup)
+    clocks = clk.summary()
+    ms_e2e = timed(lambda: step(True), max(1, args.steps), 1)
+    st = step(False).stats
+
+    # BFS-only and PPR-only batch times (device-resident)
+    ms_bfs = timed(lambda: b.run(srcs, None, depth_out=depth_d.data_ptr(), stream=sp),
+                   args.steps, 1)
+    ms_ppr = timed(lambda: b.run(None, seeds, PPR_DAMPING, PPR_TOL,
+                                 rank_out=rank_d.data_ptr(), stream=sp), args.steps, 1)
+
+    # the same instances run one by one on the plain single-graph engines
+    from graphreduce_gb300.learn import DATA, MLP
+    model = MLP.load(DATA / "schedule_head.npz")
+    eb, ep, init_b = [], [], []
+    for el in graphs:
+        e = gg.GASEngineGPU("bfs")
+        e.setGraph(el.nV, initial_vertex_data("bfs", el.nV), el.nE, None, el.src, el.dst, sp)
+        e.set_schedule_model(model)
+        eb.append(e)
+        p = gg.GASEngineGPU("pagerank")
+        p.setGraph(el.nV, initial_vertex_data("pagerank", el.nV, 0, el.out_degree()), el.nE,
+                   None, el.src, el.dst, sp)
+        ep.append(p)
+        init_b.append(torch.from_numpy(initial_vertex_data("bfs", el.nV)).to(dev))
+    out_p = torch.empty(max(el.nV for el in graphs), dtype=torch.float32, device=dev)
+    plain_ppr_iters = [0]
+
+    def plain_bfs():
+        for g, el in enumerate(graphs):
+            for l in range(L):
+                s = int(srcs[g, l])
+                eb[g].upload_vertex_data_ptr(init_b[g].data_ptr(), sp)
+                eb[g].setActive(s, s + 1, sp)
+                eb[g].run_schedule("learned", max_iterations=el.nV + 2, stream=sp)
+
+    def plain_ppr():
+        plain_ppr_iters[0] = 0
+        for g, el in enumerate(graphs):
+            for l in range(L):
+                _, pst = ep[g].ppr_precision(int(seeds[g, l]), PPR_DAMPING, PPR_TOL,
+                                             out=out_p.data_ptr(), stream=sp)
+                plain_ppr_iters[0] += pst.iterations
+
+    ms_plain_bfs = timed(plain_bfs, 1, 1)
+    ms_plain_ppr = timed(plain_ppr, 1, 1)
+    for e in eb + ep:
+        e.close()
+
+    units = bfs_units + ppr_units
+    value = units / (ms * 1e-3) / 1e9
+    # roofline of the PPR iteration (pieces + fix + residual kernels), timed by
+    # the autotuner with CUDA events: per edge its source index and the L
+    # lanes of the source's contribution; per vertex offsets (8 B), seed mask
+    # (4 B), old rank, new rank and new contribution (3 x 4L B)
+    ppr_bytes = E * (4 + 4 * L) + V * (12 + 12 * L)
+    peak, peak_kind = measured_peaks()
+    achieved = ppr_bytes / (ms_iter * 1e-3) / 1e9
+    return {
+        "metric": BATCH_METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32 (BFS) + f32 (PPR, FP64 residual)",
+        "data": "synthetic (seeded R-MAT graphs)",
+        "config": {"workload": f"batched {G} R-MAT graphs, scale U[12,20], edge factor "
+                               f"U[8,32] (seed {BATCH_SEED}), symmetrised; {L} BFS sources + "
+                               f"{L} PPR seeds each (d={PPR_DAMPING}, L1 tol {PPR_TOL})",
+                   "union_V": V, "union_E": E,
+                   "scales": scales.tolist(), "edge_factors": efs.tolist(),
+                   "bfs_units": bfs_units, "ppr_units": ppr_units,
+                   "ppr_iterations": ppr_iters, "bfs_iterations": st.bfs_iterations,
+                   "piece_edges": piece,
+                   "l2": "inputs larger than L2 (union CSR+CSC and [V][16] rank arrays)"},
+        "e2e": {"value": round(units / (ms_e2e * 1e-3) / 1e9, 4), "unit": "GTEPS",
+                "ms_per_step": round(ms_e2e, 3),
+                "h2d_bytes_per_step": int(srcs.nbytes + V * 4),
+                "d2h_bytes_per_step": int(V * L * 8)},
+        "gpu_launches": st.kernel_launches * args.steps,
+        "graph_launches_per_step": st.graph_launches,
+        "split": {"bfs_ms": round(ms_bfs, 3), "ppr_ms": round(ms_ppr, 3),
+                  "bfs_gteps": round(bfs_units / (ms_bfs * 1e-3) / 1e9, 4),
+                  "ppr_gteps": round(ppr_units / (ms_ppr * 1e-3) / 1e9, 4)},
+        "plain_sequential": {
+            "bfs_ms": round(ms_plain_bfs, 3), "ppr_ms": round(ms_plain_ppr, 3),
+            "ppr_iterations_total": plain_ppr_iters[0],
+            "bfs_speedup_of_batch": round(ms_plain_bfs / ms_bfs, 3),
+            "ppr_speedup_of_batch": round(ms_plain_ppr / ms_ppr, 3),
+            "total_speedup_of_batch": round((ms_plain_bfs + ms_plain_ppr) / ms, 3)},
+        "roofline": {"kernel": "PPR iteration (k_ppr_pieces + k_ppr_fix + k_ppr_finish)",
+                     "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": int(ppr_bytes),
+                     "avg_launch_ms": round(ms_iter, 4)},
+        "clocks": clocks,
+    }
+
+
+# ---------------------------------------------------------------------------
 # CPU baseline (the oracle, a C port of refgas.h)
 # ---------------------------------------------------------------------------
 def cpu_sssp_sample(ssp, sources, out_sssp, n_threads):
@@ -420,9 +627,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=int, default=SCALE)
-    ap.add_argument("--schedule", default="auto",
-                    choices=["auto", "generic", "push", "pull", "ordered"])
+    ap.add_argument("--schedule", default="learned",
+                    choices=["learned", "auto", "generic", "push", "pull", "ordered"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="sssp-cc", choices=["sssp-cc", "batched"])
+    ap.add_argument("--batch-graphs", type=int, default=BATCH_GRAPHS)
     ap.add_argument("--launch-list", action="store_true",
                     help="run one device-resident step only (profiling)")
     args = ap.parse_args()
@@ -434,6 +643,11 @@ def main():
         if rank != 0:
             return
         print(json.dumps(run_reference(args)), flush=True)
+        return
+
+    if args.workload == "batched":
+        if rank == 0:
+            print(json.dumps(run_batched(args)), flush=True)
         return
 
     if world > 1:

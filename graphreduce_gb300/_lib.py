@@ -73,6 +73,23 @@ class Counters(C.Structure):
                 ("pad", c_i32 * 4)]
 
 
+GAS_BATCH_MAX_LANES = 32
+
+
+class BatchJob(C.Structure):
+    _fields_ = [("bfs_lanes", c_i32), ("bfs_sources", c_vp), ("ppr_lanes", c_i32),
+                ("ppr_seeds", c_vp), ("damping", c_dbl), ("tol", c_dbl),
+                ("max_bfs_levels", c_i32), ("max_ppr_iterations", c_i32),
+                ("piece_edges", c_i32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("bfs_iterations", c_i32), ("ppr_iterations", c_i32), ("bfs_edges", c_i64),
+                ("ppr_residual", c_dbl), ("piece_edges", c_i32), ("kernel_launches", c_i32),
+                ("graph_launches", c_i32), ("pad", c_i32),
+                ("ppr_lane_residual", c_dbl * GAS_BATCH_MAX_LANES)]
+
+
 # name -> (restype, argtypes); restype "status" means gas_status_t checked.
 _SIGS = {
     "gas_status_string": (C.c_char_p, [c_i32]),
@@ -93,6 +110,10 @@ _SIGS = {
     "gas_edge_list_sample_sources": ("status", [c_vp, c_i32, c_u64, c_vp]),
     "gas_gr_write": ("status", [C.c_char_p, c_vp]),
     "gas_gr_read": ("status", [C.c_char_p, C.POINTER(c_vp)]),
+    "gas_mtx_read": ("status", [C.c_char_p, C.POINTER(c_vp)]),
+    "gas_snap_read": ("status", [C.c_char_p, C.POINTER(c_vp)]),
+    "gas_mtx_write": ("status", [C.c_char_p, c_vp]),
+    "gas_graph_read": ("status", [C.c_char_p, C.POINTER(c_vp)]),
     "gas_edge_list_to_csr": ("status", [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "gas_engine_create": ("status", [c_i32, C.POINTER(c_vp)]),
     "gas_engine_create_user": ("status", [c_size, c_size, c_size, C.POINTER(c_vp)]),
@@ -130,9 +151,23 @@ _SIGS = {
     "gas_engine_get_trace": ("status", [c_vp, c_vp, c_i32, P_i32]),
     "gas_schedule_features": (None, [c_vp, c_i32, c_i64, c_i32, c_vp]),
     "gas_engine_set_schedule_model": ("status", [c_vp, c_vp]),
-    "gas_engine_pagerank_warm_start": ("status", [c_vp, c_vp, c_vp, c_vp]),
+    "gas_engine_pagerank_warm_start": ("status", [c_vp, c_vp, c_dbl, c_vp, c_vp]),
     "gas_engine_pagerank_precision_from": ("status", [c_vp, c_dbl, c_dbl, c_i32, c_vp, c_vp,
                                                       C.POINTER(RunStats), c_vp]),
+    "gas_engine_ppr_precision": ("status", [c_vp, c_i32, c_dbl, c_dbl, c_i32, c_vp,
+                                            C.POINTER(RunStats), c_vp]),
+    "gas_batch_create": ("status", [C.POINTER(c_vp)]),
+    "gas_batch_destroy": (None, [c_vp]),
+    "gas_batch_add_graph": ("status", [c_vp, c_i32, c_i64, c_vp, c_vp, C.POINTER(c_i32)]),
+    "gas_batch_build": ("status", [c_vp, c_vp]),
+    "gas_batch_num_graphs": (c_i32, [c_vp]),
+    "gas_batch_num_vertices": (c_i32, [c_vp]),
+    "gas_batch_num_edges": (c_i64, [c_vp]),
+    "gas_batch_vertex_offset": (c_i32, [c_vp, c_i32]),
+    "gas_batch_run": ("status", [c_vp, C.POINTER(BatchJob), c_vp, c_vp,
+                                 C.POINTER(BatchStats), c_vp]),
+    "gas_batch_tune": ("status", [c_vp, c_i32, c_dbl, c_i32, C.POINTER(c_i32),
+                                  C.POINTER(C.c_float), c_vp]),
     "gas_engine_view_get": ("status", [c_vp, c_vp]),
     "gas_engine_note_applied": ("status", [c_vp, c_i32]),
     "gas_engine_read_counters": ("status", [c_vp, C.POINTER(Counters), c_vp]),

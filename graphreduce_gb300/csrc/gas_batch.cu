@@ -1,0 +1,1123 @@
+// gas_batch.cu -- many BFS sources and personalized-PageRank seeds over many
+// graphs in one CUDA-graph launch (no reference counterpart).
+//
+// The graphs are concatenated into one disjoint union graph (vertex ids
+// offset per graph), so one device loop serves every instance:
+//
+//   * multi-source BFS: lane l of a vertex belongs to source l of the
+//     vertex's own graph (graphs are disjoint, so lanes of different graphs
+//     never meet).  visited[v] and next[v] are 32-bit lane masks.  One level
+//     pushes every queued vertex's new-lane mask to its out-neighbours
+//     (atomicOr, pre-filtered by visited), marking touched vertices in a
+//     bitmap; a two-pass compaction over that bitmap writes the level into
+//     depth[v][l] for every new lane, folds the lanes into visited and
+//     builds the next queue (vertex, lane mask, inclusive out-edge ends).
+//     Depths equal those of one BFS per source.
+//   * multi-seed personalized PageRank, r_l = (1-d) e_{s_l} + d A^T D^-1 r_l
+//     for every lane l at once: ranks and contributions are [V][L] rows, so
+//     the L lanes of an in-edge's source are one contiguous 4L-byte read.
+//     The CSC edge range is cut into pieces of P edges (P autotuned); a group
+//     of L threads (one per lane) folds a piece in edge order with FP32
+//     two-sum compensation, finishing every row that lies inside the piece;
+//     rows cut by piece boundaries leave per-piece partials that a second
+//     pass folds in piece order.  The sums are deterministic.  The loop runs
+//     until the largest per-lane FP64 L1 residual is <= tol.
+//
+// Both loops are WHILE nodes of one CUDA graph (BFS loop, then PPR loop),
+// each preceded by its prologue; a run is one cudaGraphLaunch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "gas.h"
+#include "gas_device.cuh"
+#include "gas_engine_impl.h"
+#include "gas_internal.h"
+#include "gas_sched.h"
+
+using gasdev::kNT;
+using gas::fail;
+
+namespace {
+
+inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+constexpr int kMaxLanes = GAS_BATCH_MAX_LANES;
+
+// Device parameters of a run (read by the captured kernels, so that one
+// instantiated graph serves any sources, seeds, damping, tolerance and caps).
+struct BatchParams {
+  double damping;
+  double tol;
+  int32_t bfs_max_iter;
+  int32_t ppr_max_iter;
+  int32_t n_sources;  // G * bfs_lanes
+  int32_t pad;
+};
+
+__device__ __forceinline__ int warp_incl(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int o = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= d) v += o;
+  }
+  return v;
+}
+
+// Exclusive CTA scan of one int per thread (kNT threads); *total gets the sum.
+__device__ __forceinline__ int cta_excl(int v, int *total) {
+  __shared__ int s_w[kNT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int incl = warp_incl(v);
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  int pre = 0, tot = 0;
+  for (int w = 0; w < kNT / 32; ++w) {
+    if (w < warp) pre += s_w[w];
+    tot += s_w[w];
+  }
+  __syncthreads();
+  *total = tot;
+  return pre + incl - v;
+}
+
+__device__ __forceinline__ void set_cond(gas_counters *cnt, bool more, int it,
+                                         cudaGraphConditionalHandle h, int in_graph) {
+  if (more && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
+  cnt->cond = (more && it < cnt->max_iter) ? 1 : 0;
+  if (in_graph) cudaGraphSetConditional(h, cnt->cond);
+}
+
+__global__ void k_b_reset(gas_counters *cnt, const BatchParams *prm, int which,
+                          unsigned long long *edges) {
+  cnt->iteration = 0;
+  cnt->error = 0;
+  cnt->cond = 0;
+  cnt->n_changed = 0;
+  cnt->n_scatter_edges = 0;
+  cnt->max_iter = which == 0 ? prm->bfs_max_iter : prm->ppr_max_iter;
+  if (edges) *edges = 0ull;
+}
+
+// ---------------------------------------------------------------------------
+// multi-source BFS
+// ---------------------------------------------------------------------------
+struct MsPushPol {
+  typedef int32_t Val;
+  static constexpr bool kMapNeedsVertex = false;
+  const int32_t *csr_dst;
+  const int32_t *q_mask;
+  const uint32_t *visited;
+  uint32_t *next;
+  uint32_t *tbits;
+  __device__ Val zero() const { return 0; }
+  __device__ Val reduce(Val a, Val) const { return a; }
+  __device__ Val map(int, int, int) const { return 0; }
+  __device__ void emit(int, int, Val) const {}
+  // a: queue position of the pushing vertex, pos: CSR position of the edge
+  __device__ __forceinline__ void visit(int a, int, int pos) const {
+    const int v = __ldg(csr_dst + pos);
+    const uint32_t m = (uint32_t)__ldg(q_mask + a) & ~visited[v];
+    if (m) {
+      const uint32_t old = atomicOr(next + v, m);
+      if (old == 0u) atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
+    }
+  }
+};
+
+__global__ void __launch_bounds__(kNT)
+    k_ms_push(MsPushPol pol, gasdev::SlabSource src) {
+  gasdev::slab_loop<MsPushPol, false>(pol, src, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+// Level 0: every (graph, lane) source.
+__global__ void k_ms_seed(const int32_t *src_global, const BatchParams *prm, int L,
+                          uint32_t *next, uint32_t *tbits) {
+  const int n = prm->n_sources;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int v = src_global[i];
+    if (v < 0) continue;
+    atomicOr(next + v, 1u << (i % L));
+    atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
+  }
+}
+
+// The touched-vertex traversal shared by the two compaction passes: thread t
+// of a warp owns word w0 + t of the bitmap; the warp walks its 32 words one
+// at a time, lane l taking vertex 32 * word + l.  Counts this thread's queue
+// entries (vertices with new lanes and out-edges) and their out-edge total.
+__device__ __forceinline__ void ms_counts(uint32_t mine, int w0, const uint32_t *next,
+                                          const uint32_t *visited, const int32_t *csr_off,
+                                          int &q, int &d) {
+  const int lane = threadIdx.x & 31;
+  q = 0;
+  d = 0;
+  for (int i = 0; i < 32; ++i) {
+    const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
+    if (!word || !((word >> lane) & 1u)) continue;
+    const int v = (w0 + i) * 32 + lane;
+    const int deg = csr_off[v + 1] - csr_off[v];
+    if (deg > 0 && (next[v] & ~visited[v])) {
+      ++q;
+      d += deg;
+    }
+  }
+}
+
+// Pass 1: per block (queue entries, out-edges).
+__global__ void __launch_bounds__(kNT)
+    k_ms_count(const uint32_t *tbits, const uint32_t *next, const uint32_t *visited,
+               const int32_t *csr_off, int nW, int32_t *part) {
+  const int lane = threadIdx.x & 31;
+  const int w0 = blockIdx.x * kNT + threadIdx.x - lane;
+  const uint32_t mine = (w0 + lane < nW) ? tbits[w0 + lane] : 0u;
+  int q, d, tq, td;
+  ms_counts(mine, w0, next, visited, csr_off, q, d);
+  cta_excl(q, &tq);
+  cta_excl(d, &td);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = tq;
+    part[2 * blockIdx.x + 1] = td;
+  }
+}
+
+// Exclusive scan of the block pairs; totals into the counters.
+__global__ void __launch_bounds__(kNT)
+    k_ms_spine(int32_t *part, int nb, gas_counters *cnt) {
+  __shared__ int s_c[2];
+  if (threadIdx.x < 2) s_c[threadIdx.x] = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += kNT) {
+    const int i = base + threadIdx.x;
+    const int vq = i < nb ? part[2 * i] : 0, vd = i < nb ? part[2 * i + 1] : 0;
+    int tq, td;
+    const int eq = cta_excl(vq, &tq), ed = cta_excl(vd, &td);
+    const int cq = s_c[0], cd = s_c[1];
+    if (i < nb) {
+      part[2 * i] = cq + eq;
+      part[2 * i + 1] = cd + ed;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_c[0] = cq + tq;
+      s_c[1] = cd + td;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    cnt->n_changed = s_c[0];
+    cnt->n_scatter_edges = s_c[1];
+  }
+}
+
+// Pass 2: depths of the new lanes, visited, the next queue; clears next and
+// the touched bitmap.  level = counters.iteration + level_add.
+__global__ void __launch_bounds__(kNT)
+    k_ms_write(uint32_t *tbits, uint32_t *next, uint32_t *visited, const int32_t *csr_off,
+               int nW, const int32_t *part, int L, const gas_counters *cnt, int level_add,
+               int32_t *depth, int32_t *q_ids, int32_t *q_mask, int32_t *q_end,
+               int32_t *q_delta) {
+  const int level = cnt->iteration + level_add;
+  const int lane = threadIdx.x & 31;
+  const int w0 = blockIdx.x * kNT + threadIdx.x - lane;
+  const uint32_t mine = (w0 + lane < nW) ? tbits[w0 + lane] : 0u;
+  int q, d, tq, td;
+  ms_counts(mine, w0, next, visited, csr_off, q, d);
+  int pq = cta_excl(q, &tq) + part[2 * blockIdx.x];
+  int pd = cta_excl(d, &td) + part[2 * blockIdx.x + 1];
+  for (int i = 0; i < 32; ++i) {
+    const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
+    if (!word || !((word >> lane) & 1u)) continue;
+    const int v = (w0 + i) * 32 + lane;
+    const uint32_t nw = next[v] & ~visited[v];
+    next[v] = 0u;
+    if (!nw) continue;
+    visited[v] |= nw;
+    for (uint32_t m = nw; m; m &= m - 1) depth[(size_t)v * L + (__ffs(m) - 1)] = level;
+    const int off = csr_off[v];
+    const int deg = csr_off[v + 1] - off;
+    if (deg > 0) {
+      pd += deg;
+      q_ids[pq] = v;
+      q_mask[pq] = (int32_t)nw;
+      q_end[pq] = pd;
+      q_delta[pq] = off - (pd - deg);
+      ++pq;
+    }
+  }
+  if (w0 + lane < nW && mine) tbits[w0 + lane] = 0u;
+}
+
+// Loop condition after the prologue (level 0 written, no push run yet).
+__global__ void k_ms_precond(gas_counters *cnt, unsigned long long *edges,
+                             cudaGraphConditionalHandle h, int in_graph) {
+  set_cond(cnt, cnt->n_scatter_edges > 0, 0, h, in_graph);
+  if (cnt->cond) *edges += (unsigned long long)cnt->n_scatter_edges;
+}
+
+__global__ void k_ms_cond(gas_counters *cnt, unsigned long long *edges,
+                          cudaGraphConditionalHandle h, int in_graph) {
+  const int it = ++cnt->iteration;
+  set_cond(cnt, cnt->n_scatter_edges > 0, it, h, in_graph);
+  if (cnt->cond) *edges += (unsigned long long)cnt->n_scatter_edges;
+}
+
+// ---------------------------------------------------------------------------
+// multi-seed personalized PageRank
+// ---------------------------------------------------------------------------
+struct CVal {
+  float s, c;
+};
+
+// Knuth two-sum: a.s + b.s = s + err exactly; compensations add up in c.
+__device__ __forceinline__ CVal two_sum_add(CVal a, CVal b) {
+  const float s = __fadd_rn(a.s, b.s);
+  const float bp = __fsub_rn(s, a.s);
+  const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bp)), __fsub_rn(b.s, bp));
+  return CVal{s, __fadd_rn(__fadd_rn(a.c, b.c), err)};
+}
+
+struct PprArgs {
+  const int32_t *csc_off, *csc_src, *csr_off;
+  const int32_t *first_row;  // [n_pieces] first row with an edge in the piece
+  int32_t n_pieces, P, E, L, G;
+  const int32_t *fix;        // [n_fix][3] (row, first piece, last piece)
+  int32_t n_fix;
+  CVal *head, *tail;         // [n_pieces][L] partials of cut rows
+  float *rank[2], *contrib[2];
+  const uint32_t *seed_mask;
+  const BatchParams *prm;
+  gas_counters *cnt;
+};
+
+struct PprLane {
+  const float *contrib, *rank_old;
+  float *rank_new, *contrib_new;
+  float d, base;
+  int l;
+  bool on;
+};
+
+__device__ __forceinline__ PprLane ppr_lane(const PprArgs &a) {
+  PprLane o;
+  const int p = a.cnt->iteration & 1;
+  o.contrib = a.contrib[p];
+  o.rank_old = a.rank[p];
+  o.rank_new = a.rank[p ^ 1];
+  o.contrib_new = a.contrib[p ^ 1];
+  o.d = (float)a.prm->damping;
+  o.base = (float)(1.0 - a.prm->damping);
+  o.l = threadIdx.x % a.G;
+  o.on = o.l < a.L;
+  return o;
+}
+
+__device__ __forceinline__ void ppr_finish_row(const PprArgs &a, const PprLane &t, int v,
+                                               CVal acc, double &l1) {
+  const float sum = __fadd_rn(acc.s, acc.c);
+  const float b = ((__ldg(a.seed_mask + v) >> t.l) & 1u) ? t.base : 0.f;
+  const float r = __fadd_rn(b, __fmul_rn(t.d, sum));
+  const int deg = __ldg(a.csr_off + v + 1) - __ldg(a.csr_off + v);
+  const size_t k = (size_t)v * a.L + t.l;
+  l1 += fabs((double)r - (double)t.rank_old[k]);
+  t.rank_new[k] = r;
+  t.contrib_new[k] = deg ? __fdiv_rn(r, (float)deg) : 0.f;
+}
+
+// Edge-order compensated fold of one lane over [e, stop).
+__device__ __forceinline__ CVal ppr_fold(const PprArgs &a, const PprLane &t, int e, int stop) {
+  CVal acc{0.f, 0.f};
+  constexpr int U = 8;
+  for (; e + U <= stop; e += U) {
+    int u[U];
+    float x[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) u[j] = __ldg(a.csc_src + e + j);
+#pragma unroll
+    for (int j = 0; j < U; ++j) x[j] = __ldg(t.contrib + (size_t)u[j] * a.L + t.l);
+#pragma unroll
+    for (int j = 0; j < U; ++j) acc = two_sum_add(acc, CVal{x[j], 0.f});
+  }
+  for (; e < stop; ++e) {
+    const int u = __ldg(a.csc_src + e);
+    acc = two_sum_add(acc, CVal{__ldg(t.contrib + (size_t)u * a.L + t.l), 0.f});
+  }
+  return acc;
+}
+
+// Per-lane block sums of l1 in a fixed order into out[lane].
+__device__ __forceinline__ void lane_block_sums(double l1, int G, double *out) {
+  __shared__ double s[kNT];
+  s[threadIdx.x] = l1;
+  __syncthreads();
+  if (threadIdx.x < G) {
+    double t = 0.0;
+    for (int j = threadIdx.x; j < kNT; j += G) t += s[j];
+    out[threadIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kNT) k_ppr_pieces(PprArgs a, double *l1_part) {
+  const PprLane t = ppr_lane(a);
+  const int per_block = kNT / a.G;
+  const int local = threadIdx.x / a.G;
+  double l1 = 0.0;
+  if (t.on) {
+    for (int k = blockIdx.x * per_block + local; k < a.n_pieces; k += gridDim.x * per_block) {
+      int e = k * a.P;
+      const int end = min(a.E, e + a.P);
+      int r = __ldg(a.first_row + k);
+      int row_end = __ldg(a.csc_off + r + 1);
+      bool cont = __ldg(a.csc_off + r) < e;
+      for (;;) {
+        const int stop = min(row_end, end);
+        const CVal acc = ppr_fold(a, t, e, stop);
+        if (stop < row_end) {  // the piece ends inside row r
+          (cont ? a.head : a.tail)[(size_t)k * a.L + t.l] = acc;
+          break;
+        }
+        if (cont)
+          a.head[(size_t)k * a.L + t.l] = acc;
+        else
+          ppr_finish_row(a, t, r, acc, l1);
+        if (stop == end) break;
+        do {  // next row with in-edges (one exists: stop < end <= E)
+          ++r;
+          row_end = __ldg(a.csc_off + r + 1);
+        } while (row_end == stop);
+        cont = false;
+        e = stop;
+      }
+    }
+  }
+  lane_block_sums(l1, a.G, l1_part + (size_t)blockIdx.x * a.G);
+}
+
+// Rows cut by piece boundaries (partials folded in piece order) and rows
+// without in-edges (first piece -1).
+__global__ void __launch_bounds__(kNT) k_ppr_fix(PprArgs a, double *l1_part) {
+  const PprLane t = ppr_lane(a);
+  const int per_block = kNT / a.G;
+  const int local = threadIdx.x / a.G;
+  double l1 = 0.0;
+  if (t.on) {
+    for (int i = blockIdx.x * per_block + local; i < a.n_fix; i += gridDim.x * per_block) {
+      const int v = a.fix[3 * i], ps = a.fix[3 * i + 1], pe = a.fix[3 * i + 2];
+      CVal acc{0.f, 0.f};
+      if (ps >= 0) {
+        acc = a.tail[(size_t)ps * a.L + t.l];
+        for (int k = ps + 1; k <= pe; ++k) acc = two_sum_add(acc, a.head[(size_t)k * a.L + t.l]);
+      }
+      ppr_finish_row(a, t, v, acc, l1);
+    }
+  }
+  lane_block_sums(l1, a.G, l1_part + (size_t)blockIdx.x * a.G);
+}
+
+// Per-lane residuals (fixed-order sums over the blocks); the loop goes on
+// while the largest is above tol.
+__global__ void __launch_bounds__(kNT)
+    k_ppr_finish(const double *l1_part, int nblocks, int G, int L, const BatchParams *prm,
+                 gas_counters *cnt, double *lane_resid, cudaGraphConditionalHandle h,
+                 int in_graph) {
+  __shared__ double s[kNT];
+  const int l = threadIdx.x % G, j = threadIdx.x / G, nj = kNT / G;
+  double v = 0.0;
+  for (int b = j; b < nblocks; b += nj) v += l1_part[(size_t)b * G + l];
+  s[threadIdx.x] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < G)
+    for (int q = 0; q < nj; ++q) t += s[q * G + threadIdx.x];
+  __syncthreads();
+  if (threadIdx.x < G) s[threadIdx.x] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mx = 0.0;
+    for (int q = 0; q < L; ++q) {
+      lane_resid[1 + q] = s[q];
+      mx = s[q] > mx ? s[q] : mx;
+    }
+    lane_resid[0] = mx;
+    const int it = ++cnt->iteration;
+    set_cond(cnt, !(mx <= prm->tol), it, h, in_graph);
+  }
+}
+
+// r0 = e_seed per lane; contributions accordingly.
+__global__ void k_ppr_init(const uint32_t *seed_mask, const int32_t *csr_off, int nV, int L,
+                           float *rank, float *contrib) {
+  const size_t n = (size_t)nV * L;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int v = (int)(k / L), l = (int)(k % L);
+    const float r = ((seed_mask[v] >> l) & 1u) ? 1.f : 0.f;
+    const int deg = csr_off[v + 1] - csr_off[v];
+    rank[k] = r;
+    contrib[k] = deg ? __fdiv_rn(r, (float)deg) : 0.f;
+  }
+}
+
+__global__ void k_ppr_precond(gas_counters *cnt, cudaGraphConditionalHandle h, int in_graph) {
+  set_cond(cnt, true, 0, h, in_graph);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// The batch object.
+// ---------------------------------------------------------------------------
+struct gas_batch {
+  std::vector<int32_t> v_off{0};  // first vertex of every graph; back() = V
+  std::vector<int32_t> src, dst;  // union edge list (global ids) until built
+  int64_t n_edges = 0;
+  gas_engine *eng = nullptr;      // holds the union graph (CSR + CSC)
+  bool built = false;
+  gas_counters *cnt = nullptr;    // [2] device: BFS loop, PPR loop
+  gas_counters *h_cnt = nullptr;  // [2] pinned
+  BatchParams *prm = nullptr;     // device
+  unsigned long long *edges = nullptr;  // BFS edges pushed
+  double *resid = nullptr;        // [1 + 32] max and per-lane PPR residual
+  // BFS
+  uint32_t *visited = nullptr, *next = nullptr, *tbits = nullptr;
+  int32_t *depth = nullptr, *q_ids = nullptr, *q_mask = nullptr, *q_end = nullptr,
+          *q_delta = nullptr, *part = nullptr, *qpart = nullptr, *srcs = nullptr;
+  int32_t depth_lanes = 0, srcs_cap = 0;
+  // PPR
+  int32_t *first_row = nullptr, *fix = nullptr;
+  CVal *head = nullptr, *tail = nullptr;
+  float *rank[2] = {nullptr, nullptr}, *contrib[2] = {nullptr, nullptr};
+  uint32_t *seed_mask = nullptr;
+  double *l1 = nullptr;
+  int32_t n_pieces = 0, n_fix = 0, piece_edges = 0, ppr_lanes = 0, l1_cap = 0;
+  int32_t tuned_piece = 0;
+  // cached graph
+  cudaGraphExec_t graph = nullptr;
+  int32_t g_bfs_lanes = -1, g_ppr_lanes = -1, g_piece = -1;
+};
+
+namespace {
+
+template <class T>
+void bfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+void drop_graph(gas_batch *b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->g_bfs_lanes = b->g_ppr_lanes = b->g_piece = -1;
+}
+
+void free_state(gas_batch *b) {
+  drop_graph(b);
+  bfree(b->visited); bfree(b->next); bfree(b->tbits); bfree(b->depth);
+  bfree(b->q_ids); bfree(b->q_mask); bfree(b->q_end); bfree(b->q_delta);
+  bfree(b->part); bfree(b->qpart); bfree(b->srcs);
+  bfree(b->first_row); bfree(b->fix); bfree(b->head); bfree(b->tail);
+  bfree(b->seed_mask); bfree(b->l1);
+  for (int i = 0; i < 2; ++i) { bfree(b->rank[i]); bfree(b->contrib[i]); }
+  b->n_pieces = b->n_fix = b->piece_edges = b->ppr_lanes = b->depth_lanes = 0;
+  b->srcs_cap = b->l1_cap = 0;
+}
+
+int lane_group(int L) {
+  int g = 1;
+  while (g < L) g <<= 1;
+  return g;
+}
+
+int nwords(const gas_batch *b) { return (b->eng->nV + 31) / 32; }
+int ms_blocks(const gas_batch *b) { return std::max(1, (nwords(b) + kNT - 1) / kNT); }
+
+gas_status_t ensure_bfs(gas_batch *b, int lanes, int n_sources) {
+  gas_engine *e = b->eng;
+  const size_t nV = std::max(1, e->nV), nW = std::max(1, nwords(b));
+  if (!b->visited) {
+    CUDA_TRY(cudaMalloc(&b->visited, nV * 4));
+    CUDA_TRY(cudaMalloc(&b->next, nV * 4));
+    CUDA_TRY(cudaMalloc(&b->tbits, nW * 4));
+    for (int32_t **p : {&b->q_ids, &b->q_mask, &b->q_end, &b->q_delta})
+      CUDA_TRY(cudaMalloc(p, nV * 4));
+    CUDA_TRY(cudaMalloc(&b->part, ((size_t)e->nE / gasdev::kSlabChunk + 2) * 4));
+    CUDA_TRY(cudaMalloc(&b->qpart, 2 * ((size_t)ms_blocks(b) + 1) * 4));
+  }
+  if (b->depth_lanes != lanes) {
+    drop_graph(b);
+    bfree(b->depth);
+    CUDA_TRY(cudaMalloc(&b->depth, nV * lanes * 4));
+    b->depth_lanes = lanes;
+  }
+  if (b->srcs_cap < n_sources) {
+    drop_graph(b);
+    bfree(b->srcs);
+    CUDA_TRY(cudaMalloc(&b->srcs, (size_t)std::max(1, n_sources) * 4));
+    b->srcs_cap = n_sources;
+  }
+  return GAS_OK;
+}
+
+// Pieces of P edges over the CSC, their first rows, and the rows the second
+// pass finishes (cut rows and rows without in-edges).
+gas_status_t ensure_ppr(gas_batch *b, int lanes, int P, int grid_pieces, int grid_fix) {
+  gas_engine *e = b->eng;
+  const size_t nV = std::max(1, e->nV);
+  if (b->ppr_lanes != lanes) {
+    drop_graph(b);
+    for (int i = 0; i < 2; ++i) { bfree(b->rank[i]); bfree(b->contrib[i]); }
+    for (int i = 0; i < 2; ++i) {
+      CUDA_TRY(cudaMalloc(&b->rank[i], nV * lanes * 4));
+      CUDA_TRY(cudaMalloc(&b->contrib[i], nV * lanes * 4));
+    }
+    b->ppr_lanes = lanes;
+    b->piece_edges = 0;  // head/tail are sized by lanes
+  }
+  if (!b->seed_mask) CUDA_TRY(cudaMalloc(&b->seed_mask, nV * 4));
+  const int G = lane_group(lanes);
+  const int need_l1 = (grid_pieces + grid_fix) * G;
+  if (b->l1_cap < need_l1) {
+    drop_graph(b);
+    bfree(b->l1);
+    CUDA_TRY(cudaMalloc(&b->l1, (size_t)need_l1 * sizeof(double)));
+    b->l1_cap = need_l1;
+  }
+  if (b->piece_edges == P) return GAS_OK;
+  drop_graph(b);
+  const std::vector<int32_t> &off = e->h_csc_off;
+  const int32_t E = e->nE, V = e->nV;
+  const int32_t n_pieces = (int32_t)(((int64_t)E + P - 1) / P);
+  std::vector<int32_t> first((size_t)std::max(1, n_pieces));
+  for (int32_t k = 0, r = 0; k < n_pieces; ++k) {
+    const int64_t e0 = (int64_t)k * P;
+    while (off[r + 1] <= e0) ++r;  // first row with csc_off[r+1] > e0
+    first[k] = r;
+  }
+  std::vector<int32_t> fix;
+  for (int32_t v = 0; v < V; ++v) {
+    const int32_t lo = off[v], hi = off[v + 1];
+    if (lo == hi) {
+      fix.insert(fix.end(), {v, -1, -1});
+    } else {
+      const int32_t ps = lo / P, pe = (hi - 1) / P;
+      if (ps != pe) fix.insert(fix.end(), {v, ps, pe});
+    }
+  }
+  bfree(b->first_row);
+  bfree(b->fix);
+  bfree(b->head);
+  bfree(b->tail);
+  CUDA_TRY(cudaMalloc(&b->first_row, first.size() * 4));
+  CUDA_TRY(cudaMalloc(&b->fix, std::max<size_t>(1, fix.size()) * 4));
+  const size_t hp = std::max<size_t>(1, (size_t)n_pieces * lanes) * sizeof(CVal);
+  CUDA_TRY(cudaMalloc(&b->head, hp));
+  CUDA_TRY(cudaMalloc(&b->tail, hp));
+  CUDA_TRY(cudaMemcpy(b->first_row, first.data(), first.size() * 4, cudaMemcpyHostToDevice));
+  if (!fix.empty())
+    CUDA_TRY(cudaMemcpy(b->fix, fix.data(), fix.size() * 4, cudaMemcpyHostToDevice));
+  b->n_pieces = n_pieces;
+  b->n_fix = (int32_t)(fix.size() / 3);
+  b->piece_edges = P;
+  return GAS_OK;
+}
+
+struct RunCtx {
+  gas_batch *b;
+  int bfs_lanes, ppr_lanes;
+  int slab_grid, grid_pieces, grid_fix;
+  PprArgs ppr;
+};
+
+PprArgs ppr_args(gas_batch *b, int lanes) {
+  gas_engine *e = b->eng;
+  PprArgs a;
+  a.csc_off = e->csc_off;
+  a.csc_src = e->csc_src;
+  a.csr_off = e->csr_off;
+  a.first_row = b->first_row;
+  a.n_pieces = b->n_pieces;
+  a.P = b->piece_edges;
+  a.E = e->nE;
+  a.L = lanes;
+  a.G = lane_group(lanes);
+  a.fix = b->fix;
+  a.n_fix = b->n_fix;
+  a.head = b->head;
+  a.tail = b->tail;
+  for (int i = 0; i < 2; ++i) {
+    a.rank[i] = b->rank[i];
+    a.contrib[i] = b->contrib[i];
+  }
+  a.seed_mask = b->seed_mask;
+  a.prm = b->prm;
+  a.cnt = b->cnt + 1;
+  return a;
+}
+
+typedef gas_status_t (*StepFn)(RunCtx *, cudaStream_t, cudaGraphConditionalHandle, int);
+
+gas_status_t bfs_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
+  gas_batch *b = c->b;
+  gas_engine *e = b->eng;
+  const size_t nV = std::max(1, e->nV), nW = std::max(1, nwords(b));
+  const int L = c->bfs_lanes, nb = ms_blocks(b);
+  k_b_reset<<<1, 1, 0, s>>>(b->cnt, b->prm, 0, b->edges);
+  CUDA_TRY(cudaMemsetAsync(b->visited, 0, nV * 4, s));
+  CUDA_TRY(cudaMemsetAsync(b->next, 0, nV * 4, s));
+  CUDA_TRY(cudaMemsetAsync(b->tbits, 0, nW * 4, s));
+  CUDA_TRY(cudaMemsetAsync(b->depth, 0xff, nV * L * 4, s));
+  k_ms_seed<<<2 * e->num_sms, 256, 0, s>>>(b->srcs, b->prm, L, b->next, b->tbits);
+  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart);
+  k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
+  k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
+                               L, b->cnt, 0, b->depth, b->q_ids, b->q_mask, b->q_end,
+                               b->q_delta);
+  k_ms_precond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
+  gas_batch *b = c->b;
+  gas_engine *e = b->eng;
+  const int nb = ms_blocks(b);
+  const gasdev::SlabSource q = gasdev::slab_source(
+      b->q_end, b->q_ids, b->q_delta, 0, 0, &b->cnt->n_changed, &b->cnt->n_scatter_edges,
+      b->part);
+  gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, s>>>(q, b->part);
+  MsPushPol pol{e->csr_dst, b->q_mask, b->visited, b->next, b->tbits};
+  k_ms_push<<<c->slab_grid, kNT, 0, s>>>(pol, q);
+  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart);
+  k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
+  k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
+                               c->bfs_lanes, b->cnt, 1, b->depth, b->q_ids, b->q_mask,
+                               b->q_end, b->q_delta);
+  k_ms_cond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t ppr_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
+  gas_batch *b = c->b;
+  gas_engine *e = b->eng;
+  k_b_reset<<<1, 1, 0, s>>>(b->cnt + 1, b->prm, 1, nullptr);
+  k_ppr_init<<<8 * e->num_sms, 256, 0, s>>>(b->seed_mask, e->csr_off, e->nV, c->ppr_lanes,
+                                           b->rank[0], b->contrib[0]);
+  k_ppr_precond<<<1, 1, 0, s>>>(b->cnt + 1, h, ig);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t ppr_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
+  gas_batch *b = c->b;
+  const int G = c->ppr.G;
+  k_ppr_pieces<<<c->grid_pieces, kNT, 0, s>>>(c->ppr, b->l1);
+  k_ppr_fix<<<c->grid_fix, kNT, 0, s>>>(c->ppr, b->l1 + (size_t)c->grid_pieces * G);
+  k_ppr_finish<<<1, kNT, 0, s>>>(b->l1, c->grid_pieces + c->grid_fix, G, c->ppr_lanes,
+                                 b->prm, b->cnt + 1, b->resid, h, ig);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+struct Loop {
+  StepFn pro, body;
+};
+
+// One graph: for each loop, its prologue then WHILE(cond) { body }.
+gas_status_t build_chain(RunCtx *c, const Loop *loops, int n, cudaGraphExec_t *out) {
+  cudaGraph_t g = nullptr;
+  cudaStream_t cs = nullptr;
+  gas_status_t st = GAS_OK;
+  CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaError_t ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(GAS_ERR_CUDA, "batch graph stream: %s", cudaGetErrorString(ce));
+  }
+  cudaGraphNode_t prev = nullptr;
+  for (int i = 0; i < n && st == GAS_OK; ++i) {
+    cudaGraphConditionalHandle h;
+    ce = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    if (ce == cudaSuccess)
+      ce = cudaStreamBeginCaptureToGraph(cs, g, prev ? &prev : nullptr, nullptr, prev ? 1 : 0,
+                                         cudaStreamCaptureModeRelaxed);
+    if (ce != cudaSuccess) {
+      st = fail(GAS_ERR_CUDA, "batch prologue capture: %s", cudaGetErrorString(ce));
+      break;
+    }
+    st = loops[i].pro(c, cs, h, 1);
+    std::vector<cudaGraphNode_t> deps;
+    if (st == GAS_OK) {
+      cudaStreamCaptureStatus cst;
+      const cudaGraphNode_t *d = nullptr;
+      size_t nd = 0;
+      ce = cudaStreamGetCaptureInfo(cs, &cst, nullptr, nullptr, &d, nullptr, &nd);
+      if (ce == cudaSuccess) deps.assign(d, d + nd);
+      else st = fail(GAS_ERR_CUDA, "capture info: %s", cudaGetErrorString(ce));
+    }
+    cudaGraph_t cap = nullptr;
+    ce = cudaStreamEndCapture(cs, &cap);
+    if (st == GAS_OK && ce != cudaSuccess)
+      st = fail(GAS_ERR_CUDA, "end prologue capture: %s", cudaGetErrorString(ce));
+    if (st != GAS_OK) break;
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    ce = cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &p);
+    if (ce != cudaSuccess) {
+      st = fail(GAS_ERR_CUDA, "add while node: %s", cudaGetErrorString(ce));
+      break;
+    }
+    ce = cudaStreamBeginCaptureToGraph(cs, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeRelaxed);
+    if (ce != cudaSuccess) {
+      st = fail(GAS_ERR_CUDA, "body capture: %s", cudaGetErrorString(ce));
+      break;
+    }
+    st = loops[i].body(c, cs, h, 1);
+    cudaGraph_t bc = nullptr;
+    ce = cudaStreamEndCapture(cs, &bc);
+    if (st == GAS_OK && ce != cudaSuccess)
+      st = fail(GAS_ERR_CUDA, "end body capture: %s", cudaGetErrorString(ce));
+    prev = node;
+  }
+  if (st == GAS_OK) {
+    ce = cudaGraphInstantiate(out, g, 0);
+    if (ce != cudaSuccess) st = fail(GAS_ERR_CUDA, "instantiate: %s", cudaGetErrorString(ce));
+  }
+  cudaStreamDestroy(cs);
+  cudaGraphDestroy(g);
+  return st;
+}
+
+// The same loops as direct launches with one host read of the condition per
+// iteration (GAS_HOST_LOOP=1: ncu cannot profile kernels inside graphs with
+// conditional nodes).
+gas_status_t run_direct(RunCtx *c, const Loop *loops, const int *which, int n, cudaStream_t s) {
+  gas_batch *b = c->b;
+  for (int i = 0; i < n; ++i) {
+    GAS_TRY(loops[i].pro(c, s, 0, 0));
+    for (;;) {
+      CUDA_TRY(cudaMemcpyAsync(b->h_cnt + which[i], b->cnt + which[i], sizeof(gas_counters),
+                               cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaStreamSynchronize(s));
+      if (!b->h_cnt[which[i]].cond) break;
+      GAS_TRY(loops[i].body(c, s, 0, 0));
+    }
+  }
+  return GAS_OK;
+}
+
+void grids(gas_batch *b, RunCtx *c) {
+  gas_engine *e = b->eng;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ms_push, kNT, 0);
+  c->slab_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);
+  per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ppr_pieces, kNT, 0);
+  c->grid_pieces = e->num_sms * (per_sm > 0 ? per_sm : 1);
+  c->grid_fix = 2 * e->num_sms;
+}
+
+gas_status_t check_job(const gas_batch *b, const gas_batch_job *j) {
+  if (!j) return fail(GAS_ERR_INVALID, "null job");
+  if (j->bfs_lanes < 0 || j->bfs_lanes > kMaxLanes || j->ppr_lanes < 0 ||
+      j->ppr_lanes > kMaxLanes)
+    return fail(GAS_ERR_INVALID, "lanes must be in [0, %d]", kMaxLanes);
+  if (j->bfs_lanes == 0 && j->ppr_lanes == 0)
+    return fail(GAS_ERR_INVALID, "job has neither BFS nor PPR lanes");
+  if (j->bfs_lanes > 0 && !j->bfs_sources) return fail(GAS_ERR_INVALID, "null bfs_sources");
+  if (j->ppr_lanes > 0) {
+    if (!j->ppr_seeds) return fail(GAS_ERR_INVALID, "null ppr_seeds");
+    if (!(j->damping > 0.0 && j->damping < 1.0) || !(j->tol > 0.0))
+      return fail(GAS_ERR_INVALID, "damping must be in (0,1), tol > 0");
+  }
+  if (j->piece_edges < 0 || j->piece_edges > (1 << 20))
+    return fail(GAS_ERR_INVALID, "piece_edges must be in [0, 2^20]");
+  const int G = (int)b->v_off.size() - 1;
+  for (int pass = 0; pass < 2; ++pass) {
+    const int L = pass ? j->ppr_lanes : j->bfs_lanes;
+    const int32_t *ids = pass ? j->ppr_seeds : j->bfs_sources;
+    for (int g = 0; g < G; ++g)
+      for (int l = 0; l < L; ++l) {
+        const int32_t s = ids[(size_t)g * L + l];
+        if (s < -1 || s >= b->v_off[g + 1] - b->v_off[g])
+          return fail(GAS_ERR_INVALID, "%s %d of graph %d lane %d out of range",
+                      pass ? "seed" : "source", s, g, l);
+      }
+  }
+  return GAS_OK;
+}
+
+int default_piece(const gas_batch *b) { return b->tuned_piece > 0 ? b->tuned_piece : 256; }
+
+}  // namespace
+
+extern "C" {
+
+gas_status_t gas_batch_create(gas_batch **out) {
+  if (!out) return fail(GAS_ERR_INVALID, "null out");
+  *out = nullptr;
+  gas_batch *b = new (std::nothrow) gas_batch;
+  if (!b) return fail(GAS_ERR_NOMEM, "batch");
+  gas_status_t st = gas_engine_create(GAS_PROG_BFS, &b->eng);
+  if (st != GAS_OK) {
+    delete b;
+    return st;
+  }
+  *out = b;
+  return GAS_OK;
+}
+
+void gas_batch_destroy(gas_batch *b) {
+  if (!b) return;
+  free_state(b);
+  bfree(b->cnt);
+  bfree(b->prm);
+  bfree(b->edges);
+  bfree(b->resid);
+  if (b->h_cnt) cudaFreeHost(b->h_cnt);
+  gas_engine_destroy(b->eng);
+  delete b;
+}
+
+gas_status_t gas_batch_add_graph(gas_batch *b, int32_t nV, int64_t nE, const int32_t *srcs,
+                                 const int32_t *dsts, int32_t *graph_id) {
+  if (!b || nV < 0 || nE < 0 || (nE > 0 && (!srcs || !dsts)))
+    return fail(GAS_ERR_INVALID, "batch_add_graph: bad arguments");
+  if (b->built) return fail(GAS_ERR_STATE, "batch already built");
+  const int64_t base = b->v_off.back();
+  if (base + nV > INT32_MAX - 1 || b->n_edges + nE > INT32_MAX - 1)
+    return fail(GAS_ERR_TOO_LARGE, "batch exceeds the 32-bit index space");
+  for (int64_t i = 0; i < nE; ++i)
+    if (srcs[i] < 0 || srcs[i] >= nV || dsts[i] < 0 || dsts[i] >= nV)
+      return fail(GAS_ERR_INVALID, "batch_add_graph: edge %lld outside [0, %d)",
+                  (long long)i, nV);
+  try {
+    const size_t n0 = b->src.size();
+    b->src.resize(n0 + nE);
+    b->dst.resize(n0 + nE);
+    for (int64_t i = 0; i < nE; ++i) {
+      b->src[n0 + i] = (int32_t)(srcs[i] + base);
+      b->dst[n0 + i] = (int32_t)(dsts[i] + base);
+    }
+    b->v_off.push_back((int32_t)(base + nV));
+  } catch (...) {
+    return fail(GAS_ERR_NOMEM, "batch edge list");
+  }
+  b->n_edges += nE;
+  if (graph_id) *graph_id = (int32_t)b->v_off.size() - 2;
+  return GAS_OK;
+}
+
+gas_status_t gas_batch_build(gas_batch *b, void *stream) {
+  if (!b) return fail(GAS_ERR_INVALID, "null batch");
+  if (b->built) return fail(GAS_ERR_STATE, "batch already built");
+  if (b->v_off.size() < 2) return fail(GAS_ERR_STATE, "batch has no graphs");
+  const int32_t nV = b->v_off.back();
+  std::vector<int32_t> vd((size_t)std::max(1, nV), -1);
+  GAS_TRY(gas_engine_set_graph(b->eng, nV, vd.data(), (int64_t)b->src.size(), nullptr,
+                               b->src.data(), b->dst.data(), stream));
+  if (!b->cnt) {
+    CUDA_TRY(cudaMalloc(&b->cnt, 2 * sizeof(gas_counters)));
+    CUDA_TRY(cudaMemset(b->cnt, 0, 2 * sizeof(gas_counters)));
+    CUDA_TRY(cudaMallocHost(&b->h_cnt, 2 * sizeof(gas_counters)));
+    CUDA_TRY(cudaMalloc(&b->prm, sizeof(BatchParams)));
+    CUDA_TRY(cudaMalloc(&b->edges, sizeof(unsigned long long)));
+    CUDA_TRY(cudaMalloc(&b->resid, (1 + kMaxLanes) * sizeof(double)));
+  }
+  std::vector<int32_t>().swap(b->src);
+  std::vector<int32_t>().swap(b->dst);
+  b->built = true;
+  return GAS_OK;
+}
+
+int32_t gas_batch_num_graphs(const gas_batch *b) {
+  return b ? (int32_t)b->v_off.size() - 1 : 0;
+}
+
+int32_t gas_batch_num_vertices(const gas_batch *b) { return b ? b->v_off.back() : 0; }
+
+int64_t gas_batch_num_edges(const gas_batch *b) { return b ? b->n_edges : 0; }
+
+int32_t gas_batch_vertex_offset(const gas_batch *b, int32_t g) {
+  return (b && g >= 0 && g < (int32_t)b->v_off.size()) ? b->v_off[g] : -1;
+}
+
+gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *depth_out,
+                           float *rank_out, gas_batch_stats *stats, void *stream) {
+  if (!b || !b->built) return fail(GAS_ERR_STATE, "batch not built");
+  GAS_TRY(check_job(b, job));
+  gas_engine *e = b->eng;
+  cudaStream_t s = S(stream);
+  const int G = gas_batch_num_graphs(b), nV = e->nV;
+  const int LB = job->bfs_lanes, LP = job->ppr_lanes;
+  if (stats) *stats = gas_batch_stats{};
+  RunCtx c;
+  c.b = b;
+  c.bfs_lanes = LB;
+  c.ppr_lanes = LP;
+  grids(b, &c);
+  const int P = job->piece_edges > 0 ? job->piece_edges : default_piece(b);
+  BatchParams prm{};
+  prm.damping = LP ? job->damping : 0.85;
+  prm.tol = LP ? job->tol : 1.0;
+  prm.bfs_max_iter = job->max_bfs_levels > 0 ? job->max_bfs_levels : nV + 2;
+  prm.ppr_max_iter = job->max_ppr_iterations > 0 ? job->max_ppr_iterations : 1000;
+  prm.n_sources = G * LB;
+  std::vector<int32_t> sg;
+  if (LB) {
+    GAS_TRY(ensure_bfs(b, LB, G * LB));
+    sg.resize((size_t)G * LB);
+    for (int g = 0; g < G; ++g)
+      for (int l = 0; l < LB; ++l) {
+        const int32_t v = job->bfs_sources[(size_t)g * LB + l];
+        sg[(size_t)g * LB + l] = v < 0 ? -1 : v + b->v_off[g];
+      }
+  }
+  std::vector<uint32_t> mask;
+  if (LP) {
+    GAS_TRY(ensure_ppr(b, LP, P, c.grid_pieces, c.grid_fix));
+    mask.assign((size_t)std::max(1, nV), 0u);
+    for (int g = 0; g < G; ++g)
+      for (int l = 0; l < LP; ++l) {
+        const int32_t v = job->ppr_seeds[(size_t)g * LP + l];
+        if (v >= 0) mask[(size_t)v + b->v_off[g]] |= 1u << l;
+      }
+    c.ppr = ppr_args(b, LP);
+  }
+  Loop loops[2];
+  int which[2];
+  int n = 0;
+  if (LB) { loops[n] = Loop{bfs_prologue, bfs_body}; which[n++] = 0; }
+  if (LP) { loops[n] = Loop{ppr_prologue, ppr_body}; which[n++] = 1; }
+  const bool direct = gas::host_loop_requested();
+  if (!direct && (!b->graph || b->g_bfs_lanes != LB || b->g_ppr_lanes != LP ||
+                  b->g_piece != (LP ? P : -1))) {
+    drop_graph(b);
+    GAS_TRY(build_chain(&c, loops, n, &b->graph));
+    b->g_bfs_lanes = LB;
+    b->g_ppr_lanes = LP;
+    b->g_piece = LP ? P : -1;
+  }
+  CUDA_TRY(cudaMemcpyAsync(b->prm, &prm, sizeof(prm), cudaMemcpyHostToDevice, s));
+  if (LB) CUDA_TRY(cudaMemcpyAsync(b->srcs, sg.data(), sg.size() * 4, cudaMemcpyHostToDevice, s));
+  if (LP)
+    CUDA_TRY(cudaMemcpyAsync(b->seed_mask, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice,
+                             s));
+  if (direct) {
+    GAS_TRY(run_direct(&c, loops, which, n, s));
+  } else {
+    CUDA_TRY(cudaGraphLaunch(b->graph, s));
+  }
+  CUDA_TRY(cudaMemcpyAsync(b->h_cnt, b->cnt, 2 * sizeof(gas_counters), cudaMemcpyDeviceToHost, s));
+  unsigned long long edges = 0;
+  double resid[1 + kMaxLanes] = {};
+  if (LB) CUDA_TRY(cudaMemcpyAsync(&edges, b->edges, sizeof(edges), cudaMemcpyDeviceToHost, s));
+  if (LP) CUDA_TRY(cudaMemcpyAsync(resid, b->resid, sizeof(resid), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  const gas_counters cb = b->h_cnt[0], cp = b->h_cnt[1];
+  if (depth_out && LB)
+    CUDA_TRY(cudaMemcpyAsync(depth_out, b->depth, (size_t)nV * LB * 4, cudaMemcpyDefault, s));
+  if (rank_out && LP)
+    CUDA_TRY(cudaMemcpyAsync(rank_out, b->rank[cp.iteration & 1], (size_t)nV * LP * 4,
+                             cudaMemcpyDefault, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (stats) {
+    stats->bfs_iterations = LB ? cb.iteration : 0;
+    stats->bfs_edges = (int64_t)edges;
+    stats->ppr_iterations = LP ? cp.iteration : 0;
+    stats->ppr_residual = resid[0];
+    stats->piece_edges = LP ? P : 0;
+    // BFS: prologue 6 kernels, 6 per level; PPR: prologue 3, 3 per iteration
+    stats->kernel_launches = (LB ? 6 + 6 * cb.iteration : 0) + (LP ? 3 + 3 * cp.iteration : 0);
+    stats->graph_launches = direct ? 0 : 1;
+    for (int l = 0; l < LP; ++l) stats->ppr_lane_residual[l] = resid[1 + l];
+  }
+  if (LB && cb.error) {
+    CUDA_TRY(cudaMemset(&b->cnt[0].error, 0, sizeof(int32_t)));
+    return fail(cb.error == GAS_ERR_ITER_CAP ? GAS_ERR_ITER_CAP : GAS_ERR_DEVICE,
+                "batch bfs: device error %d after %d levels", cb.error, cb.iteration);
+  }
+  if (LP && cp.error) {
+    CUDA_TRY(cudaMemset(&b->cnt[1].error, 0, sizeof(int32_t)));
+    return fail(cp.error == GAS_ERR_ITER_CAP ? GAS_ERR_ITER_CAP : GAS_ERR_DEVICE,
+                "batch ppr: residual %.3e after %d iterations", resid[0], cp.iteration);
+  }
+  return GAS_OK;
+}
+
+gas_status_t gas_batch_tune(gas_batch *b, int32_t ppr_lanes, double damping, int32_t trials,
+                            int32_t *piece_edges_out, float *ms_per_iter_out, void *stream) {
+  if (!b || !b->built) return fail(GAS_ERR_STATE, "batch not built");
+  if (ppr_lanes < 1 || ppr_lanes > kMaxLanes || !(damping > 0.0 && damping < 1.0))
+    return fail(GAS_ERR_INVALID, "batch_tune: bad arguments");
+  if (trials <= 0) trials = 3;
+  gas_engine *e = b->eng;
+  cudaStream_t s = S(stream);
+  RunCtx c;
+  c.b = b;
+  c.bfs_lanes = 0;
+  c.ppr_lanes = ppr_lanes;
+  grids(b, &c);
+  BatchParams prm{};
+  prm.damping = damping;
+  prm.tol = 0.0;
+  prm.ppr_max_iter = INT_MAX;
+  CUDA_TRY(cudaMemcpyAsync(b->prm, &prm, sizeof(prm), cudaMemcpyHostToDevice, s));
+  const int cands[] = {64, 128, 256, 512, 1024, 2048};
+  int best = 0;
+  float best_ms = 0.f;
+  cudaEvent_t ev[2];
+  CUDA_TRY(cudaEventCreate(&ev[0]));
+  CUDA_TRY(cudaEventCreate(&ev[1]));
+  gas_status_t st = GAS_OK;
+  for (int P : cands) {
+    st = ensure_ppr(b, ppr_lanes, P, c.grid_pieces, c.grid_fix);
+    if (st != GAS_OK) break;
+    c.ppr = ppr_args(b, ppr_lanes);
+    // a seed in lane 0 of vertex 0 makes the timed iterations do real work
+    const uint32_t one = 1u;
+    if (cudaMemsetAsync(b->seed_mask, 0, (size_t)std::max(1, e->nV) * 4, s) != cudaSuccess ||
+        cudaMemcpyAsync(b->seed_mask, &one, 4, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      st = fail(GAS_ERR_CUDA, "batch_tune: seed upload");
+      break;
+    }
+    st = ppr_prologue(&c, s, 0, 0);
+    if (st == GAS_OK) st = ppr_body(&c, s, 0, 0);  // warm-up
+    if (st != GAS_OK) break;
+    cudaEventRecord(ev[0], s);
+    for (int t = 0; t < trials && st == GAS_OK; ++t) st = ppr_body(&c, s, 0, 0);
+    cudaEventRecord(ev[1], s);
+    if (cudaEventSynchronize(ev[1]) != cudaSuccess) {
+      st = fail(GAS_ERR_CUDA, "batch_tune: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    ms /= (float)trials;
+    if (!best || ms < best_ms) {
+      best = P;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (st != GAS_OK) return st;
+  b->tuned_piece = best;
+  drop_graph(b);
+  if (piece_edges_out) *piece_edges_out = best;
+  if (ms_per_iter_out) *ms_per_iter_out = best_ms;
+  return GAS_OK;
+}
+
+}  // extern "C"

@@ -462,7 +462,7 @@ void free_graph(gas_engine *e) {
   dfree(e->tpart); dfree(e->dpart);
   dfree(e->ppart); dfree(e->cpart); dfree(e->cnt);
   for (int i = 0; i < 2; ++i) { dfree(e->pr_rank[i]); dfree(e->pr_contrib[i]); }
-  dfree(e->pr_inv_deg); dfree(e->pr_l1);
+  dfree(e->pr_seed); dfree(e->pr_l1);
   dfree(e->q_ids); dfree(e->q_vals); dfree(e->q_end); dfree(e->q_delta); dfree(e->snap);
   dfree(e->qpart); dfree(e->cbits); dfree(e->mbits);
   dfree(e->ne_vid); dfree(e->ne_end); dfree(e->zero_vid);

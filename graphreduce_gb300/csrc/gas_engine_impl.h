@@ -64,7 +64,7 @@ struct gas_engine {
   // precision PageRank buffers (lazily allocated)
   float *pr_rank[2] = {nullptr, nullptr};
   float *pr_contrib[2] = {nullptr, nullptr};
-  float *pr_inv_deg = nullptr;
+  int32_t *pr_seed = nullptr;  // personalization seed of the run (-1: none)
   double *pr_l1 = nullptr;
   int32_t pr_l1_cap = 0;
   double pr_damping = 0.0;

@@ -5,6 +5,8 @@
 #include <parallel/algorithm>
 
 #include <algorithm>
+#include <cctype>
+#include <climits>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -422,6 +424,168 @@ gas_status_t gas_gr_read(const char *path, gas_edge_list **out) {
   }
   *out = el;
   return GAS_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Text formats: MatrixMarket coordinate and GraphLab / SNAP edge lists.
+// ---------------------------------------------------------------------------
+namespace {
+
+enum Sym { kSymNone, kSymSym, kSymSkew, kSymHerm };
+
+bool blank_line(const char *p) {
+  for (; *p; ++p)
+    if (!isspace((unsigned char)*p)) return false;
+  return true;
+}
+
+// The line loop shared by both formats (loadGraph_common semantics).
+gas_status_t read_lines(FILE *f, const char *path, char comment, bool skip_size_line,
+                        bool one_based, Sym sym, bool values, gas_edge_list *el) {
+  char buf[1024];
+  int64_t line = 0;
+  int64_t max_v = 0;
+  bool size_line = skip_size_line;
+  while (fgets(buf, sizeof buf, f)) {
+    ++line;
+    if (buf[0] == 0 || buf[0] == comment || blank_line(buf)) continue;
+    if (size_line) {
+      size_line = false;
+      continue;
+    }
+    long long a, b;
+    int used = 0;
+    if (sscanf(buf, "%lld%lld%n", &a, &b, &used) != 2)
+      return gas::fail(GAS_ERR_IO, "%s:%lld: cannot parse src/dst", path, (long long)line);
+    if (one_based) {
+      --a;
+      --b;
+    }
+    if (a < 0 || b < 0 || a >= INT32_MAX || b >= INT32_MAX)
+      return gas::fail(GAS_ERR_IO, "%s:%lld: vertex id out of range", path, (long long)line);
+    float val = 0.f;
+    if (values && sscanf(buf + used, "%f", &val) != 1)
+      return gas::fail(GAS_ERR_IO, "%s:%lld: missing edge value", path, (long long)line);
+    if (a == b) {
+      if (values) continue;  // dropped before the largest id is updated
+    } else {
+      el->src.push_back((int32_t)a);
+      el->dst.push_back((int32_t)b);
+      if (sym != kSymNone) {
+        el->src.push_back((int32_t)b);
+        el->dst.push_back((int32_t)a);
+      }
+      if (values) {
+        el->w.push_back((int32_t)val);
+        if (sym == kSymSym) el->w.push_back((int32_t)val);
+        if (sym == kSymSkew) el->w.push_back((int32_t)(-val));
+      }
+    }
+    max_v = std::max<int64_t>(max_v, std::max(a, b));
+  }
+  if (ferror(f)) return gas::fail(GAS_ERR_IO, "%s: read error", path);
+  el->nV = (int32_t)(max_v + 1);
+  el->has_w = values;
+  return GAS_OK;
+}
+
+gas_status_t read_text(const char *path, bool mtx, gas_edge_list **out) {
+  if (!path || !out) return gas::fail(GAS_ERR_INVALID, "null argument");
+  FILE *f = fopen(path, "r");
+  if (!f) return gas::fail(GAS_ERR_IO, "cannot open %s", path);
+  Sym sym = kSymNone;
+  bool values = false;
+  if (mtx) {
+    char hdr[1024];
+    char t[5][64] = {};
+    if (!fgets(hdr, sizeof hdr, f) ||
+        sscanf(hdr, "%63s %63s %63s %63s %63s", t[0], t[1], t[2], t[3], t[4]) != 5) {
+      fclose(f);
+      return gas::fail(GAS_ERR_IO, "%s: bad MatrixMarket header", path);
+    }
+    if (strcmp(t[1], "matrix") != 0 || strcmp(t[2], "coordinate") != 0) {
+      fclose(f);
+      return gas::fail(GAS_ERR_IO, "%s: only 'matrix coordinate' files are read", path);
+    }
+    if (strcmp(t[3], "complex") == 0) {
+      fclose(f);
+      return gas::fail(GAS_ERR_UNSUPPORTED, "%s: complex edge values", path);
+    }
+    values = strcmp(t[3], "pattern") != 0;
+    if (strcmp(t[4], "general") == 0) sym = kSymNone;
+    else if (strcmp(t[4], "symmetric") == 0) sym = kSymSym;
+    else if (strcmp(t[4], "skew-symmetric") == 0) sym = kSymSkew;
+    else if (strcmp(t[4], "hermitian") == 0) sym = kSymHerm;
+    else {
+      fclose(f);
+      return gas::fail(GAS_ERR_IO, "%s: unrecognised symmetry '%s'", path, t[4]);
+    }
+    if (sym == kSymHerm && values) {
+      fclose(f);
+      return gas::fail(GAS_ERR_UNSUPPORTED, "%s: hermitian files with values", path);
+    }
+  }
+  gas_edge_list *el = new (std::nothrow) gas_edge_list;
+  if (!el) {
+    fclose(f);
+    return gas::fail(GAS_ERR_NOMEM, "text graph");
+  }
+  gas_status_t st;
+  try {
+    st = read_lines(f, path, mtx ? '%' : '#', mtx, mtx, sym, values, el);
+  } catch (...) {
+    st = gas::fail(GAS_ERR_NOMEM, "%s: edge list", path);
+  }
+  fclose(f);
+  if (st != GAS_OK) {
+    delete el;
+    return st;
+  }
+  *out = el;
+  return GAS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gas_status_t gas_mtx_read(const char *path, gas_edge_list **out) {
+  return read_text(path, true, out);
+}
+
+gas_status_t gas_snap_read(const char *path, gas_edge_list **out) {
+  return read_text(path, false, out);
+}
+
+gas_status_t gas_mtx_write(const char *path, const gas_edge_list *el) {
+  if (!path || !el) return gas::fail(GAS_ERR_INVALID, "mtx_write: null argument");
+  FILE *f = fopen(path, "w");
+  if (!f) return gas::fail(GAS_ERR_IO, "cannot open %s for writing", path);
+  const size_t nE = el->src.size();
+  bool ok = fprintf(f, "%%%%MatrixMarket matrix coordinate Integer general\n") > 0;
+  ok = ok && fprintf(f, "%d %d %zu\n", el->nV, el->nV, nE) > 0;
+  for (size_t i = 0; ok && i < nE; ++i) {
+    if (el->has_w)
+      ok = fprintf(f, "%d %d %d\n", el->src[i] + 1, el->dst[i] + 1, el->w[i]) > 0;
+    else
+      ok = fprintf(f, "%d %d\n", el->src[i] + 1, el->dst[i] + 1) > 0;
+  }
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) return gas::fail(GAS_ERR_IO, "short write to %s", path);
+  return GAS_OK;
+}
+
+gas_status_t gas_graph_read(const char *path, gas_edge_list **out) {
+  if (!path || !out) return gas::fail(GAS_ERR_INVALID, "null argument");
+  const char *dot = strrchr(path, '.');
+  if (dot && strcmp(dot, ".gz") == 0)
+    return gas::fail(GAS_ERR_UNSUPPORTED, "%s: gzip input is not read; decompress it", path);
+  if (dot && strncmp(dot, ".edge", 5) == 0) return gas_snap_read(path, out);
+  if (dot && strncmp(dot, ".mtx", 4) == 0) return gas_mtx_read(path, out);
+  if (dot && strncmp(dot, ".gr", 3) == 0) return gas_gr_read(path, out);
+  return gas::fail(GAS_ERR_UNSUPPORTED, "%s: unrecognised file extension", path);
 }
 
 }  // extern "C"

@@ -322,14 +322,49 @@ __global__ void k_warm_init(const int32_t *csr_off, const int32_t *csc_off, int 
   }
 }
 
+// Per-block FP64 sums of init over all vertices and over vertices without
+// out-edges (fixed order inside a block).
+__global__ void __launch_bounds__(256)
+    k_warm_mass(const int32_t *csr_off, const float *init, int nV, double *part) {
+  __shared__ double s_all[256], s_dang[256];
+  double all = 0.0, dang = 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    const double r = init[v];
+    all += r;
+    if (csr_off[v + 1] == csr_off[v]) dang += r;
+  }
+  s_all[threadIdx.x] = all;
+  s_dang[threadIdx.x] = dang;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s_all[threadIdx.x] += s_all[threadIdx.x + o];
+      s_dang[threadIdx.x] += s_dang[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s_all[0];
+    part[2 * blockIdx.x + 1] = s_dang[0];
+  }
+}
+
+__global__ void k_warm_scale(float *init, int nV, float scale) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x)
+    init[v] = __fmul_rn(init[v], scale);
+}
+
 }  // namespace
 
 extern "C" gas_status_t gas_engine_pagerank_warm_start(gas_engine *e, const gas_mlp *m,
-                                                       float *init, void *stream) {
+                                                       double damping, float *init,
+                                                       void *stream) {
   if (!e || !m || !init) return gas::fail(GAS_ERR_INVALID, "null argument");
   if (!e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
   if (m->n_in != GAS_WARM_FEATURES || m->n_out != 1)
     return gas::fail(GAS_ERR_INVALID, "warm-start model must be %d -> 1", GAS_WARM_FEATURES);
+  if (!(damping > 0.0 && damping < 1.0))
+    return gas::fail(GAS_ERR_INVALID, "damping must be in (0,1)");
   const int nV = e->nV;
   if (nV == 0) return GAS_OK;
   std::vector<float> x((size_t)kWarmGrid * kWarmGrid * GAS_WARM_FEATURES);
@@ -338,12 +373,16 @@ extern "C" gas_status_t gas_engine_pagerank_warm_start(gas_engine *e, const gas_
       gasfeat::warm_features(0.5f * i, 0.5f * o, nV, e->nE,
                              &x[((size_t)i * kWarmGrid + o) * GAS_WARM_FEATURES]);
   float *dx = nullptr, *dy = nullptr, *dinit = nullptr;
+  double *dpart = nullptr;
+  const int mass_blocks = 2 * e->num_sms;
+  std::vector<double> part(2 * (size_t)mass_blocks);
   cudaPointerAttributes attr;
   const bool on_device = cudaPointerGetAttributes(&attr, init) == cudaSuccess &&
                          attr.type == cudaMemoryTypeDevice;
   cudaError_t ce = cudaMalloc(&dx, x.size() * 4);
   if (ce == cudaSuccess) ce = cudaMalloc(&dy, (size_t)kWarmGrid * kWarmGrid * 4);
   if (ce == cudaSuccess && !on_device) ce = cudaMalloc(&dinit, (size_t)nV * 4);
+  if (ce == cudaSuccess) ce = cudaMalloc(&dpart, part.size() * sizeof(double));
   if (ce == cudaSuccess)
     ce = cudaMemcpyAsync(dx, x.data(), x.size() * 4, cudaMemcpyHostToDevice, S(stream));
   gas_status_t st = GAS_OK;
@@ -352,6 +391,32 @@ extern "C" gas_status_t gas_engine_pagerank_warm_start(gas_engine *e, const gas_
     float *out = on_device ? init : dinit;
     k_warm_init<<<8 * e->num_sms, 256, 0, S(stream)>>>(e->csr_off, e->csc_off, nV, dy, out);
     ce = cudaGetLastError();
+    // Mass correction: PageRank without dangling redistribution has total
+    // mass m* = (1-d) / (1 - d (1 - delta)) at its fixed point, delta being
+    // the share of the mass on vertices without out-edges; the error along
+    // the fixed point itself decays only at rate d, so the start is scaled
+    // to m* (delta estimated from the prediction).
+    if (ce == cudaSuccess) {
+      k_warm_mass<<<mass_blocks, 256, 0, S(stream)>>>(e->csr_off, out, nV, dpart);
+      ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(part.data(), dpart, part.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost, S(stream));
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(stream));
+    if (ce == cudaSuccess) {
+      double all = 0.0, dang = 0.0;
+      for (int b = 0; b < mass_blocks; ++b) {
+        all += part[2 * b];
+        dang += part[2 * b + 1];
+      }
+      const double delta = all > 0.0 ? dang / all : 0.0;
+      const double mstar = (1.0 - damping) / (1.0 - damping * (1.0 - delta));
+      if (all > 0.0) {
+        k_warm_scale<<<8 * e->num_sms, 256, 0, S(stream)>>>(out, nV, (float)(mstar / all));
+        ce = cudaGetLastError();
+      }
+    }
     if (ce == cudaSuccess && !on_device)
       ce = cudaMemcpyAsync(init, dinit, (size_t)nV * 4, cudaMemcpyDeviceToHost, S(stream));
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(stream));
@@ -359,6 +424,7 @@ extern "C" gas_status_t gas_engine_pagerank_warm_start(gas_engine *e, const gas_
   cudaFree(dx);
   cudaFree(dy);
   cudaFree(dinit);
+  cudaFree(dpart);
   if (st != GAS_OK) return st;
   if (ce != cudaSuccess)
     return gas::fail(GAS_ERR_CUDA, "warm start: %s", cudaGetErrorString(ce));

@@ -257,8 +257,11 @@ struct PrPol {
   const float *rank_old;
   float *rank_new;
   float *contrib_new;
-  float base;
+  float base;       // (1-d)/N, every vertex (seed < 0)
+  float base_seed;  // (1-d), the seed only (personalized)
   float damping;
+  const int32_t *seed_p;
+  int32_t seed;
   double l1;
   __device__ Val zero() const { return PrVal{0.0f, 0.0f}; }
   __device__ __forceinline__ Val reduce(const Val &a, const Val &b) const {
@@ -269,7 +272,8 @@ struct PrPol {
   }
   __device__ __forceinline__ void emit(int, int v, const Val &g) {
     const float sum = __fadd_rn(g.s, g.c);
-    const float r = __fadd_rn(base, __fmul_rn(damping, sum));
+    const float b = seed < 0 ? base : (v == seed ? base_seed : 0.0f);
+    const float r = __fadd_rn(b, __fmul_rn(damping, sum));
     const int deg = __ldg(csr_off + v + 1) - __ldg(csr_off + v);
     rank_new[v] = r;
     contrib_new[v] = deg ? __fdiv_rn(r, (float)deg) : 0.0f;
@@ -289,6 +293,7 @@ __device__ __forceinline__ void pr_bind(PrPol &pol, const PrBufs &b,
   pol.rank_old = b.rank[p];
   pol.rank_new = b.rank[p ^ 1];
   pol.contrib_new = b.contrib[p ^ 1];
+  pol.seed = *pol.seed_p;
   pol.l1 = 0.0;
 }
 
@@ -361,13 +366,14 @@ __global__ void __launch_bounds__(kNT)
   }
 }
 
-// Initial ranks: 1/N, or the caller's vector already copied into rank.
+// Initial ranks: 1/N, e_seed (seed >= 0), or the caller's vector already
+// copied into rank.
 __global__ void k_pr_init(float *rank, float *contrib, const int32_t *csr_off,
-                          int n, float r0, int have_init) {
+                          int n, float r0, int have_init, int seed) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += gridDim.x * blockDim.x) {
     const int deg = csr_off[v + 1] - csr_off[v];
-    const float r = have_init ? rank[v] : r0;
+    const float r = have_init ? rank[v] : seed < 0 ? r0 : (v == seed ? 1.0f : 0.0f);
     rank[v] = r;
     contrib[v] = deg ? __fdiv_rn(r, (float)deg) : 0.0f;
   }
@@ -417,9 +423,11 @@ extern "C" gas_status_t gas_engine_pagerank_precision(
                                             ranks, stats, stream);
 }
 
-extern "C" gas_status_t gas_engine_pagerank_precision_from(
-    gas_engine *e, double damping, double tol, int32_t max_iterations,
-    const float *init, float *ranks, gas_run_stats *stats, void *stream) {
+namespace {
+
+gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max_iterations,
+                          const float *init, int32_t seed, float *ranks, gas_run_stats *stats,
+                          void *stream) {
   if (!e || !e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
   if (!(damping > 0.0 && damping < 1.0) || !(tol > 0.0))
     return gas::fail(GAS_ERR_INVALID, "damping must be in (0,1), tol > 0");
@@ -427,10 +435,12 @@ extern "C" gas_status_t gas_engine_pagerank_precision_from(
   if (stats) *stats = gas_run_stats{};
   const int nV = e->nV;
   if (nV == 0) return GAS_OK;
+  if (seed >= nV) return gas::fail(GAS_ERR_INVALID, "seed %d outside [0, %d)", seed, nV);
   for (int i = 0; i < 2; ++i) {
     if (!e->pr_rank[i]) CUDA_TRY(cudaMalloc(&e->pr_rank[i], (size_t)nV * 4));
     if (!e->pr_contrib[i]) CUDA_TRY(cudaMalloc(&e->pr_contrib[i], (size_t)nV * 4));
   }
+  if (!e->pr_seed) CUDA_TRY(cudaMalloc(&e->pr_seed, sizeof(int32_t)));
   PrCtx c;
   int per_sm = 0;
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pr_slab, kNT, 0));
@@ -450,7 +460,10 @@ extern "C" gas_status_t gas_engine_pagerank_precision_from(
   c.pol.csc_src = e->csc_src;
   c.pol.csr_off = e->csr_off;
   c.pol.base = (float)((1.0 - damping) / (double)nV);
+  c.pol.base_seed = (float)(1.0 - damping);
   c.pol.damping = (float)damping;
+  c.pol.seed_p = e->pr_seed;
+  c.pol.seed = -1;
   c.pol.l1 = 0.0;
   c.bufs.rank[0] = e->pr_rank[0];
   c.bufs.rank[1] = e->pr_rank[1];
@@ -471,12 +484,15 @@ extern "C" gas_status_t gas_engine_pagerank_precision_from(
   }
   CUDA_TRY(cudaMemcpyAsync(c.residual + 1, &tol, sizeof(double),
                            cudaMemcpyHostToDevice, S(stream)));
+  CUDA_TRY(cudaMemcpyAsync(e->pr_seed, &seed, sizeof(int32_t), cudaMemcpyHostToDevice,
+                           S(stream)));
   gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, S(stream)>>>(c.src, e->slab_dpart);
   if (init)
     CUDA_TRY(cudaMemcpyAsync(e->pr_rank[0], init, (size_t)nV * 4, cudaMemcpyDefault,
                              S(stream)));
   k_pr_init<<<gas::engine_grid(nV, kNT, 8 * e->num_sms), kNT, 0, S(stream)>>>(
-      e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV), init ? 1 : 0);
+      e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV), init ? 1 : 0,
+      seed);
   k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
   cudaError_t ce = cudaGetLastError();
   if (host_loop) {
@@ -510,4 +526,20 @@ extern "C" gas_status_t gas_engine_pagerank_precision_from(
     return gas::fail(GAS_ERR_ITER_CAP, "pagerank: residual %.3e after %d iterations",
                      resid, cnt.iteration);
   return GAS_OK;
+}
+
+}  // namespace
+
+extern "C" gas_status_t gas_engine_pagerank_precision_from(
+    gas_engine *e, double damping, double tol, int32_t max_iterations,
+    const float *init, float *ranks, gas_run_stats *stats, void *stream) {
+  return pagerank_run(e, damping, tol, max_iterations, init, -1, ranks, stats, stream);
+}
+
+extern "C" gas_status_t gas_engine_ppr_precision(gas_engine *e, int32_t seed, double damping,
+                                                 double tol, int32_t max_iterations,
+                                                 float *ranks, gas_run_stats *stats,
+                                                 void *stream) {
+  if (seed < 0) return gas::fail(GAS_ERR_INVALID, "ppr: seed must be >= 0");
+  return pagerank_run(e, damping, tol, max_iterations, nullptr, seed, ranks, stats, stream);
 }

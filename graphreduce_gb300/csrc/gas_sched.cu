@@ -586,7 +586,8 @@ __global__ void k_fast_finish(gas_counters *cnt) {
 struct FastCtx {
   int nW;
   int n_qblocks;
-  int slab_grid;  // resident CTAs of the slab kernels
+  int slab_grid;  // resident CTAs of the pull slab kernel
+  int push_grid;  // resident CTAs of the push kernel
   bool seeded;  // iteration 0 from the full range via the finite-value seed
 };
 
@@ -665,6 +666,7 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
       &e->cnt->n_scatter_edges, e->slab_qpart);
   k_push_partition<<<2 * e->num_sms, 256, 0, cs>>>(qsrc, e->slab_qpart, e->cnt);
   const int grid = c.slab_grid;  // resident CTAs only (persistent warps)
+  const int pgrid = c.push_grid;
   const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
   const gasdev::SlabSource dsrc = dense_csc(e);
   int32_t *cf = (int32_t *)e->slab_first, *cc = (int32_t *)e->slab_carry;
@@ -682,11 +684,11 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   }
   if (e->prog == GAS_PROG_BFS) {
     BfsPushPol pol{e->csr_dst, (int32_t *)e->vd, e->cbits, 0};
-    k_bfs_push<<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
+    k_bfs_push<<<pgrid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
   } else if (e->prog == GAS_PROG_SSSP) {
     PushPol<true> pol{e->csr_dst, (const int32_t *)e->csr_ed, e->q_vals,
                       (int32_t *)e->vd, e->cbits, zero_cap};
-    k_push<PushPol<true>><<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
+    k_push<PushPol<true>><<<pgrid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
     PullPol<true> pp{e->csc_src, (const int32_t *)e->csc_ed, e->snap, (int32_t *)e->vd,
                      e->cbits, zero_cap};
     k_pull<PullPol<true>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->slab_fix,
@@ -696,7 +698,7 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   } else {
     PushPol<false> pol{e->csr_dst, nullptr, e->q_vals, (int32_t *)e->vd, e->cbits,
                        zero_cap};
-    k_push<PushPol<false>><<<grid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
+    k_push<PushPol<false>><<<pgrid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
     PullPol<false> pp{e->csc_src, nullptr, e->snap, (int32_t *)e->vd, e->cbits, zero_cap};
     k_pull<PullPol<false>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->slab_fix,
                                                  e->slab_fix_n, e->cnt);
@@ -828,6 +830,14 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<PullPol<true>>, kNT, 0);
     ctx.slab_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);
+    per_sm = 0;
+    if (e->prog == GAS_PROG_BFS)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_push, kNT, 0);
+    else if (e->prog == GAS_PROG_SSSP)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_push<PushPol<true>>, kNT, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_push<PushPol<false>>, kNT, 0);
+    ctx.push_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);
   }
   ctx.seeded = e->prog != GAS_PROG_BFS && e->active_full && !e->counts_dirty &&
                e->n_active == e->nV;

@@ -188,9 +188,13 @@ class GASEngineGPU:
         L.call("gas_engine_set_schedule_model", self._h, None if mlp is None else mlp.handle)
         self._sched_model = mlp
 
-    def pagerank_warm_start(self, mlp, out: np.ndarray | None = None) -> np.ndarray:
+    def pagerank_warm_start(self, mlp, damping: float = 0.85,
+                            out: np.ndarray | None = None) -> np.ndarray:
+        """Initial PageRank vector proposed by the warm-start head, scaled to
+        the fixed point's mass for this damping."""
         init = out if out is not None else np.zeros(self.nVertices, np.float32)
-        L.call("gas_engine_pagerank_warm_start", self._h, mlp.handle, init.ctypes.data, None)
+        L.call("gas_engine_pagerank_warm_start", self._h, mlp.handle, damping,
+               init.ctypes.data, None)
         return init
 
     def pagerank_precision_from(self, init: np.ndarray | None, damping: float = 0.85,
@@ -202,6 +206,21 @@ class GASEngineGPU:
         L.call("gas_engine_pagerank_precision_from", self._h, damping, tol, max_iterations,
                None if ip is None else ip.ctypes.data, ranks.ctypes.data, C.byref(st),
                _stream_ptr(stream))
+        return ranks, st
+
+    def ppr_precision(self, seed: int, damping: float = 0.85, tol: float = 1e-6,
+                      max_iterations: int = 1000, out=None, stream=None):
+        """Personalized PageRank of one seed -> (ranks, RunStats).  out: a
+        float32 numpy array, a device pointer (int), or None for a new host
+        array; ranks is None when out is a device pointer."""
+        st = RunStats()
+        if isinstance(out, int):
+            ranks, ptr = None, out
+        else:
+            ranks = out if out is not None else np.zeros(self.nVertices, np.float32)
+            ptr = ranks.ctypes.data
+        L.call("gas_engine_ppr_precision", self._h, int(seed), damping, tol, max_iterations,
+               ptr, C.byref(st), _stream_ptr(stream))
         return ranks, st
 
     def counters(self) -> L.Counters:

@@ -117,6 +117,21 @@ class EdgeList:
         L.call("gas_gr_read", str(path).encode(), C.byref(h))
         return cls._from_handle(h.value)
 
+    def write_mtx(self, path: str) -> None:
+        """MatrixMarket coordinate, 1-based, "Integer general" (writeGraph_mtx)."""
+        h = self._handle()
+        try:
+            L.call("gas_mtx_write", str(path).encode(), h)
+        finally:
+            L.load().gas_edge_list_destroy(h)
+
+    @classmethod
+    def read(cls, path: str) -> "EdgeList":
+        """.mtx, .edge (GraphLab / SNAP) or .gr, chosen by extension (loadGraph)."""
+        h = C.c_void_p()
+        L.call("gas_graph_read", str(path).encode(), C.byref(h))
+        return cls._from_handle(h.value)
+
     # -- degrees / CSR --------------------------------------------------------
     def out_degree(self) -> np.ndarray:
         return np.bincount(self.src, minlength=self.nV).astype(np.int32)

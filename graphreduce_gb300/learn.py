@@ -225,8 +225,12 @@ def warm_samples(el: EdgeList, per_graph: int, seed: int):
     ranks, _ = eng.pagerank_precision(0.85, 1e-6)
     eng.close()
     X = warm_features(el)
-    t = np.log(np.maximum(ranks.astype(np.float64) * el.nV, 1e-30)).astype(np.float32)
-    idx = np.random.default_rng(seed).choice(el.nV, size=min(per_graph, el.nV), replace=False)
+    r = np.maximum(ranks.astype(np.float64), 1e-30)
+    t = np.log(r * el.nV).astype(np.float32)
+    # vertices drawn in proportion to their rank: the squared log error is
+    # then weighted like the vertex's share of the L1 error of the start
+    p = r / r.sum()
+    idx = np.random.default_rng(seed).choice(el.nV, size=per_graph, replace=True, p=p)
     return X[idx], t[idx]
 
 

@@ -116,6 +116,24 @@ gas_status_t gas_edge_list_sample_sources(const gas_edge_list *el, int32_t k,
 gas_status_t gas_gr_write(const char *path, const gas_edge_list *el);
 gas_status_t gas_gr_read(const char *path, gas_edge_list **out);
 
+/* Text formats of graphio.cpp (plain files; gzip is not read):
+ * gas_mtx_read replaces loadGraph_MatrixMarket (graphio.cpp:190-270):
+ * "%%MatrixMarket matrix coordinate <type> <symmetry>" header, '%' comments,
+ * the size line ignored, 1-based ids, self loops dropped, "symmetric" /
+ * "skew-symmetric" (and value-less "hermitian") add the reverse edge right
+ * after each edge (skew: negated value), values parsed as float and
+ * truncated to int, "pattern" gives no edge data, "complex" is rejected,
+ * nV = largest id + 1 (a self loop of a valued file does not count, as in
+ * loadGraph_common, graphio.cpp:69-176).  gas_snap_read replaces
+ * loadGraph_GraphLabSnap (graphio.cpp:178-188): '#' comments, 0-based
+ * "src dst" lines, self loops dropped, no edge data.  gas_mtx_write replaces
+ * writeGraph_mtx (graphio.cpp:416-437).  gas_graph_read dispatches on the
+ * extension like loadGraph (graphio.cpp:441-473): .edge, .mtx, .gr. */
+gas_status_t gas_mtx_read(const char *path, gas_edge_list **out);
+gas_status_t gas_snap_read(const char *path, gas_edge_list **out);
+gas_status_t gas_mtx_write(const char *path, const gas_edge_list *el);
+gas_status_t gas_graph_read(const char *path, gas_edge_list **out);
+
 /* edgeListToCSR (util.cuh:80-111): offsets[nV+1], out[nE] = vals in key
  * order, perm[nE] = original edge index (out / perm may be NULL).  Edges of
  * one key keep their edge-list order (stable). */
@@ -361,11 +379,14 @@ gas_status_t gas_engine_set_schedule_model(gas_engine *e, const gas_mlp *m);
  * 1 + degree, over 32) plus graph-level log sizes go through a one-output
  * model (n_in = GAS_WARM_FEATURES) predicting log(N * rank); init receives
  * exp(prediction) / N for every vertex (device or host pointer, nV
- * floats).  The model is evaluated on a 64 x 64 grid of log-degrees and
- * interpolated bilinearly per vertex. */
+ * floats), scaled so that its total equals the mass the fixed point of
+ * PageRank with this damping has: (1-d) / (1 - d (1 - delta)), delta the
+ * predicted share on vertices without out-edges.  The model is evaluated on
+ * a 64 x 64 grid of log-degrees and interpolated bilinearly per vertex. */
 #define GAS_WARM_FEATURES 4
 gas_status_t gas_engine_pagerank_warm_start(gas_engine *e, const gas_mlp *m,
-                                            float *init, void *stream);
+                                            double damping, float *init,
+                                            void *stream);
 
 /* gas_engine_pagerank_precision from a given initial vector (nV floats,
  * device or host; NULL = the uniform 1/N). */
@@ -375,6 +396,79 @@ gas_status_t gas_engine_pagerank_precision_from(gas_engine *e, double damping,
                                                 const float *init, float *ranks,
                                                 gas_run_stats *stats,
                                                 void *stream);
+
+/* Personalized PageRank of one seed on the engine's graph (no reference
+ * counterpart): r = (1-d) e_seed + d A^T D^-1 r from r0 = e_seed, with the
+ * kernels, compensation and residual of gas_engine_pagerank_precision.
+ * The single-instance form of the batched PPR below. */
+gas_status_t gas_engine_ppr_precision(gas_engine *e, int32_t seed, double damping,
+                                      double tol, int32_t max_iterations,
+                                      float *ranks, gas_run_stats *stats,
+                                      void *stream);
+
+/* ======================================================================= */
+/* Batched engine: many graphs, many BFS sources and personalized-PageRank */
+/* seeds per graph, one CUDA-graph launch.  No reference counterpart.      */
+/* ======================================================================= */
+
+/* The graphs are stored as one disjoint union graph; graph g's vertex v is
+ * union vertex gas_batch_vertex_offset(b, g) + v.  Results are laid out
+ * [union vertex][lane]. */
+typedef struct gas_batch gas_batch;
+gas_status_t gas_batch_create(gas_batch **out);
+void gas_batch_destroy(gas_batch *b);
+/* Appends a graph (edge list over [0, nV)); graph_id may be NULL. */
+gas_status_t gas_batch_add_graph(gas_batch *b, int32_t nV, int64_t nE,
+                                 const int32_t *srcs, const int32_t *dsts,
+                                 int32_t *graph_id);
+/* Uploads the union graph (CSR + CSC); no graphs can be added afterwards. */
+gas_status_t gas_batch_build(gas_batch *b, void *stream);
+int32_t gas_batch_num_graphs(const gas_batch *b);
+int32_t gas_batch_num_vertices(const gas_batch *b);
+int64_t gas_batch_num_edges(const gas_batch *b);
+int32_t gas_batch_vertex_offset(const gas_batch *b, int32_t graph);
+
+#define GAS_BATCH_MAX_LANES 32
+
+typedef struct {
+  int32_t bfs_lanes;           /* 0..32 BFS sources per graph (0: no BFS)   */
+  const int32_t *bfs_sources;  /* [graphs][bfs_lanes] local ids, -1 unused  */
+  int32_t ppr_lanes;           /* 0..32 PPR seeds per graph (0: no PPR)     */
+  const int32_t *ppr_seeds;    /* [graphs][ppr_lanes] local ids, -1 unused  */
+  double damping;              /* PPR damping d in (0, 1)                   */
+  double tol;                  /* PPR: stop when every lane's L1 step <= tol */
+  int32_t max_bfs_levels;      /* <= 0: union V + 2                         */
+  int32_t max_ppr_iterations;  /* <= 0: 1000                                */
+  int32_t piece_edges;         /* PPR edges per piece; 0: tuned or 256      */
+} gas_batch_job;
+
+typedef struct {
+  int32_t bfs_iterations;      /* push levels run                           */
+  int32_t ppr_iterations;
+  int64_t bfs_edges;           /* out-edges pushed (lanes of a vertex share) */
+  double ppr_residual;         /* largest per-lane L1 step at the end       */
+  int32_t piece_edges;         /* piece size the PPR loop used              */
+  int32_t kernel_launches;
+  int32_t graph_launches;      /* 1, or 0 with GAS_HOST_LOOP=1              */
+  int32_t pad;
+  double ppr_lane_residual[GAS_BATCH_MAX_LANES];
+} gas_batch_stats;
+
+/* Runs the job's BFS lanes, then its PPR lanes, as one CUDA-graph launch.
+ * depth_out [V][bfs_lanes] int32 (-1 unreached) and rank_out
+ * [V][ppr_lanes] float may be host or device pointers, or NULL.  A lane
+ * whose source or seed is -1 stays unreached / all zero.  GAS_ERR_ITER_CAP
+ * when a cap ends a loop (results are then those of the last step). */
+gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job,
+                           int32_t *depth_out, float *rank_out,
+                           gas_batch_stats *stats, void *stream);
+
+/* Autotuner: times a few PPR iterations for each piece size in
+ * {64, 128, ..., 2048} with ppr_lanes lanes and keeps the fastest for runs
+ * whose job says piece_edges = 0. */
+gas_status_t gas_batch_tune(gas_batch *b, int32_t ppr_lanes, double damping,
+                            int32_t trials, int32_t *piece_edges_out,
+                            float *ms_per_iter_out, void *stream);
 
 /* ======================================================================= */
 /* Views used by include/gpugas.h to launch its Program-typed kernels.     */

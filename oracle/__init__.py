@@ -41,9 +41,12 @@ def _oracle():
             lib.orc_pagerank.argtypes = [c_i32, c_i64, c_vp, c_vp, c_vp]
             lib.orc_pagerank_fp64.argtypes = [c_i32, c_i64, c_vp, c_vp, c_dbl, c_dbl, c_i64,
                                               c_vp, c_vp]
+            lib.orc_ppr_fp64.argtypes = [c_i32, c_i64, c_vp, c_vp, c_i32, c_dbl, c_dbl, c_i64,
+                                         c_vp, c_vp]
             lib.orc_pagerank_fp64_step.argtypes = [c_i32, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp]
             lib.orc_pagerank_fp64_step.restype = c_dbl
-            for f in ("orc_bfs", "orc_sssp", "orc_cc", "orc_pagerank", "orc_pagerank_fp64"):
+            for f in ("orc_bfs", "orc_sssp", "orc_cc", "orc_pagerank", "orc_pagerank_fp64",
+                      "orc_ppr_fp64"):
                 getattr(lib, f).restype = c_i64
             _orc = lib
     return _orc
@@ -102,6 +105,16 @@ def pagerank_fp64(nV, src, dst, damping=0.85, tol=1e-6, max_iter=1000):
     return out, _check(it, "pagerank_fp64"), l1.value
 
 
+def ppr_fp64(nV, src, dst, seed, damping=0.85, tol=1e-12, max_iter=10000):
+    """Personalized PageRank of one seed in FP64 -> (rank float64[nV], iterations, L1)."""
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(nV, np.float64)
+    l1 = C.c_double()
+    it = _oracle().orc_ppr_fp64(nV, s.shape[0], s.ctypes.data, d.ctypes.data, int(seed),
+                                damping, tol, max_iter, out.ctypes.data, C.byref(l1))
+    return out, _check(it, "ppr_fp64"), l1.value
+
+
 def pagerank_fp64_step(nV, src, dst, r, damping=0.85):
     """One FP64 precision-form step from ranks r -> (r', L1)."""
     s, d = _i32(src), _i32(dst)
@@ -146,6 +159,7 @@ def _reference():
                 getattr(lib, f).restype = c_i64
             lib.ref_edge_list_to_csr.argtypes = [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]
             lib.ref_write_gr.argtypes = [C.c_char_p, c_i32, c_i32, c_vp, c_vp, c_vp]
+            lib.ref_write_mtx.argtypes = [C.c_char_p, c_i32, c_i32, c_vp, c_vp, c_vp]
             lib.ref_load_graph.argtypes = [C.c_char_p, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]
             lib.ref_load_graph.restype = c_i64
             _ref = lib
@@ -198,6 +212,13 @@ def ref_write_gr(path, nV, offsets, dsts, weights):
     w = None if weights is None else _i32(weights)
     _reference().ref_write_gr(str(path).encode(), nV, d.shape[0], o.ctypes.data, d.ctypes.data,
                               None if w is None else w.ctypes.data)
+
+
+def ref_write_mtx(path, nV, srcs, dsts, weights):
+    s, d = _i32(srcs), _i32(dsts)
+    w = None if weights is None else _i32(weights)
+    _reference().ref_write_mtx(str(path).encode(), nV, s.shape[0], s.ctypes.data, d.ctypes.data,
+                               None if w is None else w.ctypes.data)
 
 
 def ref_load_graph(path, cap, want_weights=True):

@@ -344,6 +344,56 @@ ORC_EXPORT int64_t orc_pagerank_fp64(int32_t nV, int64_t nE,
   return it;
 }
 
+/* Personalized PageRank in FP64 (no reference counterpart; the formula of
+ * orc_pagerank_fp64 with the teleport term on one seed): r0 = e_seed;
+ * r'_v = (1-d) [v == seed] + d * sum_{u->v} r_u / outdeg(u); stop after the
+ * first iteration whose L1 residual <= tol, or fail with -3 after max_iter
+ * iterations.  Returns iterations; *l1_out = last residual. */
+ORC_EXPORT int64_t orc_ppr_fp64(int32_t nV, int64_t nE, const int32_t *srcs,
+                                const int32_t *dsts, int32_t seed, double damping,
+                                double tol, int64_t max_iter, double *rank,
+                                double *l1_out)
+{
+  orc_graph g;
+  double *r, *rn, *contrib;
+  int64_t it = 0;
+  int32_t v;
+  double l1 = 0.0;
+  if (nV <= 0 || seed < 0 || seed >= nV) return -1;
+  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
+  r = (double *)malloc(sizeof(double) * (size_t)nV);
+  rn = (double *)malloc(sizeof(double) * (size_t)nV);
+  contrib = (double *)malloc(sizeof(double) * (size_t)nV);
+  if (!r || !rn || !contrib) {
+    free(r); free(rn); free(contrib); graph_free(&g); return -2;
+  }
+  for (v = 0; v < nV; ++v) r[v] = v == seed ? 1.0 : 0.0;
+  for (;;) {
+    if (it >= max_iter) { it = -3; break; }
+    for (v = 0; v < nV; ++v) {
+      int64_t od = g.csr_off[v + 1] - g.csr_off[v];
+      contrib[v] = od ? r[v] / (double)od : 0.0;
+    }
+    l1 = 0.0;
+    for (v = 0; v < nV; ++v) {
+      double s = 0.0;
+      int64_t ie;
+      for (ie = g.csc_off[v]; ie < g.csc_off[v + 1]; ++ie)
+        s += contrib[g.csc_src[ie]];
+      rn[v] = (v == seed ? 1.0 - damping : 0.0) + damping * s;
+      l1 += fabs(rn[v] - r[v]);
+    }
+    { double *t = r; r = rn; rn = t; }
+    ++it;
+    if (l1 <= tol) break;
+  }
+  for (v = 0; v < nV; ++v) rank[v] = r[v];
+  if (l1_out) *l1_out = l1;
+  free(r); free(rn); free(contrib);
+  graph_free(&g);
+  return it;
+}
+
 /* One precision-form step on given ranks (FP64), for per-iteration checks
  * of a GPU step: out[v] = (1-d)/N + d * sum r_u/outdeg(u); returns L1. */
 ORC_EXPORT double orc_pagerank_fp64_step(int32_t nV, int64_t nE,

@@ -191,6 +191,13 @@ int ref_write_gr(const char *fname, int nV, int nE, const int *offsets,
   return 0;
 }
 
+// graphio.cpp:416-437
+int ref_write_mtx(const char *fname, int nV, int nE, const int *srcs, const int *dsts,
+                  const int *weights) {
+  writeGraph_mtx(fname, nV, nE, srcs, dsts, weights);
+  return 0;
+}
+
 // graphio.cpp:274-362 through loadGraph (graphio.cpp:441-473).  Returns the
 // edge count; srcs/dsts/weights must hold cap entries.
 int64_t ref_load_graph(const char *fname, int want_weights, int cap, int *nV,

@@ -77,6 +77,85 @@ def run_case(name, nV, s, d, w, source, directed_pr=True):
           f"sssp_it={rec.get('sssp_iters')} cc_it={rec.get('cc_iters')} pr_it={rec.get('pr_iters')}")
 
 
+# Small hand-made text graphs covering the loader's rules: comments, blank
+# lines, the ignored size line, 1-based ids, fractional and negative values
+# (truncated), self loops with and without values, and every symmetry.
+TEXT_GRAPHS = {
+    "general_real.mtx": (
+        "%%MatrixMarket matrix coordinate real general\n"
+        "% a comment\n"
+        "%another one\n"
+        "5 5 7\n"
+        "1 2 2.7\n"
+        "2 3 -1.5\n"
+        "3 1 10\n"
+        "\n"
+        "4 5 0.25\n"
+        "6 6 3.0\n"
+        "5 4 64\n"
+        "2 2 1.0\n"),
+    "symmetric_int.mtx": (
+        "%%MatrixMarket matrix coordinate integer symmetric\n"
+        "4 4 4\n"
+        "2 1 5\n"
+        "3 1 7\n"
+        "   \n"
+        "4 3 9\n"
+        "4 4 2\n"),
+    "skew.mtx": (
+        "%%MatrixMarket matrix coordinate real skew-symmetric\n"
+        "3 3 2\n"
+        "2 1 1.9\n"
+        "3 2 -4.2\n"),
+    "pattern_general.mtx": (
+        "%%MatrixMarket matrix coordinate pattern general\n"
+        "% self loop on the largest id still counts here\n"
+        "7 7 4\n"
+        "1 2\n"
+        "2 3\n"
+        "3 1\n"
+        "7 7\n"),
+    "pattern_sym.mtx": (
+        "%%MatrixMarket matrix coordinate pattern symmetric\n"
+        "5 5 3\n"
+        "1 5\n"
+        "2 5\n"
+        "3 4\n"),
+    "snap.edge": (
+        "# GraphLab / SNAP edge list\n"
+        "# FromNodeId ToNodeId\n"
+        "0 1\n"
+        "1 2\n"
+        "2 0\n"
+        "3 3\n"
+        "\n"
+        "2 4\n"),
+}
+
+
+def text_formats():
+    d = OUT / "text"
+    d.mkdir(exist_ok=True)
+    res = {}
+    for name, body in TEXT_GRAPHS.items():
+        p = d / name
+        p.write_text(body)
+        valued = name.endswith(".mtx") and "pattern" not in name
+        nV, s, t, w = oracle.ref_load_graph(p, 64, want_weights=valued)
+        key = name.replace(".", "_")
+        res[f"{key}_nV"] = np.int64(nV)
+        res[f"{key}_src"], res[f"{key}_dst"] = s, t
+        if valued:
+            res[f"{key}_w"] = w
+    np.savez_compressed(OUT / "text_formats.npz", **res)
+    # a MatrixMarket file written by the reference's writeGraph_mtx
+    el = EdgeList.rmat(6, 4, seed=31).with_uniform_weights(1, 64, 3)
+    oracle.ref_write_mtx(OUT / "text" / "ref_written.mtx", el.nV, el.src, el.dst, el.weights)
+    np.savez_compressed(OUT / "ref_written_mtx.npz", nV=np.int64(el.nV), src=el.src,
+                        dst=el.dst, w=el.weights)
+    print("text/*.mtx, text/*.edge, text_formats.npz, ref_written_mtx.npz")
+
+
 def main():
     build()
     build_oracle(with_reference=True)
@@ -106,6 +185,7 @@ def main():
     off_csr, dst_csr, perm_csr = edge_list_to_csr(el.nV, s, d)
     oracle.ref_write_gr(OUT / "ref_written.gr", el.nV, off_csr, dst_csr, w[perm_csr])
     print("csr_ties.npz, ref_written.gr")
+    text_formats()
 
 
 if __name__ == "__main__":
