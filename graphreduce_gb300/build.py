@@ -28,7 +28,7 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fPIC,-fopenmp,-fvisibility=default",
     f"-I{INCLUDE}", f"-I{CSRC}",
 ]
-SOURCES = ["gas_engine.cu", "gas_runs.cu", "gas_sched.cu", "gas_noalloc.cu", "gas_batch.cu",
+SOURCES = ["gas_engine.cu", "gas_runs.cu", "gas_sched.cu", "gas_noalloc.cu", "gas_batch.cu", "gas_build.cu",
            "gas_learn.cu", "gas_host_graph.cpp"]
 
 

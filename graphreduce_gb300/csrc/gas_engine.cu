@@ -462,7 +462,11 @@ void free_graph(gas_engine *e) {
   dfree(e->tpart); dfree(e->dpart);
   dfree(e->ppart); dfree(e->cpart); dfree(e->cnt);
   for (int i = 0; i < 2; ++i) { dfree(e->pr_rank[i]); dfree(e->pr_contrib[i]); }
-  dfree(e->pr_seed); dfree(e->pr_l1);
+  dfree(e->pr_seed); dfree(e->pr_l1); dfree(e->csr_to_csc);
+  e->h_csr_perm.clear();
+  e->h_csr_to_csc.clear();
+  e->host_ed = nullptr;
+  e->edges_dirty = false;
   dfree(e->q_ids); dfree(e->q_vals); dfree(e->q_end); dfree(e->q_delta); dfree(e->snap);
   dfree(e->qpart); dfree(e->cbits); dfree(e->mbits);
   dfree(e->ne_vid); dfree(e->ne_end); dfree(e->zero_vid);
@@ -741,34 +745,40 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   e->nE = (int32_t)nE;
   e->host_vd = vertex_data;
 
-  // CSC / CSR on the host (stable counting sort), edge data permuted into
-  // both orders (gpugas.h:1358-1378).
-  std::vector<int32_t> csc_src, csc_perm, csr_off, csr_dst, csr_perm;
-  try {
-    e->h_csc_off.assign((size_t)nV + 1, 0);
-    csc_src.resize(nE); csc_perm.resize(nE);
-    csr_off.resize((size_t)nV + 1); csr_dst.resize(nE); csr_perm.resize(nE);
-  } catch (...) {
-    return gas::fail(GAS_ERR_NOMEM, "set_graph: host arrays");
-  }
-  GAS_TRY(gas::build_csr_host(nV, nE, dsts, srcs, e->h_csc_off.data(),
-                              csc_src.data(), csc_perm.data()));
-  GAS_TRY(gas::build_csr_host(nV, nE, srcs, dsts, csr_off.data(),
-                              csr_dst.data(), csr_perm.data()));
+  // CSC / CSR (stable by edge-list order), edge data permuted into both
+  // orders (gpugas.h:1358-1378): on the device for large graphs, by a
+  // counting sort on the host otherwise (GAS_GRAPH_BUILD=host|device forces
+  // one).
   const size_t eb = e->ebytes;
-  std::vector<uint8_t> ed_csc, ed_csr;
   const bool have_ed = edge_data && eb > 0;
-  if (have_ed) {
+  const bool want_perms = have_ed && e->prog == GAS_PROG_USER;
+  const bool dev_build = gas::device_build_for(nE);
+  std::vector<int32_t> csc_src, csc_perm, csr_off, csr_dst, csr_perm;
+  std::vector<uint8_t> ed_csc, ed_csr;
+  if (!dev_build) {
     try {
-      ed_csc.resize((size_t)nE * eb);
-      ed_csr.resize((size_t)nE * eb);
+      e->h_csc_off.assign((size_t)nV + 1, 0);
+      csc_src.resize(nE); csc_perm.resize(nE);
+      csr_off.resize((size_t)nV + 1); csr_dst.resize(nE); csr_perm.resize(nE);
     } catch (...) {
-      return gas::fail(GAS_ERR_NOMEM, "set_graph: edge data");
+      return gas::fail(GAS_ERR_NOMEM, "set_graph: host arrays");
     }
-    const uint8_t *src = (const uint8_t *)edge_data;
-    for (int64_t i = 0; i < nE; ++i) {
-      memcpy(&ed_csc[i * eb], src + (size_t)csc_perm[i] * eb, eb);
-      memcpy(&ed_csr[i * eb], src + (size_t)csr_perm[i] * eb, eb);
+    GAS_TRY(gas::build_csr_host(nV, nE, dsts, srcs, e->h_csc_off.data(),
+                                csc_src.data(), csc_perm.data()));
+    GAS_TRY(gas::build_csr_host(nV, nE, srcs, dsts, csr_off.data(),
+                                csr_dst.data(), csr_perm.data()));
+    if (have_ed) {
+      try {
+        ed_csc.resize((size_t)nE * eb);
+        ed_csr.resize((size_t)nE * eb);
+      } catch (...) {
+        return gas::fail(GAS_ERR_NOMEM, "set_graph: edge data");
+      }
+      const uint8_t *src = (const uint8_t *)edge_data;
+      for (int64_t i = 0; i < nE; ++i) {
+        memcpy(&ed_csc[i * eb], src + (size_t)csc_perm[i] * eb, eb);
+        memcpy(&ed_csr[i * eb], src + (size_t)csr_perm[i] * eb, eb);
+      }
     }
   }
 
@@ -803,6 +813,25 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   e->n_cblocks = (int32_t)std::max<size_t>(1, (nW + kCompactBlock - 1) / kCompactBlock);
   GAS_TRY(dalloc(&e->cpart, 2 * (size_t)e->n_cblocks));
   GAS_TRY(dalloc(&e->cnt, 1));
+
+  if (dev_build)
+    GAS_TRY(gas::build_graph_device(e, srcs, dsts, have_ed ? edge_data : nullptr,
+                                    want_perms ? &csc_perm : nullptr,
+                                    want_perms ? &csr_perm : nullptr, stream));
+  if (want_perms) {
+    // a user program may scatter into its edge data: keep what maps the
+    // two device copies onto each other and back to the caller's order
+    try {
+      std::vector<int32_t> inv((size_t)nE);
+      for (int64_t i = 0; i < nE; ++i) inv[csc_perm[i]] = (int32_t)i;
+      e->h_csr_to_csc.resize((size_t)nE);
+      for (int64_t j = 0; j < nE; ++j) e->h_csr_to_csc[j] = inv[csr_perm[j]];
+      e->h_csr_perm = csr_perm;
+    } catch (...) {
+      return gas::fail(GAS_ERR_NOMEM, "set_graph: edge maps");
+    }
+    e->host_ed = const_cast<void *>(edge_data);
+  }
 
   // rows of the CSC with / without in-edges, for the dense slab passes
   std::vector<int32_t> ne_vid, ne_end, zero_vid;
@@ -844,9 +873,13 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   if (!zero_vid.empty())
     CUDA_TRY(cudaMemcpyAsync(e->zero_vid, zero_vid.data(), zero_vid.size() * 4,
                              cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(e->csc_off, e->h_csc_off.data(), (V + 1) * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(e->csr_off, csr_off.data(), (V + 1) * 4, cudaMemcpyHostToDevice, st));
-  if (E) {
+  if (!dev_build) {
+    CUDA_TRY(cudaMemcpyAsync(e->csc_off, e->h_csc_off.data(), (V + 1) * 4,
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(e->csr_off, csr_off.data(), (V + 1) * 4, cudaMemcpyHostToDevice,
+                             st));
+  }
+  if (E && !dev_build) {
     CUDA_TRY(cudaMemcpyAsync(e->csc_src, csc_src.data(), E * 4, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(e->csr_dst, csr_dst.data(), E * 4, cudaMemcpyHostToDevice, st));
     if (have_ed) {
@@ -959,6 +992,66 @@ gas_status_t gas_engine_get_results(gas_engine *e, void *stream) {
     CUDA_TRY(cudaMemcpyAsync(e->host_vd, e->vd, (size_t)e->nV * e->vbytes,
                              cudaMemcpyDeviceToHost, S(stream)));
   CUDA_TRY(cudaStreamSynchronize(S(stream)));
+  if (e->edges_dirty && e->host_ed && e->nE) {
+    // edge data a user scatter changed, back into the caller's order
+    const size_t eb = e->ebytes;
+    std::vector<uint8_t> tmp;
+    try {
+      tmp.resize((size_t)e->nE * eb);
+    } catch (...) {
+      return gas::fail(GAS_ERR_NOMEM, "get_results: edge data");
+    }
+    CUDA_TRY(cudaMemcpyAsync(tmp.data(), e->csr_ed, tmp.size(), cudaMemcpyDeviceToHost,
+                             S(stream)));
+    CUDA_TRY(cudaStreamSynchronize(S(stream)));
+    uint8_t *dst = static_cast<uint8_t *>(e->host_ed);
+    for (int32_t j = 0; j < e->nE; ++j)
+      memcpy(dst + (size_t)e->h_csr_perm[j] * eb, &tmp[(size_t)j * eb], eb);
+    e->edges_dirty = false;
+  }
+  return GAS_OK;
+}
+
+gas_status_t gas_engine_download_graph(gas_engine *e, int32_t *csc_off, int32_t *csc_src,
+                                       int32_t *csr_off, int32_t *csr_dst, void *csc_ed,
+                                       void *csr_ed, void *stream) {
+  if (!e || !e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
+  const size_t V1 = (size_t)e->nV + 1, E = (size_t)e->nE, eb = e->ebytes;
+  cudaStream_t st = S(stream);
+  const struct {
+    void *dst;
+    const void *src;
+    size_t bytes;
+  } cp[] = {{csc_off, e->csc_off, V1 * 4}, {csc_src, e->csc_src, E * 4},
+            {csr_off, e->csr_off, V1 * 4}, {csr_dst, e->csr_dst, E * 4},
+            {csc_ed, e->csc_ed, E * eb}, {csr_ed, e->csr_ed, E * eb}};
+  for (const auto &c : cp)
+    if (c.dst && c.src && c.bytes)
+      CUDA_TRY(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return GAS_OK;
+}
+
+gas_status_t gas_engine_prepare_scatter(gas_engine *e, const int32_t **csr_to_csc,
+                                        void *stream) {
+  if (!e || !e->has_graph) return gas::fail(GAS_ERR_STATE, "scatter before set_graph");
+  if (e->prog != GAS_PROG_USER)
+    return gas::fail(GAS_ERR_UNSUPPORTED, "prepare_scatter is for user programs");
+  if (e->counts_dirty) GAS_TRY(sync_counts(e, stream));
+  if (e->slots_pending) {
+    k_commit<<<grid_for(e->n_active, kNT, 8 * e->num_sms), kNT, 0, S(stream)>>>(
+        e->act, e->cnt, (const uint8_t *)e->slot, (uint8_t *)e->vd, (int)e->vbytes);
+    CUDA_TRY(cudaGetLastError());
+    e->slots_pending = false;
+  }
+  const bool have = e->csr_ed && e->nE > 0 && !e->h_csr_to_csc.empty();
+  if (have && !e->csr_to_csc) {
+    GAS_TRY(dalloc(&e->csr_to_csc, (size_t)e->nE));
+    CUDA_TRY(cudaMemcpyAsync(e->csr_to_csc, e->h_csr_to_csc.data(), (size_t)e->nE * 4,
+                             cudaMemcpyHostToDevice, S(stream)));
+  }
+  if (csr_to_csc) *csr_to_csc = have ? e->csr_to_csc : nullptr;
+  e->edges_dirty = e->edges_dirty || have;
   return GAS_OK;
 }
 

@@ -37,6 +37,11 @@ struct gas_engine {
   size_t vbytes = 0, gbytes = 0, ebytes = 0;
   int32_t nV = 0, nE = 0;
   void *host_vd = nullptr;
+  void *host_ed = nullptr;             // caller's edge data (user engines)
+  std::vector<int32_t> h_csr_perm;     // edge-list index of each CSR edge
+  std::vector<int32_t> h_csr_to_csc;   // CSC position of each CSR edge
+  int32_t *csr_to_csc = nullptr;       // device copy (on first scatter)
+  bool edges_dirty = false;            // a user scatter may have changed edge data
   std::vector<int32_t> h_csc_off;  // for host-side counts in setActive
 
   // device graph
@@ -127,6 +132,15 @@ gas_status_t engine_commit(gas_engine *e, void *stream);
 // host copy of the counters (synchronises the stream)
 gas_status_t engine_sync_counts(gas_engine *e, void *stream);
 int engine_grid(int64_t work_items, int per_block, int cap);
+// CSR/CSC on the device (gas_build.cu): fills csc_off/csc_src/csr_off/
+// csr_dst (+ csc_ed/csr_ed), which must be allocated, and h_csc_off; the
+// permutations (edge-list index per CSC / CSR position) when asked for.
+gas_status_t build_graph_device(gas_engine *e, const int32_t *srcs, const int32_t *dsts,
+                                const void *edge_data, std::vector<int32_t> *csc_perm,
+                                std::vector<int32_t> *csr_perm, void *stream);
+// Whether set_graph builds on the device: GAS_GRAPH_BUILD=host|device, else
+// from 1M edges up.
+bool device_build_for(int64_t n_edges);
 // grid of a k_partition launch (fixed while capturing)
 int engine_partition_grid(gas_engine *e, int64_t items, int tile);
 // GAS_HOST_LOOP=1: device loops run as direct launches with one host read

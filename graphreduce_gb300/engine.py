@@ -223,6 +223,22 @@ class GASEngineGPU:
                ptr, C.byref(st), _stream_ptr(stream))
         return ranks, st
 
+    def graph_arrays(self) -> dict:
+        """Host copies of the CSC and CSR the engine built (edge data as int32
+        for the built-in programs)."""
+        nV, nE = self.nVertices, self.nEdges
+        out = {k: np.empty(nV + 1, np.int32) for k in ("csc_off", "csr_off")}
+        out.update({k: np.empty(nE, np.int32) for k in ("csc_src", "csr_dst")})
+        ptr = {k: v.ctypes.data for k, v in out.items()}
+        if self.program == SSSP:
+            out["csc_w"] = np.empty(nE, np.int32)
+            out["csr_w"] = np.empty(nE, np.int32)
+        L.call("gas_engine_download_graph", self._h, ptr["csc_off"], ptr["csc_src"],
+               ptr["csr_off"], ptr["csr_dst"],
+               out["csc_w"].ctypes.data if "csc_w" in out else None,
+               out["csr_w"].ctypes.data if "csr_w" in out else None, None)
+        return out
+
     def counters(self) -> L.Counters:
         c = L.Counters()
         L.call("gas_engine_read_counters", self._h, C.byref(c), None)

@@ -523,6 +523,23 @@ gas_status_t gas_engine_view_get(gas_engine *e, gas_engine_view *view);
  * vertex data in place. */
 gas_status_t gas_engine_note_applied(gas_engine *e, int32_t wrote_slots);
 
+/* Host copies of the engine's CSC and CSR (any pointer may be NULL):
+ * csc_off[nV+1], csc_src[nE], csr_off[nV+1], csr_dst[nE], and the edge data
+ * in CSC and CSR order (nE records each).  Edges of one row keep their
+ * edge-list order (edgeListToCSR / edgeListToCSC, util.cuh:80-121). */
+gas_status_t gas_engine_download_graph(gas_engine *e, int32_t *csc_off, int32_t *csc_src,
+                                       int32_t *csr_off, int32_t *csr_dst, void *csc_ed,
+                                       void *csr_ed, void *stream);
+
+/* Before a user program's scatter kernel (refgas.h:175-196 semantics, which
+ * the reference GPU engine skips, gpugas.h:942): publishes the vertex data
+ * the last apply wrote, marks the edge data as modified on the device (so
+ * that get_results copies it back into the caller's edge array, in edge-list
+ * order) and returns the CSC position of every CSR edge (NULL without edge
+ * data), through which the kernel keeps the two device copies equal. */
+gas_status_t gas_engine_prepare_scatter(gas_engine *e, const int32_t **csr_to_csc,
+                                        void *stream);
+
 /* Host copy of the counters (synchronises the stream). */
 gas_status_t gas_engine_read_counters(gas_engine *e, gas_counters *out,
                                       void *stream);

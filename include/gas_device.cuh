@@ -477,6 +477,50 @@ __global__ void __launch_bounds__(kNT)
   }
 }
 
+// Program::scatter on the GPU (refgas.h:175-196): for every active slot
+// whose apply returned true, every out-edge in CSR order gets
+// scatter(src, dst, edge) with the vertex data apply left.  One warp per
+// active vertex; every edge belongs to one source, so no two threads touch
+// the same edge record.  The CSR copy of the edge data is updated and
+// mirrored into the CSC copy that the next gather reads.  Programs opt in
+// with `static const bool runScatter = true;` (the reference GPU engine
+// never calls scatter, gpugas.h:942, and the reference apps' scatter is
+// empty).
+template <class P, class = void>
+struct RunsScatter { static constexpr bool value = false; };
+template <class P>
+struct RunsScatter<P, decltype((void)P::runScatter, void())> {
+  static constexpr bool value = P::runScatter;
+};
+
+template <class P>
+__global__ void __launch_bounds__(kNT)
+    k_scatter_user(const int32_t *act, const gas_counters *cnt, const uint8_t *ret,
+                   const int32_t *csr_off, const int32_t *csr_dst,
+                   const typename P::VertexData *vd, typename P::EdgeData *csr_ed,
+                   typename P::EdgeData *csc_ed, const int32_t *csr_to_csc) {
+  typedef typename P::EdgeData ED;
+  const int n = cnt->n_active;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n; i += nwarps) {
+    if (!ret[i]) continue;
+    const int sv = act[i];
+    const int e1 = csr_off[sv + 1];
+    for (int pos = csr_off[sv] + lane; pos < e1; pos += 32) {
+      const int dv = csr_dst[pos];
+      if (csr_ed) {
+        ED ed = csr_ed[pos];
+        P::scatter(vd + sv, vd + dv, &ed);
+        csr_ed[pos] = ed;
+        csc_ed[csr_to_csc[pos]] = ed;
+      } else {
+        ED ed{};
+        P::scatter(vd + sv, vd + dv, &ed);
+      }
+    }
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Warp-slab segmented passes (dense CSC pulls, PageRank, frontier pushes).

@@ -119,6 +119,23 @@ class GASEngineGPU {
     GPUGAS_CUDA(cudaGetLastError());
   }
 
+  void launchScatter() {
+    gas_counters c;
+    GPUGAS_CHECK(gas_engine_read_counters(m_engine, &c, 0));
+    if (c.n_active == 0) return;
+    const int32_t *map = 0;
+    GPUGAS_CHECK(gas_engine_prepare_scatter(m_engine, &map, 0));
+    const long long warps = c.n_active;
+    const long long blocks = (warps * 32 + gasdev::kNT - 1) / gasdev::kNT;
+    const int grid = (int)(blocks < 8 * m_view.num_sms ? blocks : 8 * m_view.num_sms);
+    EdgeData *csr_ed = map ? static_cast<EdgeData *>(const_cast<void *>(m_view.csr_ed)) : 0;
+    gasdev::k_scatter_user<Program><<<grid, gasdev::kNT>>>(
+        m_view.active, m_view.counters, m_view.apply_ret, m_view.csr_off, m_view.csr_dst,
+        static_cast<const VertexData *>(m_view.vertex_data), csr_ed,
+        static_cast<EdgeData *>(const_cast<void *>(m_view.csc_ed)), map);
+    GPUGAS_CUDA(cudaGetLastError());
+  }
+
   void flushGather() {
     if (!m_pendingGather) return;
     m_pendingGather = false;
@@ -194,9 +211,12 @@ class GASEngineGPU {
     GPUGAS_CHECK(gas_engine_note_applied(m_engine, 0));
   }
 
-  // gpugas.h:1650-1759
+  // gpugas.h:1650-1759.  Program::scatter runs on the GPU when the program
+  // asks for it with `static const bool runScatter = true;`; otherwise, as
+  // in the reference GPU engine, only the activation happens.
   void scatterActivate(bool haveScatter = true) {
     flushGather();
+    if (haveScatter && gasdev::RunsScatter<Program>::value) launchScatter();
     GPUGAS_CHECK(gas_engine_scatter_activate(m_engine, haveScatter ? 1 : 0, 0));
     m_haveGatherTmp = false;
   }
