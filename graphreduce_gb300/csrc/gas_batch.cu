@@ -148,25 +148,54 @@ __global__ void k_ms_seed(const int32_t *src_global, const BatchParams *prm, int
   }
 }
 
-// The touched-vertex traversal shared by the two compaction passes: thread t
-// of a warp owns word w0 + t of the bitmap; the warp walks its 32 words one
-// at a time, lane l taking vertex 32 * word + l.  Counts this thread's queue
-// entries (vertices with new lanes and out-edges) and their out-edge total.
-__device__ __forceinline__ void ms_counts(uint32_t mine, int w0, const uint32_t *next,
-                                          const uint32_t *visited, const int32_t *csr_off,
-                                          int &q, int &d) {
+// The touched-vertex traversal shared by the two compaction passes: a warp
+// owns 8 words of the touched bitmap (lanes 0..7 load them), lane l takes
+// vertex 32 w + l of each word, and all 8 words' loads are issued before
+// any is used.  For a touched vertex: its new lanes and out-edge range.
+constexpr int kMsWarpWords = 8;
+constexpr int kMsBlockWords = kMsWarpWords * (kNT / 32);  // 64 words
+
+struct MsWarp {
+  uint32_t myword;
+  uint32_t nw[kMsWarpWords];  // new lanes (0: not touched or nothing new)
+  int off[kMsWarpWords];
+  int deg[kMsWarpWords];
+};
+
+__device__ __forceinline__ void ms_load(const uint32_t *tbits, const uint32_t *next,
+                                        const uint32_t *visited, const int32_t *csr_off,
+                                        int nW, int w0, MsWarp &w) {
   const int lane = threadIdx.x & 31;
+  w.myword = (lane < kMsWarpWords && w0 + lane < nW) ? tbits[w0 + lane] : 0u;
+#pragma unroll
+  for (int i = 0; i < kMsWarpWords; ++i) {
+    const uint32_t word = __shfl_sync(0xffffffffu, w.myword, i);
+    w.nw[i] = 0u;
+    w.off[i] = 0;
+    w.deg[i] = 0;
+    if ((word >> lane) & 1u) {
+      const int v = (w0 + i) * 32 + lane;
+      w.nw[i] = next[v] & ~visited[v];
+      w.off[i] = csr_off[v];
+      w.deg[i] = csr_off[v + 1] - w.off[i];
+    }
+  }
+}
+
+// queue entries (vertices with new lanes and out-edges) and their out-edges
+__device__ __forceinline__ void ms_totals(const MsWarp &w, int &q, int &d) {
   q = 0;
   d = 0;
-  for (int i = 0; i < 32; ++i) {
-    const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
-    if (!word || !((word >> lane) & 1u)) continue;
-    const int v = (w0 + i) * 32 + lane;
-    const int deg = csr_off[v + 1] - csr_off[v];
-    if (deg > 0 && (next[v] & ~visited[v])) {
-      ++q;
-      d += deg;
-    }
+#pragma unroll
+  for (int i = 0; i < kMsWarpWords; ++i) {
+    const bool in = w.nw[i] && w.deg[i] > 0;
+    q += in;
+    d += in ? w.deg[i] : 0;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    q += __shfl_xor_sync(0xffffffffu, q, o);
+    d += __shfl_xor_sync(0xffffffffu, d, o);
   }
 }
 
@@ -174,45 +203,53 @@ __device__ __forceinline__ void ms_counts(uint32_t mine, int w0, const uint32_t 
 __global__ void __launch_bounds__(kNT)
     k_ms_count(const uint32_t *tbits, const uint32_t *next, const uint32_t *visited,
                const int32_t *csr_off, int nW, int32_t *part) {
-  const int lane = threadIdx.x & 31;
-  const int w0 = blockIdx.x * kNT + threadIdx.x - lane;
-  const uint32_t mine = (w0 + lane < nW) ? tbits[w0 + lane] : 0u;
-  int q, d, tq, td;
-  ms_counts(mine, w0, next, visited, csr_off, q, d);
-  cta_excl(q, &tq);
-  cta_excl(d, &td);
+  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
+  MsWarp w;
+  ms_load(tbits, next, visited, csr_off, nW, w0, w);
+  int q, d;
+  ms_totals(w, q, d);
+  if (lane == 0) {
+    s_q[warp] = q;
+    s_d[warp] = d;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
+    int tq = 0, td = 0;
+    for (int k = 0; k < kNT / 32; ++k) {
+      tq += s_q[k];
+      td += s_d[k];
+    }
     part[2 * blockIdx.x] = tq;
     part[2 * blockIdx.x + 1] = td;
   }
 }
 
-// Exclusive scan of the block pairs; totals into the counters.
+// Exclusive scan of the block pairs in one pass (thread t folds a run of
+// ceil(nb / kNT) blocks); totals into the counters.
 __global__ void __launch_bounds__(kNT)
     k_ms_spine(int32_t *part, int nb, gas_counters *cnt) {
-  __shared__ int s_c[2];
-  if (threadIdx.x < 2) s_c[threadIdx.x] = 0;
-  __syncthreads();
-  for (int base = 0; base < nb; base += kNT) {
-    const int i = base + threadIdx.x;
-    const int vq = i < nb ? part[2 * i] : 0, vd = i < nb ? part[2 * i + 1] : 0;
-    int tq, td;
-    const int eq = cta_excl(vq, &tq), ed = cta_excl(vd, &td);
-    const int cq = s_c[0], cd = s_c[1];
-    if (i < nb) {
-      part[2 * i] = cq + eq;
-      part[2 * i + 1] = cd + ed;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      s_c[0] = cq + tq;
-      s_c[1] = cd + td;
-    }
-    __syncthreads();
+  const int per = (nb + kNT - 1) / kNT;
+  const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
+  int sq = 0, sd = 0;
+  for (int b = b0; b < b1; ++b) {
+    sq += part[2 * b];
+    sd += part[2 * b + 1];
+  }
+  int tq, td;
+  int pq = cta_excl(sq, &tq);
+  int pd = cta_excl(sd, &td);
+  for (int b = b0; b < b1; ++b) {
+    const int q = part[2 * b], d = part[2 * b + 1];
+    part[2 * b] = pq;
+    part[2 * b + 1] = pd;
+    pq += q;
+    pd += d;
   }
   if (threadIdx.x == 0) {
-    cnt->n_changed = s_c[0];
-    cnt->n_scatter_edges = s_c[1];
+    cnt->n_changed = tq;
+    cnt->n_scatter_edges = td;
   }
 }
 
@@ -223,35 +260,57 @@ __global__ void __launch_bounds__(kNT)
                int nW, const int32_t *part, int L, const gas_counters *cnt, int level_add,
                int32_t *depth, int32_t *q_ids, int32_t *q_mask, int32_t *q_end,
                int32_t *q_delta) {
+  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   const int level = cnt->iteration + level_add;
-  const int lane = threadIdx.x & 31;
-  const int w0 = blockIdx.x * kNT + threadIdx.x - lane;
-  const uint32_t mine = (w0 + lane < nW) ? tbits[w0 + lane] : 0u;
-  int q, d, tq, td;
-  ms_counts(mine, w0, next, visited, csr_off, q, d);
-  int pq = cta_excl(q, &tq) + part[2 * blockIdx.x];
-  int pd = cta_excl(d, &td) + part[2 * blockIdx.x + 1];
-  for (int i = 0; i < 32; ++i) {
-    const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
-    if (!word || !((word >> lane) & 1u)) continue;
-    const int v = (w0 + i) * 32 + lane;
-    const uint32_t nw = next[v] & ~visited[v];
-    next[v] = 0u;
-    if (!nw) continue;
-    visited[v] |= nw;
-    for (uint32_t m = nw; m; m &= m - 1) depth[(size_t)v * L + (__ffs(m) - 1)] = level;
-    const int off = csr_off[v];
-    const int deg = csr_off[v + 1] - off;
-    if (deg > 0) {
-      pd += deg;
-      q_ids[pq] = v;
-      q_mask[pq] = (int32_t)nw;
-      q_end[pq] = pd;
-      q_delta[pq] = off - (pd - deg);
-      ++pq;
-    }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
+  MsWarp w;
+  ms_load(tbits, next, visited, csr_off, nW, w0, w);
+  int q, d;
+  ms_totals(w, q, d);
+  if (lane == 0) {
+    s_q[warp] = q;
+    s_d[warp] = d;
   }
-  if (w0 + lane < nW && mine) tbits[w0 + lane] = 0u;
+  __syncthreads();
+  int bq = part[2 * blockIdx.x], bd = part[2 * blockIdx.x + 1];
+  for (int k = 0; k < warp; ++k) {
+    bq += s_q[k];
+    bd += s_d[k];
+  }
+  if (w.myword) tbits[w0 + lane] = 0u;
+#pragma unroll
+  for (int i = 0; i < kMsWarpWords; ++i) {
+    const int v = (w0 + i) * 32 + lane;
+    const uint32_t word = __shfl_sync(0xffffffffu, w.myword, i);
+    if (!word) continue;  // warp-uniform
+    const bool touched = (word >> lane) & 1u;
+    const uint32_t nw = w.nw[i];
+    if (touched) next[v] = 0u;
+    if (nw) {
+      visited[v] |= nw;
+      for (uint32_t m = nw; m; m &= m - 1) depth[(size_t)v * L + (__ffs(m) - 1)] = level;
+    }
+    const int deg = nw ? w.deg[i] : 0;
+    const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
+    if (!qb) continue;
+    int incl = deg;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (deg > 0) {
+      const int pos = bq + __popc(qb & ((1u << lane) - 1u));
+      const int end = bd + incl;
+      q_ids[pos] = v;
+      q_mask[pos] = (int32_t)nw;
+      q_end[pos] = end;
+      q_delta[pos] = w.off[i] - (end - deg);
+    }
+    bq += __popc(qb);
+    bd += __shfl_sync(0xffffffffu, incl, 31);
+  }
 }
 
 // Loop condition after the prologue (level 0 written, no push run yet).
@@ -287,8 +346,9 @@ struct PprArgs {
   const int32_t *csc_off, *csc_src, *csr_off;
   const int32_t *first_row;  // [n_pieces] first row with an edge in the piece
   int32_t n_pieces, P, E, L, G;
-  const int32_t *fix;        // [n_fix][3] (row, first piece, last piece)
-  int32_t n_fix;
+  const int32_t *fix;        // [n_fix][3] (row, first piece, last piece):
+  int32_t n_fix;             // rows cut by pieces, then rows without
+  int32_t n_split;           // in-edges (first piece -1) from n_split on
   CVal *head, *tail;         // [n_pieces][L] partials of cut rows
   float *rank[2], *contrib[2];
   const uint32_t *seed_mask;
@@ -330,7 +390,10 @@ __device__ __forceinline__ void ppr_finish_row(const PprArgs &a, const PprLane &
   t.contrib_new[k] = deg ? __fdiv_rn(r, (float)deg) : 0.f;
 }
 
-// Edge-order compensated fold of one lane over [e, stop).
+// Edge-order fold of one lane over [e, stop): groups of 8 contributions are
+// summed pairwise in FP32 (relative error <= 3 u of the group's sum, the
+// terms being non-negative), and the group sums are accumulated with two-sum
+// compensation, so the error of a row stays near 3 u of its value.
 __device__ __forceinline__ CVal ppr_fold(const PprArgs &a, const PprLane &t, int e, int stop) {
   CVal acc{0.f, 0.f};
   constexpr int U = 8;
@@ -341,8 +404,9 @@ __device__ __forceinline__ CVal ppr_fold(const PprArgs &a, const PprLane &t, int
     for (int j = 0; j < U; ++j) u[j] = __ldg(a.csc_src + e + j);
 #pragma unroll
     for (int j = 0; j < U; ++j) x[j] = __ldg(t.contrib + (size_t)u[j] * a.L + t.l);
-#pragma unroll
-    for (int j = 0; j < U; ++j) acc = two_sum_add(acc, CVal{x[j], 0.f});
+    const float g = __fadd_rn(__fadd_rn(__fadd_rn(x[0], x[1]), __fadd_rn(x[2], x[3])),
+                              __fadd_rn(__fadd_rn(x[4], x[5]), __fadd_rn(x[6], x[7])));
+    acc = two_sum_add(acc, CVal{g, 0.f});
   }
   for (; e < stop; ++e) {
     const int u = __ldg(a.csc_src + e);
@@ -399,15 +463,19 @@ __global__ void __launch_bounds__(kNT) k_ppr_pieces(PprArgs a, double *l1_part) 
   lane_block_sums(l1, a.G, l1_part + (size_t)blockIdx.x * a.G);
 }
 
-// Rows cut by piece boundaries (partials folded in piece order) and rows
-// without in-edges (first piece -1).
+// Rows cut by piece boundaries (partials folded in piece order), and in the
+// first iteration the rows without in-edges (first piece -1): their rank is
+// (1-d) [seed] from then on, so it is written into both buffers once and
+// those rows are skipped afterwards.
 __global__ void __launch_bounds__(kNT) k_ppr_fix(PprArgs a, double *l1_part) {
   const PprLane t = ppr_lane(a);
   const int per_block = kNT / a.G;
   const int local = threadIdx.x / a.G;
+  const bool first = a.cnt->iteration == 0;
+  const int limit = first ? a.n_fix : a.n_split;
   double l1 = 0.0;
   if (t.on) {
-    for (int i = blockIdx.x * per_block + local; i < a.n_fix; i += gridDim.x * per_block) {
+    for (int i = blockIdx.x * per_block + local; i < limit; i += gridDim.x * per_block) {
       const int v = a.fix[3 * i], ps = a.fix[3 * i + 1], pe = a.fix[3 * i + 2];
       CVal acc{0.f, 0.f};
       if (ps >= 0) {
@@ -415,6 +483,12 @@ __global__ void __launch_bounds__(kNT) k_ppr_fix(PprArgs a, double *l1_part) {
         for (int k = ps + 1; k <= pe; ++k) acc = two_sum_add(acc, a.head[(size_t)k * a.L + t.l]);
       }
       ppr_finish_row(a, t, v, acc, l1);
+      if (ps < 0) {  // first iteration only: the other buffer too (the
+                     // pieces of this iteration have read it already)
+        const size_t k = (size_t)v * a.L + t.l;
+        a.rank[0][k] = t.rank_new[k];
+        a.contrib[0][k] = t.contrib_new[k];
+      }
     }
   }
   lane_block_sums(l1, a.G, l1_part + (size_t)blockIdx.x * a.G);
@@ -495,7 +569,7 @@ struct gas_batch {
   float *rank[2] = {nullptr, nullptr}, *contrib[2] = {nullptr, nullptr};
   uint32_t *seed_mask = nullptr;
   double *l1 = nullptr;
-  int32_t n_pieces = 0, n_fix = 0, piece_edges = 0, ppr_lanes = 0, l1_cap = 0;
+  int32_t n_pieces = 0, n_fix = 0, n_split = 0, piece_edges = 0, ppr_lanes = 0, l1_cap = 0;
   int32_t tuned_piece = 0;
   // cached graph
   cudaGraphExec_t graph = nullptr;
@@ -524,7 +598,7 @@ void free_state(gas_batch *b) {
   bfree(b->first_row); bfree(b->fix); bfree(b->head); bfree(b->tail);
   bfree(b->seed_mask); bfree(b->l1);
   for (int i = 0; i < 2; ++i) { bfree(b->rank[i]); bfree(b->contrib[i]); }
-  b->n_pieces = b->n_fix = b->piece_edges = b->ppr_lanes = b->depth_lanes = 0;
+  b->n_pieces = b->n_fix = b->n_split = b->piece_edges = b->ppr_lanes = b->depth_lanes = 0;
   b->srcs_cap = b->l1_cap = 0;
 }
 
@@ -535,7 +609,9 @@ int lane_group(int L) {
 }
 
 int nwords(const gas_batch *b) { return (b->eng->nV + 31) / 32; }
-int ms_blocks(const gas_batch *b) { return std::max(1, (nwords(b) + kNT - 1) / kNT); }
+int ms_blocks(const gas_batch *b) {
+  return std::max(1, (nwords(b) + kMsBlockWords - 1) / kMsBlockWords);
+}
 
 gas_status_t ensure_bfs(gas_batch *b, int lanes, int n_sources) {
   gas_engine *e = b->eng;
@@ -599,16 +675,18 @@ gas_status_t ensure_ppr(gas_batch *b, int lanes, int P, int grid_pieces, int gri
     while (off[r + 1] <= e0) ++r;  // first row with csc_off[r+1] > e0
     first[k] = r;
   }
-  std::vector<int32_t> fix;
+  std::vector<int32_t> fix, zero;
   for (int32_t v = 0; v < V; ++v) {
     const int32_t lo = off[v], hi = off[v + 1];
     if (lo == hi) {
-      fix.insert(fix.end(), {v, -1, -1});
+      zero.insert(zero.end(), {v, -1, -1});
     } else {
       const int32_t ps = lo / P, pe = (hi - 1) / P;
       if (ps != pe) fix.insert(fix.end(), {v, ps, pe});
     }
   }
+  const int32_t n_split = (int32_t)(fix.size() / 3);
+  fix.insert(fix.end(), zero.begin(), zero.end());
   bfree(b->first_row);
   bfree(b->fix);
   bfree(b->head);
@@ -623,6 +701,7 @@ gas_status_t ensure_ppr(gas_batch *b, int lanes, int P, int grid_pieces, int gri
     CUDA_TRY(cudaMemcpy(b->fix, fix.data(), fix.size() * 4, cudaMemcpyHostToDevice));
   b->n_pieces = n_pieces;
   b->n_fix = (int32_t)(fix.size() / 3);
+  b->n_split = n_split;
   b->piece_edges = P;
   return GAS_OK;
 }
@@ -648,6 +727,7 @@ PprArgs ppr_args(gas_batch *b, int lanes) {
   a.G = lane_group(lanes);
   a.fix = b->fix;
   a.n_fix = b->n_fix;
+  a.n_split = b->n_split;
   a.head = b->head;
   a.tail = b->tail;
   for (int i = 0; i < 2; ++i) {
@@ -825,7 +905,7 @@ void grids(gas_batch *b, RunCtx *c) {
   per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ppr_pieces, kNT, 0);
   c->grid_pieces = e->num_sms * (per_sm > 0 ? per_sm : 1);
-  c->grid_fix = 2 * e->num_sms;
+  c->grid_fix = 8 * e->num_sms;
 }
 
 gas_status_t check_job(const gas_batch *b, const gas_batch_job *j) {

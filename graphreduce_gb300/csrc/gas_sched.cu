@@ -114,12 +114,12 @@ __global__ void k_seed_finite(const int32_t *vd, int nV, int32_t zero_cap,
 // frontier compaction: changed bitmap -> queue of the members with out-edges
 // (id, value at the end of the iteration, end of its out-edge range in the
 // queue's edge space, CSR position offset), membership bitmap + snapshots of
-// all members for the dense pull.  One lane per vertex: each warp takes 32
+// all members for the dense pull.  One lane per vertex: each warp takes 8
 // bitmap words; a word's 32 lanes read their out-degrees coalesced, a ballot
 // gives queue positions, a warp scan gives edge offsets.
 // ---------------------------------------------------------------------------
-constexpr int kQWordsPerWarp = 32;
-constexpr int kQWordsPerBlock = kQWordsPerWarp * (kNT / 32);  // 256 words
+constexpr int kQWordsPerWarp = 8;
+constexpr int kQWordsPerBlock = kQWordsPerWarp * (kNT / 32);  // 64 words
 
 __device__ __forceinline__ int warp_incl_sum_i(int v) {
   const int lane = threadIdx.x & 31;
@@ -131,49 +131,38 @@ __device__ __forceinline__ int warp_incl_sum_i(int v) {
   return v;
 }
 
-// A warp owns 32 bitmap words.  Sparse warps (few set bits) give each lane
-// one word and walk its set bits; dense warps walk the words one at a time
-// with one lane per vertex, so the out-degree loads are coalesced.
-constexpr int kQDenseBits = 96;
-
-struct QLane {
-  uint32_t word;  // this lane's bitmap word
-  bool dense;     // warp-uniform
+// A warp owns 8 bitmap words; lane l takes vertex 32 w + l of each word, so
+// the out-offset loads of a word are coalesced, and the 8 words' loads are
+// issued before any of them is used.
+struct QWarp {
+  int off[kQWordsPerWarp];
+  int deg[kQWordsPerWarp];  // 0 when the bit is clear
+  uint32_t myword;          // lanes 0..7: word w0 + lane
 };
 
-__device__ __forceinline__ QLane q_lane(const uint32_t *cbits, int nW, int w0) {
+__device__ __forceinline__ void q_warp_load(const uint32_t *cbits, const int32_t *csr_off,
+                                            int nW, int w0, QWarp &w) {
   const int lane = threadIdx.x & 31;
-  QLane q;
-  q.word = (w0 + lane < nW) ? cbits[w0 + lane] : 0u;
-  q.dense = __reduce_add_sync(0xffffffffu, (unsigned)__popc(q.word)) > kQDenseBits;
-  return q;
+  w.myword = (lane < kQWordsPerWarp && w0 + lane < nW) ? cbits[w0 + lane] : 0u;
+#pragma unroll
+  for (int i = 0; i < kQWordsPerWarp; ++i) {
+    const uint32_t word = __shfl_sync(0xffffffffu, w.myword, i);
+    w.off[i] = 0;
+    w.deg[i] = 0;
+    if ((word >> lane) & 1u) {
+      const int v = (w0 + i) * 32 + lane;
+      w.off[i] = csr_off[v];
+      w.deg[i] = csr_off[v + 1] - w.off[i];
+    }
+  }
 }
 
-// per-warp (queue entries, out-edges) of its 32 words
-__device__ __forceinline__ void q_warp_counts(const QLane &ql, const int32_t *csr_off,
-                                              int w0, int *cq, int *cd) {
-  const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void q_warp_totals(const QWarp &w, int *cq, int *cd) {
   int q = 0, d = 0;
-  if (ql.dense) {
-    for (int i = 0; i < kQWordsPerWarp; ++i) {
-      const uint32_t word = __shfl_sync(0xffffffffu, ql.word, i);
-      if (!word) continue;
-      const int v = (w0 + i) * 32 + lane;
-      int deg = 0;
-      if ((word >> lane) & 1u) deg = csr_off[v + 1] - csr_off[v];
-      q += deg > 0;
-      d += deg;
-    }
-  } else {
-    uint32_t m = ql.word;
-    while (m) {
-      const int bit = __ffs(m) - 1;
-      m &= m - 1;
-      const int v = (w0 + lane) * 32 + bit;
-      const int deg = csr_off[v + 1] - csr_off[v];
-      q += deg > 0;
-      d += deg;
-    }
+#pragma unroll
+  for (int i = 0; i < kQWordsPerWarp; ++i) {
+    q += w.deg[i] > 0;
+    d += w.deg[i];
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -197,9 +186,10 @@ __global__ void __launch_bounds__(kNT)
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
-  const QLane ql = q_lane(cbits, nW, w0);
+  QWarp w;
+  q_warp_load(cbits, csr_off, nW, w0, w);
   int cq, cd;
-  q_warp_counts(ql, csr_off, w0, &cq, &cd);
+  q_warp_totals(w, &cq, &cd);
   if (lane == 0) {
     s_q[warp] = cq;
     s_d[warp] = cd;
@@ -207,42 +197,40 @@ __global__ void __launch_bounds__(kNT)
   __syncthreads();
   if (threadIdx.x == 0) {
     int tq = 0, td = 0;
-    for (int w = 0; w < kNT / 32; ++w) {
-      tq += s_q[w];
-      td += s_d[w];
+    for (int k = 0; k < kNT / 32; ++k) {
+      tq += s_q[k];
+      td += s_d[k];
     }
     part[2 * blockIdx.x] = tq;
     part[2 * blockIdx.x + 1] = td;
   }
 }
 
+// Exclusive scan of the block pairs in one pass: thread t folds a run of
+// ceil(nb / kNT) consecutive blocks, one CTA scan, then the runs are
+// rewritten as prefixes.
 __global__ void __launch_bounds__(kNT)
     k_q_spine(int32_t *part, int nb, gas_counters *cnt) {
-  __shared__ int s_carry[2];
-  if (threadIdx.x < 2) s_carry[threadIdx.x] = 0;
-  __syncthreads();
-  for (int base = 0; base < nb; base += kNT) {
-    const int i = base + threadIdx.x;
-    const int vc = i < nb ? part[2 * i] : 0;
-    const int vd = i < nb ? part[2 * i + 1] : 0;
-    int tc, td;
-    const int ec = cta_excl_sum(vc, &tc);
-    const int ed = cta_excl_sum(vd, &td);
-    const int cc = s_carry[0], cd = s_carry[1];
-    if (i < nb) {
-      part[2 * i] = cc + ec;
-      part[2 * i + 1] = cd + ed;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      s_carry[0] = cc + tc;
-      s_carry[1] = cd + td;
-    }
-    __syncthreads();
+  const int per = (nb + kNT - 1) / kNT;
+  const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
+  int sq = 0, sd = 0;
+  for (int b = b0; b < b1; ++b) {
+    sq += part[2 * b];
+    sd += part[2 * b + 1];
+  }
+  int tq, td;
+  int pq = cta_excl_sum(sq, &tq);
+  int pd = cta_excl_sum(sd, &td);
+  for (int b = b0; b < b1; ++b) {
+    const int q = part[2 * b], d = part[2 * b + 1];
+    part[2 * b] = pq;
+    part[2 * b + 1] = pd;
+    pq += q;
+    pd += d;
   }
   if (threadIdx.x == 0) {
-    cnt->n_changed = s_carry[0];       // queue length (members with out-edges)
-    cnt->n_scatter_edges = s_carry[1]; // their out-edges
+    cnt->n_changed = tq;        // queue length (members with out-edges)
+    cnt->n_scatter_edges = td;  // their out-edges
   }
 }
 
@@ -255,79 +243,44 @@ __global__ void __launch_bounds__(kNT)
   if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
-  const QLane ql = q_lane(cbits, nW, w0);
+  QWarp w;
+  q_warp_load(cbits, csr_off, nW, w0, w);
+  int val[kQWordsPerWarp];
+#pragma unroll
+  for (int i = 0; i < kQWordsPerWarp; ++i)
+    val[i] = w.deg[i] > 0 ? vd[(w0 + i) * 32 + lane] : 0;
   int cq, cd;
-  q_warp_counts(ql, csr_off, w0, &cq, &cd);
+  q_warp_totals(w, &cq, &cd);
   if (lane == 0) {
     s_q[warp] = cq;
     s_d[warp] = cd;
   }
   __syncthreads();
   int bq = part[2 * blockIdx.x], bd = part[2 * blockIdx.x + 1];
-  for (int w = 0; w < warp; ++w) {
-    bq += s_q[w];
-    bd += s_d[w];
+  for (int k = 0; k < warp; ++k) {
+    bq += s_q[k];
+    bd += s_d[k];
   }
-  if (ql.word) cbits[w0 + lane] = 0u;
-  if (ql.dense) {
-    for (int i = 0; i < kQWordsPerWarp; ++i) {
-      const uint32_t word = __shfl_sync(0xffffffffu, ql.word, i);
-      if (!word) continue;
+  if (w.myword) cbits[w0 + lane] = 0u;
+#pragma unroll
+  for (int i = 0; i < kQWordsPerWarp; ++i) {
+    const int deg = w.deg[i];
+    const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
+    if (!qb) continue;  // warp-uniform
+    const int incl = warp_incl_sum_i(deg);
+    if (deg > 0) {
       const int v = (w0 + i) * 32 + lane;
-      int deg = 0, off = 0;
-      if ((word >> lane) & 1u) {
-        off = csr_off[v];
-        deg = csr_off[v + 1] - off;
-      }
-      const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
-      const int incl = warp_incl_sum_i(deg);
-      if (deg > 0) {
-        const int val = vd[v];
-        const int pos = bq + __popc(qb & ((1u << lane) - 1u));
-        const int end = bd + incl;
-        q_ids[pos] = v;
-        q_vals[pos] = val;
-        q_end[pos] = end;
-        q_delta[pos] = off - (end - deg);
-        snap[v] = val;
-        if (hist) atomicAdd(&s_hist[gasfeat::degree_bucket(deg)], 1);
-      }
-      bq += __popc(qb);
-      bd += __shfl_sync(0xffffffffu, incl, 31);
+      const int pos = bq + __popc(qb & ((1u << lane) - 1u));
+      const int end = bd + incl;
+      q_ids[pos] = v;
+      q_vals[pos] = val[i];
+      q_end[pos] = end;
+      q_delta[pos] = w.off[i] - (end - deg);
+      snap[v] = val[i];
+      if (hist) atomicAdd(&s_hist[gasfeat::degree_bucket(deg)], 1);
     }
-  } else {
-    // lane-local counts first, then a warp scan gives each lane its offsets
-    int lq = 0, ld = 0;
-    uint32_t m = ql.word;
-    while (m) {
-      const int bit = __ffs(m) - 1;
-      m &= m - 1;
-      const int v = (w0 + lane) * 32 + bit;
-      const int deg = csr_off[v + 1] - csr_off[v];
-      lq += deg > 0;
-      ld += deg;
-    }
-    int pq = warp_incl_sum_i(lq) - lq + bq;
-    int pd = warp_incl_sum_i(ld) - ld + bd;
-    m = ql.word;
-    while (m) {
-      const int bit = __ffs(m) - 1;
-      m &= m - 1;
-      const int v = (w0 + lane) * 32 + bit;
-      const int off = csr_off[v];
-      const int deg = csr_off[v + 1] - off;
-      if (deg > 0) {
-        const int val = vd[v];
-        pd += deg;
-        q_ids[pq] = v;
-        q_vals[pq] = val;
-        q_end[pq] = pd;
-        q_delta[pq] = off - (pd - deg);
-        snap[v] = val;
-        if (hist) atomicAdd(&s_hist[gasfeat::degree_bucket(deg)], 1);
-        ++pq;
-      }
-    }
+    bq += __popc(qb);
+    bd += __shfl_sync(0xffffffffu, incl, 31);
   }
   if (hist) {
     __syncthreads();
