@@ -170,9 +170,11 @@ def run_ours(args, rank, world):
 
     t = time.time()
     e_s = gg.GASEngineGPU("sssp")
+    e_c = gg.GASEngineGPU("cc")
+    for e in (e_s, e_c):
+        e.set_edge_placement(args.edges)
     vd_s = initial_vertex_data("sssp", ssp.nV, int(sources[0]))
     e_s.setGraph(ssp.nV, vd_s, ssp.nE, ssp.weights, ssp.src, ssp.dst, sp)
-    e_c = gg.GASEngineGPU("cc")
     vd_c = initial_vertex_data("cc", ccg.nV)
     e_c.setGraph(ccg.nV, vd_c, ccg.nE, None, ccg.src, ccg.dst, sp)
     log(f"setGraph (host CSR/CSC build + upload) {time.time() - t:.1f}s")
@@ -284,7 +286,7 @@ def run_ours(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded R-MAT + grid islands; reference datasets unavailable)",
-        "config": config_dict(args.scale, {"schedule": args.schedule,
+        "config": config_dict(args.scale, {"schedule": args.schedule, "edges": args.edges,
                                            "edges_visited_per_step": ev_units,
                                            "iterations": {"sssp": iters["sssp"],
                                                           "cc": iters["cc"]}}),
@@ -630,6 +632,8 @@ def main():
     ap.add_argument("--schedule", default="learned",
                     choices=["learned", "auto", "generic", "push", "pull", "ordered"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--edges", default="device", choices=["device", "host"],
+                    help="edge arrays in HBM or in pinned host memory (NVLink-C2C)")
     ap.add_argument("--workload", default="sssp-cc", choices=["sssp-cc", "batched"])
     ap.add_argument("--batch-graphs", type=int, default=BATCH_GRAPHS)
     ap.add_argument("--launch-list", action="store_true",

@@ -168,6 +168,7 @@ _SIGS = {
                                  C.POINTER(BatchStats), c_vp]),
     "gas_batch_tune": ("status", [c_vp, c_i32, c_dbl, c_i32, C.POINTER(c_i32),
                                   C.POINTER(C.c_float), c_vp]),
+    "gas_engine_set_edge_placement": ("status", [c_vp, c_i32]),
     "gas_engine_download_graph": ("status", [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "gas_engine_prepare_scatter": ("status", [c_vp, C.POINTER(c_vp), c_vp]),
     "gas_engine_view_get": ("status", [c_vp, c_vp]),

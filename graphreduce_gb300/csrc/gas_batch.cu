@@ -120,13 +120,31 @@ struct MsPushPol {
   __device__ Val reduce(Val a, Val) const { return a; }
   __device__ Val map(int, int, int) const { return 0; }
   __device__ void emit(int, int, Val) const {}
-  // a: queue position of the pushing vertex, pos: CSR position of the edge
-  __device__ __forceinline__ void visit(int a, int, int pos) const {
-    const int v = __ldg(csr_dst + pos);
-    const uint32_t m = (uint32_t)__ldg(q_mask + a) & ~visited[v];
-    if (m) {
-      const uint32_t old = atomicOr(next + v, m);
-      if (old == 0u) atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
+  // a: queue position of the pushing vertex, pos: CSR position of the edge.
+  // visited does not change during the push.  A push that sees next[v]
+  // already non-zero (through L2) only ORs its lanes in; one that sees 0
+  // uses the returned old value, and the one that turned next[v] non-zero
+  // sets the touched bit -- exactly one per touched vertex.
+  struct Probe {
+    int v;
+    uint32_t m;
+    bool first;
+  };
+  __device__ __forceinline__ Probe probe(bool valid, int a, int, int pos) const {
+    Probe p{0, 0u, false};
+    if (valid) {
+      p.v = __ldg(csr_dst + pos);
+      p.m = (uint32_t)__ldg(q_mask + a) & ~__ldg(visited + p.v);
+      p.first = p.m && __ldcg(next + p.v) == 0u;
+    }
+    return p;
+  }
+  __device__ __forceinline__ void commit(const Probe &p) const {
+    if (!p.m) return;
+    if (!p.first) {
+      atomicOr(next + p.v, p.m);
+    } else if (atomicOr(next + p.v, p.m) == 0u) {
+      atomicOr(tbits + ((uint32_t)p.v >> 5), 1u << (p.v & 31));
     }
   }
 };
@@ -259,7 +277,7 @@ __global__ void __launch_bounds__(kNT)
     k_ms_write(uint32_t *tbits, uint32_t *next, uint32_t *visited, const int32_t *csr_off,
                int nW, const int32_t *part, int L, const gas_counters *cnt, int level_add,
                int32_t *depth, int32_t *q_ids, int32_t *q_mask, int32_t *q_end,
-               int32_t *q_delta) {
+               int32_t *q_delta, int32_t *chunk_row) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   const int level = cnt->iteration + level_add;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -307,6 +325,10 @@ __global__ void __launch_bounds__(kNT)
       q_mask[pos] = (int32_t)nw;
       q_end[pos] = end;
       q_delta[pos] = w.off[i] - (end - deg);
+      // chunk partition of the next push (chunks starting in this range)
+      for (int c = (end - deg + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk;
+           c * gasdev::kSlabChunk < end; ++c)
+        chunk_row[c] = pos;
     }
     bq += __popc(qb);
     bd += __shfl_sync(0xffffffffu, incl, 31);
@@ -757,7 +779,7 @@ gas_status_t bfs_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle 
   k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
   k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
                                L, b->cnt, 0, b->depth, b->q_ids, b->q_mask, b->q_end,
-                               b->q_delta);
+                               b->q_delta, b->part);
   k_ms_precond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
@@ -770,14 +792,13 @@ gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, i
   const gasdev::SlabSource q = gasdev::slab_source(
       b->q_end, b->q_ids, b->q_delta, 0, 0, &b->cnt->n_changed, &b->cnt->n_scatter_edges,
       b->part);
-  gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, s>>>(q, b->part);
   MsPushPol pol{e->csr_dst, b->q_mask, b->visited, b->next, b->tbits};
   k_ms_push<<<c->slab_grid, kNT, 0, s>>>(pol, q);
   k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart);
   k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
   k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
                                c->bfs_lanes, b->cnt, 1, b->depth, b->q_ids, b->q_mask,
-                               b->q_end, b->q_delta);
+                               b->q_end, b->q_delta, b->part);
   k_ms_cond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
@@ -1118,8 +1139,8 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
     stats->ppr_iterations = LP ? cp.iteration : 0;
     stats->ppr_residual = resid[0];
     stats->piece_edges = LP ? P : 0;
-    // BFS: prologue 6 kernels, 6 per level; PPR: prologue 3, 3 per iteration
-    stats->kernel_launches = (LB ? 6 + 6 * cb.iteration : 0) + (LP ? 3 + 3 * cp.iteration : 0);
+    // BFS: prologue 6 kernels, 5 per level; PPR: prologue 3, 3 per iteration
+    stats->kernel_launches = (LB ? 6 + 5 * cb.iteration : 0) + (LP ? 3 + 3 * cp.iteration : 0);
     stats->graph_launches = direct ? 0 : 1;
     for (int l = 0; l < LP; ++l) stats->ppr_lane_residual[l] = resid[1 + l];
   }

@@ -453,9 +453,43 @@ void dfree(T *&p) {
   p = nullptr;
 }
 
+// Edge arrays in pinned, mapped host memory (GAS_EDGES_HOST): kernels read
+// them over NVLink-C2C through their device address.
+template <class T>
+gas_status_t halloc(T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  void *h = nullptr;
+  cudaError_t e = cudaHostAlloc(&h, n * sizeof(T), cudaHostAllocMapped);
+  void *d = nullptr;
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer(&d, h, 0);
+  if (e != cudaSuccess) {
+    if (h) cudaFreeHost(h);
+    return gas::fail(GAS_ERR_NOMEM, "cudaHostAlloc of %zu bytes: %s", n * sizeof(T),
+                     cudaGetErrorString(e));
+  }
+  if (d != h) {  // kernels and the host must see one address (UVA)
+    cudaFreeHost(h);
+    return gas::fail(GAS_ERR_UNSUPPORTED, "host edge arrays need unified addressing");
+  }
+  *p = static_cast<T *>(h);
+  return GAS_OK;
+}
+
+template <class T>
+void hfree(T *&p) {
+  if (p) cudaFreeHost((void *)p);
+  p = nullptr;
+}
+
 void free_graph(gas_engine *e) {
-  dfree(e->csc_off); dfree(e->csc_src); dfree(e->csr_off); dfree(e->csr_dst);
-  dfree(e->csc_ed); dfree(e->csr_ed);
+  dfree(e->csc_off); dfree(e->csr_off);
+  if (e->edges_on_host) {
+    hfree(e->csc_src); hfree(e->csr_dst); hfree(e->csc_ed); hfree(e->csr_ed);
+  } else {
+    dfree(e->csc_src); dfree(e->csr_dst); dfree(e->csc_ed); dfree(e->csr_ed);
+  }
+  e->edges_on_host = false;
   dfree(e->vd); dfree(e->act); dfree(e->scan); dfree(e->sscan); dfree(e->ret);
   dfree(e->slot); dfree(e->gres); dfree(e->bits);
   dfree(e->tile_first); dfree(e->tile_carry); dfree(e->tile_a0);
@@ -784,12 +818,22 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
 
   const size_t V = (size_t)nV, E = (size_t)nE;
   GAS_TRY(dalloc(&e->csc_off, V + 1));
-  GAS_TRY(dalloc(&e->csc_src, E));
   GAS_TRY(dalloc(&e->csr_off, V + 1));
-  GAS_TRY(dalloc(&e->csr_dst, E));
-  if (have_ed) {
-    GAS_TRY(dalloc((uint8_t **)&e->csc_ed, E * eb));
-    GAS_TRY(dalloc((uint8_t **)&e->csr_ed, E * eb));
+  e->edges_on_host = e->edge_place == GAS_EDGES_HOST;
+  if (e->edges_on_host) {
+    GAS_TRY(halloc(&e->csc_src, E));
+    GAS_TRY(halloc(&e->csr_dst, E));
+    if (have_ed) {
+      GAS_TRY(halloc((uint8_t **)&e->csc_ed, E * eb));
+      GAS_TRY(halloc((uint8_t **)&e->csr_ed, E * eb));
+    }
+  } else {
+    GAS_TRY(dalloc(&e->csc_src, E));
+    GAS_TRY(dalloc(&e->csr_dst, E));
+    if (have_ed) {
+      GAS_TRY(dalloc((uint8_t **)&e->csc_ed, E * eb));
+      GAS_TRY(dalloc((uint8_t **)&e->csr_ed, E * eb));
+    }
   }
   GAS_TRY(dalloc((uint8_t **)&e->vd, V * e->vbytes));
   GAS_TRY(dalloc(&e->act, V));
@@ -880,11 +924,11 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
                              st));
   }
   if (E && !dev_build) {
-    CUDA_TRY(cudaMemcpyAsync(e->csc_src, csc_src.data(), E * 4, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(e->csr_dst, csr_dst.data(), E * 4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(e->csc_src, csc_src.data(), E * 4, cudaMemcpyDefault, st));
+    CUDA_TRY(cudaMemcpyAsync(e->csr_dst, csr_dst.data(), E * 4, cudaMemcpyDefault, st));
     if (have_ed) {
-      CUDA_TRY(cudaMemcpyAsync(e->csc_ed, ed_csc.data(), E * eb, cudaMemcpyHostToDevice, st));
-      CUDA_TRY(cudaMemcpyAsync(e->csr_ed, ed_csr.data(), E * eb, cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(e->csc_ed, ed_csc.data(), E * eb, cudaMemcpyDefault, st));
+      CUDA_TRY(cudaMemcpyAsync(e->csr_ed, ed_csr.data(), E * eb, cudaMemcpyDefault, st));
     }
   }
   if (V)
@@ -1001,7 +1045,7 @@ gas_status_t gas_engine_get_results(gas_engine *e, void *stream) {
     } catch (...) {
       return gas::fail(GAS_ERR_NOMEM, "get_results: edge data");
     }
-    CUDA_TRY(cudaMemcpyAsync(tmp.data(), e->csr_ed, tmp.size(), cudaMemcpyDeviceToHost,
+    CUDA_TRY(cudaMemcpyAsync(tmp.data(), e->csr_ed, tmp.size(), cudaMemcpyDefault,
                              S(stream)));
     CUDA_TRY(cudaStreamSynchronize(S(stream)));
     uint8_t *dst = static_cast<uint8_t *>(e->host_ed);
@@ -1009,6 +1053,14 @@ gas_status_t gas_engine_get_results(gas_engine *e, void *stream) {
       memcpy(dst + (size_t)e->h_csr_perm[j] * eb, &tmp[(size_t)j * eb], eb);
     e->edges_dirty = false;
   }
+  return GAS_OK;
+}
+
+gas_status_t gas_engine_set_edge_placement(gas_engine *e, gas_edge_placement_t where) {
+  if (!e) return gas::fail(GAS_ERR_INVALID, "null engine");
+  if (where != GAS_EDGES_DEVICE && where != GAS_EDGES_HOST)
+    return gas::fail(GAS_ERR_INVALID, "unknown edge placement %d", (int)where);
+  e->edge_place = where;
   return GAS_OK;
 }
 
@@ -1027,7 +1079,7 @@ gas_status_t gas_engine_download_graph(gas_engine *e, int32_t *csc_off, int32_t 
             {csc_ed, e->csc_ed, E * eb}, {csr_ed, e->csr_ed, E * eb}};
   for (const auto &c : cp)
     if (c.dst && c.src && c.bytes)
-      CUDA_TRY(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDefault, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   return GAS_OK;
 }

@@ -42,6 +42,8 @@ struct gas_engine {
   std::vector<int32_t> h_csr_to_csc;   // CSC position of each CSR edge
   int32_t *csr_to_csc = nullptr;       // device copy (on first scatter)
   bool edges_dirty = false;            // a user scatter may have changed edge data
+  int edge_place = GAS_EDGES_DEVICE;   // placement for the next set_graph
+  bool edges_on_host = false;          // csc_src/csr_dst/csc_ed/csr_ed are pinned host memory
   std::vector<int32_t> h_csc_off;  // for host-side counts in setActive
 
   // device graph

@@ -58,31 +58,41 @@ __device__ inline void mlp_eval(const float *wf, int n_in, int n_out, const floa
 }
 
 // One warp evaluates a two-output model on one feature vector (BF16
-// weights in global memory): each lane owns hidden units lane and lane+32;
-// every lane returns both logits.
+// weights in global memory): lane l owns hidden units 2l and 2l+1, so every
+// weight row is one coalesced 4-byte load per lane, and the rows are
+// unrolled by 8 so that their loads overlap; every lane returns both
+// logits.
 __device__ inline void mlp_warp_logits(const __nv_bfloat16 *w, int n_in, const float *x,
                                        float *logits) {
   const Layout L = layout(n_in, 2);
   const int lane = threadIdx.x & 31;
-  float h1a = __bfloat162float(w[L.b1 + lane]), h1b = __bfloat162float(w[L.b1 + lane + 32]);
+  const __nv_bfloat162 *w2v = reinterpret_cast<const __nv_bfloat162 *>(w);
+  // element offsets of the layout are even, so row r, units (2l, 2l+1) is
+  // the bf16 pair at (offset + r * 64) / 2 + l
+  float2 h1 = __bfloat1622float2(w2v[L.b1 / 2 + lane]);
+#pragma unroll 8
   for (int i = 0; i < n_in; ++i) {
-    h1a += x[i] * __bfloat162float(w[L.w1 + i * kH + lane]);
-    h1b += x[i] * __bfloat162float(w[L.w1 + i * kH + lane + 32]);
+    const float2 wv = __bfloat1622float2(w2v[(L.w1 + (size_t)i * kH) / 2 + lane]);
+    h1.x += x[i] * wv.x;
+    h1.y += x[i] * wv.y;
   }
-  h1a = h1a > 0.f ? h1a : 0.f;
-  h1b = h1b > 0.f ? h1b : 0.f;
-  float h2a = __bfloat162float(w[L.b2 + lane]), h2b = __bfloat162float(w[L.b2 + lane + 32]);
+  h1.x = h1.x > 0.f ? h1.x : 0.f;
+  h1.y = h1.y > 0.f ? h1.y : 0.f;
+  float2 h2 = __bfloat1622float2(w2v[L.b2 / 2 + lane]);
+#pragma unroll 8
   for (int i = 0; i < kH; ++i) {
-    const float hi = __shfl_sync(0xffffffffu, i < 32 ? h1a : h1b, i & 31);
-    h2a += hi * __bfloat162float(w[L.w2 + i * kH + lane]);
-    h2b += hi * __bfloat162float(w[L.w2 + i * kH + lane + 32]);
+    const float hi = __shfl_sync(0xffffffffu, (i & 1) ? h1.y : h1.x, i >> 1);
+    const float2 wv = __bfloat1622float2(w2v[(L.w2 + (size_t)i * kH) / 2 + lane]);
+    h2.x += hi * wv.x;
+    h2.y += hi * wv.y;
   }
-  h2a = h2a > 0.f ? h2a : 0.f;
-  h2b = h2b > 0.f ? h2b : 0.f;
-  float o0 = h2a * __bfloat162float(w[L.w3 + lane * 2]) +
-             h2b * __bfloat162float(w[L.w3 + (lane + 32) * 2]);
-  float o1 = h2a * __bfloat162float(w[L.w3 + lane * 2 + 1]) +
-             h2b * __bfloat162float(w[L.w3 + (lane + 32) * 2 + 1]);
+  h2.x = h2.x > 0.f ? h2.x : 0.f;
+  h2.y = h2.y > 0.f ? h2.y : 0.f;
+  // w3 rows are (unit j: logit 0, logit 1): units 2l, 2l+1 are 4 values
+  const float2 a = __bfloat1622float2(w2v[L.w3 / 2 + 2 * lane]);
+  const float2 b = __bfloat1622float2(w2v[L.w3 / 2 + 2 * lane + 1]);
+  float o0 = h2.x * a.x + h2.y * b.x;
+  float o1 = h2.x * a.y + h2.y * b.y;
   for (int d = 16; d > 0; d >>= 1) {
     o0 += __shfl_xor_sync(0xffffffffu, o0, d);
     o1 += __shfl_xor_sync(0xffffffffu, o1, d);

@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kNT)
 __global__ void __launch_bounds__(kNT)
     k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int32_t *part,
               const int32_t *vd, int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
-              int32_t *q_delta, int32_t *snap, int32_t *hist) {
+              int32_t *q_delta, int32_t *snap, int32_t *hist, int32_t *chunk_row) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   __shared__ int s_hist[8];
   if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
@@ -278,6 +278,11 @@ __global__ void __launch_bounds__(kNT)
       q_delta[pos] = w.off[i] - (end - deg);
       snap[v] = val[i];
       if (hist) atomicAdd(&s_hist[gasfeat::degree_bucket(deg)], 1);
+      // the push's chunk partition: every kSlabChunk-edge chunk that starts
+      // inside this entry's edge range starts in queue row pos
+      for (int c = (end - deg + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk;
+           c * gasdev::kSlabChunk < end; ++c)
+        chunk_row[c] = pos;
     }
     bq += __popc(qb);
     bd += __shfl_sync(0xffffffffu, incl, 31);
@@ -305,14 +310,29 @@ struct PushPol {
   __device__ Val reduce(Val a, Val) const { return a; }
   __device__ Val map(int, int, int) const { return 0; }
   __device__ void emit(int, int, Val) const {}
-  __device__ __forceinline__ void visit(int a, int, int pos) const {
-    const int v = __ldg(csr_dst + pos);
-    int cand = __ldg(q_vals + a);
-    if (kWeighted) cand += __ldg(csr_w + pos);
-    if (cand > zero_cap) cand = zero_cap;
-    if (cand < *(volatile const int32_t *)(vd + v)) {
-      const int old = atomicMin(vd + v, cand);
-      if (cand < old) atomicOr(cbits + ((uint32_t)v >> 5), 1u << (v & 31));
+  // The pre-check reads the state through L2 (ld.global.cg): a value read
+  // during the push lies between the iteration's start value and the final
+  // one, so cand < it means the vertex ends the iteration below its start
+  // value -- it changed -- and the bit is set without waiting for the
+  // atomic's result; both updates are fire-and-forget reductions.
+  struct Probe {
+    int v, cand, cur;
+  };
+  __device__ __forceinline__ Probe probe(bool valid, int a, int, int pos) const {
+    Probe p{0, 0, INT_MIN};
+    if (valid) {
+      p.v = __ldg(csr_dst + pos);
+      int cand = __ldg(q_vals + a);
+      if (kWeighted) cand += __ldg(csr_w + pos);
+      p.cand = cand > zero_cap ? zero_cap : cand;
+      p.cur = __ldcg(vd + p.v);
+    }
+    return p;
+  }
+  __device__ __forceinline__ void commit(const Probe &p) const {
+    if (p.cand < p.cur) {
+      atomicMin(vd + p.v, p.cand);
+      atomicOr(cbits + ((uint32_t)p.v >> 5), 1u << (p.v & 31));
     }
   }
 };
@@ -328,11 +348,26 @@ struct BfsPushPol {
   __device__ Val reduce(Val a, Val) const { return a; }
   __device__ Val map(int, int, int) const { return 0; }
   __device__ void emit(int, int, Val) const {}
-  __device__ __forceinline__ void visit(int, int, int pos) const {
-    const int v = __ldg(csr_dst + pos);
-    if (*(volatile const int32_t *)(depth + v) == -1 &&
-        atomicCAS(depth + v, -1, level) == -1)
-      atomicOr(cbits + ((uint32_t)v >> 5), 1u << (v & 31));
+  // Every writer of an iteration stores the same level, so an unreached
+  // vertex (seen through L2) is claimed with a plain store and its bit set
+  // with a reduction.
+  struct Probe {
+    int v;
+    bool unreached;
+  };
+  __device__ __forceinline__ Probe probe(bool valid, int, int, int pos) const {
+    Probe p{0, false};
+    if (valid) {
+      p.v = __ldg(csr_dst + pos);
+      p.unreached = __ldcg(depth + p.v) == -1;
+    }
+    return p;
+  }
+  __device__ __forceinline__ void commit(const Probe &p) const {
+    if (p.unreached) {
+      __stcg(depth + p.v, level);
+      atomicOr(cbits + ((uint32_t)p.v >> 5), 1u << (p.v & 31));
+    }
   }
 };
 
@@ -349,28 +384,6 @@ __global__ void __launch_bounds__(kNT)
   pol.level = cnt->iteration;
   gasdev::slab_loop<BfsPushPol, false>(pol, src, nullptr, nullptr, nullptr, nullptr,
                                        nullptr);
-}
-
-// Chunk partitions of the frontier queue, only when this iteration pushes.
-__global__ void __launch_bounds__(256)
-    k_push_partition(gasdev::SlabSource src, int32_t *part, const gas_counters *cnt) {
-  if (cnt->mode != kModePush) return;
-  int nS, E;
-  gasdev::slab_sizes(src, nS, E);
-  const int nchunks = (E + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks;
-       c += gridDim.x * blockDim.x) {
-    const int e = c * gasdev::kSlabChunk;
-    int lo = 0, hi = nS;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (src.ends[mid] <= e)
-        lo = mid + 1;
-      else
-        hi = mid;
-    }
-    part[c] = lo;
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -569,7 +582,8 @@ gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c) {
   k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart,
                                          (const int32_t *)e->vd, e->q_ids, e->q_vals,
                                          e->q_end, e->q_delta, e->snap,
-                                         (e->trace_on || e->sched_model) ? e->hist : nullptr);
+                                         (e->trace_on || e->sched_model) ? e->hist : nullptr,
+                                         e->slab_qpart);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -617,7 +631,6 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   const gasdev::SlabSource qsrc = gasdev::slab_source(
       e->q_end, e->q_ids, e->q_delta, 0, 0, &e->cnt->n_changed,
       &e->cnt->n_scatter_edges, e->slab_qpart);
-  k_push_partition<<<2 * e->num_sms, 256, 0, cs>>>(qsrc, e->slab_qpart, e->cnt);
   const int grid = c.slab_grid;  // resident CTAs only (persistent warps)
   const int pgrid = c.push_grid;
   const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
@@ -641,7 +654,7 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   } else if (e->prog == GAS_PROG_SSSP) {
     PushPol<true> pol{e->csr_dst, (const int32_t *)e->csr_ed, e->q_vals,
                       (int32_t *)e->vd, e->cbits, zero_cap};
-    k_push<PushPol<true>><<<pgrid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
+    k_push<decltype(pol)><<<pgrid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
     PullPol<true> pp{e->csc_src, (const int32_t *)e->csc_ed, e->snap, (int32_t *)e->vd,
                      e->cbits, zero_cap};
     k_pull<PullPol<true>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->slab_fix,
@@ -651,7 +664,7 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   } else {
     PushPol<false> pol{e->csr_dst, nullptr, e->q_vals, (int32_t *)e->vd, e->cbits,
                        zero_cap};
-    k_push<PushPol<false>><<<pgrid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
+    k_push<decltype(pol)><<<pgrid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
     PullPol<false> pp{e->csc_src, nullptr, e->snap, (int32_t *)e->vd, e->cbits, zero_cap};
     k_pull<PullPol<false>><<<grid, kNT, 0, cs>>>(pp, dsrc, cf, cc, e->slab_a0, e->slab_fix,
                                                  e->slab_fix_n, e->cnt);
@@ -832,9 +845,10 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     stats->pull_iters = c.n_pull;
     // prologue (gather/apply, fixup, commit | bfs apply; seed; 3 compaction;
     // precond) + per iteration (push, pull, pull fixup | bfs push;
-    // 3 compaction; cond) + reset + finish
+    // 3 compaction, which also partitions the next push; cond) + reset +
+    // finish
     const int pro = e->prog == GAS_PROG_BFS ? 7 : (ctx.seeded ? 7 : 11);
-    const int per = e->prog == GAS_PROG_BFS ? 6 : 8;
+    const int per = e->prog == GAS_PROG_BFS ? 5 : 7;
     const int loop_iters = ctx.seeded ? c.iteration : (c.iteration > 0 ? c.iteration - 1 : 0);
     stats->kernel_launches = pro + per * loop_iters + 2;
   }

@@ -223,6 +223,11 @@ class GASEngineGPU:
                ptr, C.byref(st), _stream_ptr(stream))
         return ranks, st
 
+    def set_edge_placement(self, where: str) -> None:
+        """"device" (HBM) or "host" (pinned host memory read over NVLink-C2C);
+        applies from the next setGraph."""
+        L.call("gas_engine_set_edge_placement", self._h, {"device": 0, "host": 1}[where])
+
     def graph_arrays(self) -> dict:
         """Host copies of the CSC and CSR the engine built (edge data as int32
         for the built-in programs)."""

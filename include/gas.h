@@ -523,6 +523,15 @@ gas_status_t gas_engine_view_get(gas_engine *e, gas_engine_view *view);
  * vertex data in place. */
 gas_status_t gas_engine_note_applied(gas_engine *e, int32_t wrote_slots);
 
+/* Where set_graph puts the edge arrays (CSC sources, CSR destinations and
+ * their edge data; offsets and vertex state stay in HBM).  GAS_EDGES_HOST
+ * keeps them in pinned host memory that the kernels read over NVLink-C2C,
+ * for graphs whose edges do not fit in HBM -- the role of the reference's
+ * host-resident shards (gpugas.h:456-584, 1398-1469).  Applies from the
+ * next set_graph. */
+typedef enum { GAS_EDGES_DEVICE = 0, GAS_EDGES_HOST = 1 } gas_edge_placement_t;
+gas_status_t gas_engine_set_edge_placement(gas_engine *e, gas_edge_placement_t where);
+
 /* Host copies of the engine's CSC and CSR (any pointer may be NULL):
  * csc_off[nV+1], csc_src[nE], csr_off[nV+1], csr_dst[nE], and the edge data
  * in CSC and CSR order (nE records each).  Edges of one row keep their

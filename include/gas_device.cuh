@@ -604,6 +604,16 @@ struct IntMin<Pol, decltype((void)Pol::kIntMin, void())> {
   static constexpr bool value = Pol::kIntMin;
 };
 
+// Visit policies may split visit() into probe() (the loads: returns a
+// Probe) and commit(Probe) (the updates), so that slab_loop issues the loads
+// of both slabs in flight before either slab's updates.
+template <class Pol, class = void>
+struct TwoPhase { static constexpr bool value = false; };
+template <class Pol>
+struct TwoPhase<Pol, decltype((void)sizeof(typename Pol::Probe), void())> {
+  static constexpr bool value = true;
+};
+
 // Segment of every lane's edge in one 32-edge slab starting at s.
 struct SlabRows {
   int row;
@@ -725,8 +735,16 @@ __device__ __forceinline__ void slab_loop(Pol &pol, const SlabSource src,
         if (kVert && src.vid) vB = __ldg(src.vid + B.row);
       }
       if constexpr (!kReduce) {
-        if (A.valid) pol.visit(A.row, vA, posA);
-        if (two && B.valid) pol.visit(B.row, vB, posB);
+        if constexpr (TwoPhase<Pol>::value) {
+          // both slabs' loads first, then their (fire-and-forget) updates
+          const typename Pol::Probe pa = pol.probe(A.valid, A.row, vA, posA);
+          const typename Pol::Probe pb = pol.probe(two && B.valid, B.row, vB, posB);
+          pol.commit(pa);
+          pol.commit(pb);
+        } else {
+          if (A.valid) pol.visit(A.row, vA, posA);
+          if (two && B.valid) pol.visit(B.row, vB, posB);
+        }
         r = two ? B.r_next : A.r_next;
       } else {
         Val valA = A.valid ? pol.map(A.row, vA, posA) : pol.zero();
