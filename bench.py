@@ -46,6 +46,14 @@ N_SOURCES = 8
 N_ISLANDS, ISLAND_SIDE = 4096, 32
 METRIC = "GTEPS (SSSP x8 + CC, R-MAT scale 22)"
 MAX_ITERS = 20000  # far above any run of this workload; bounds a device loop
+# DRAM bytes (read + write) per launch of the push kernel on this workload
+# (scale 22, learned schedule, edges in HBM): one-pass ncu metrics
+# dram__bytes_read.sum + dram__bytes_write.sum over all 145 k_push launches of
+# one step, captured with
+#   GAS_HOST_LOOP=1 ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,\
+#     dram__bytes_write.sum --clock-control none -k regex:^k_push$ \
+#     python bench.py --launch-list --no-cpu-baseline
+PUSH_TRAFFIC_S22 = 208.4e6
 
 
 def log(*a):
@@ -276,6 +284,10 @@ def run_ours(args, rank, world):
     split = per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources,
                            args.schedule, sp, stream)
     roof = kernel_roofline(e_s, e_c, dev_s, dev_c, ssp, ccg, args.schedule, sp)
+    if (roof["kernel"].startswith("k_push") and args.scale == SCALE and args.edges == "device"
+            and args.schedule in ("learned", "push")):
+        roof["traffic"] = PUSH_TRAFFIC_S22
+        roof["traffic_source"] = "ncu dram bytes per k_push launch, same workload"
     peak, peak_kind = measured_peaks()
     roof["peak"] = peak
     roof["frac"] = roof["achieved"] / peak

@@ -120,31 +120,15 @@ struct MsPushPol {
   __device__ Val reduce(Val a, Val) const { return a; }
   __device__ Val map(int, int, int) const { return 0; }
   __device__ void emit(int, int, Val) const {}
-  // a: queue position of the pushing vertex, pos: CSR position of the edge.
-  // visited does not change during the push.  A push that sees next[v]
-  // already non-zero (through L2) only ORs its lanes in; one that sees 0
-  // uses the returned old value, and the one that turned next[v] non-zero
-  // sets the touched bit -- exactly one per touched vertex.
-  struct Probe {
-    int v;
-    uint32_t m;
-    bool first;
-  };
-  __device__ __forceinline__ Probe probe(bool valid, int a, int, int pos) const {
-    Probe p{0, 0u, false};
-    if (valid) {
-      p.v = __ldg(csr_dst + pos);
-      p.m = (uint32_t)__ldg(q_mask + a) & ~__ldg(visited + p.v);
-      p.first = p.m && __ldcg(next + p.v) == 0u;
-    }
-    return p;
-  }
-  __device__ __forceinline__ void commit(const Probe &p) const {
-    if (!p.m) return;
-    if (!p.first) {
-      atomicOr(next + p.v, p.m);
-    } else if (atomicOr(next + p.v, p.m) == 0u) {
-      atomicOr(tbits + ((uint32_t)p.v >> 5), 1u << (p.v & 31));
+  // a: queue position of the pushing vertex, pos: CSR position of the edge
+  // (visited does not change during the push; the first lane to make
+  // next[v] non-zero marks v as touched)
+  __device__ __forceinline__ void visit(int a, int, int pos) const {
+    const int v = __ldg(csr_dst + pos);
+    const uint32_t m = (uint32_t)__ldg(q_mask + a) & ~visited[v];
+    if (m) {
+      const uint32_t old = atomicOr(next + v, m);
+      if (old == 0u) atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
     }
   }
 };

@@ -18,8 +18,8 @@ struct Layout {
   size_t w1, b1, w2, b2, w3, b3, total;
 };
 
-__host__ __device__ inline Layout layout(int n_in, int n_out) {
-  Layout l;
+__host__ __device__ constexpr Layout layout(int n_in, int n_out) {
+  Layout l{};
   l.n_in = n_in;
   l.n_out = n_out;
   l.w1 = 0;

@@ -463,10 +463,20 @@ __device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now
   } else if (forced == 2) {
     mode = kModePull;
   } else if (forced == 3 && c.model) {
+    // the schedule head's weights (10.5 KB) into shared memory in one round
+    // of independent 16-byte loads, then the warp evaluates from there
+    constexpr int kW = (int)gaslearn::layout(GAS_SCHED_FEATURES, 2).total;
+    __shared__ __align__(16) __nv_bfloat16 s_w[kW];
+    const uint4 *src = reinterpret_cast<const uint4 *>(c.model);
+    uint4 *dst = reinterpret_cast<uint4 *>(s_w);
+    constexpr int kVec = kW * 2 / 16;
+    for (int i = lane; i < kVec; i += 32) dst[i] = src[i];
+    for (int i = kVec * 8 + lane; i < kW; i += 32) s_w[i] = c.model[i];
+    __syncwarp();
     float f[GAS_SCHED_FEATURES], lg[2];
     gasfeat::schedule_features(cnt->n_changed, cnt->n_scatter_edges, c.hist, it, c.nV,
                                c.nE, c.weighted, f);
-    gaslearn::mlp_warp_logits(c.model, GAS_SCHED_FEATURES, f, lg);
+    gaslearn::mlp_warp_logits(s_w, GAS_SCHED_FEATURES, f, lg);
     mode = lg[1] > lg[0] ? kModePull : kModePush;
   } else {
     mode = ((long long)cnt->n_scatter_edges * cnt->pull_div > (long long)c.nE)
