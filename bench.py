@@ -397,6 +397,13 @@ def kernel_roofline(e_s, e_c, dev_s, dev_c, ssp, ccg, schedule, sp):
 BATCH_GRAPHS, BATCH_LANES, BATCH_SEED = 64, 16, 6
 BATCH_METRIC = "GTEPS (batched: 64 R-MAT graphs x (16 BFS + 16 PPR))"
 PPR_DAMPING, PPR_TOL = 0.85, 1e-6
+# DRAM bytes (read + write) of one PPR iteration of this workload (64 graphs,
+# 16 lanes): one-pass ncu metrics over all 31 k_ppr_pieces and k_ppr_fix
+# launches of a run (9.50 GB + 0.80 GB per iteration), captured with
+#   GAS_HOST_LOOP=1 ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,\
+#     dram__bytes_write.sum --clock-control none -k regex:"k_ppr_pieces|k_ppr_fix" \
+#     python bench.py --workload batched --launch-list
+PPR_TRAFFIC_64 = 10.30e9
 
 
 def make_batched_workload(n_graphs=BATCH_GRAPHS):
@@ -574,12 +581,120 @@ def run_batched(args):
             "total_speedup_of_batch": round((ms_plain_bfs + ms_plain_ppr) / ms, 3)},
         "roofline": {"kernel": "PPR iteration (k_ppr_pieces + k_ppr_fix + k_ppr_finish)",
                      "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": PPR_TRAFFIC_64 if G == BATCH_GRAPHS else None,
+                     "traffic_note": "DRAM bytes per iteration; the [V][16] contribution "
+                                     "gathers are mostly L2 hits",
                      "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": int(ppr_bytes),
                      "avg_launch_ms": round(ms_iter, 4)},
         "clocks": clocks,
     }
+
+
+# ---------------------------------------------------------------------------
+# precision-form PageRank: R-MAT scale 24, directed
+# ---------------------------------------------------------------------------
+PR_SCALE, PR_SEED = 24, 4
+PR_METRIC = "GTEPS (precision PageRank, R-MAT scale 24 directed, E x iterations / time)"
+
+
+def run_pagerank(args):
+    import torch
+
+    import graphreduce_gb300 as gg
+    from graphreduce_gb300.engine import initial_vertex_data
+    from graphreduce_gb300.graph import EdgeList
+    from graphreduce_gb300.learn import DATA, MLP
+
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    scale = args.pr_scale
+    t = time.time()
+    el = EdgeList.rmat(scale, EDGE_FACTOR, *RMAT_ABC, seed=PR_SEED, symmetrize=False)
+    log(f"pagerank workload: scale {scale}: V={el.nV} E={el.nE}, generated in "
+        f"{time.time() - t:.1f}s")
+    e = gg.GASEngineGPU("pagerank")
+    e.setGraph(el.nV, initial_vertex_data("pagerank", el.nV, 0, el.out_degree()), el.nE,
+               None, el.src, el.dst, sp)
+    warm_model = MLP.load(DATA / "warm_start_head.npz")
+    ranks_d = torch.empty(el.nV, dtype=torch.float32, device="cuda")
+    init_d = torch.empty(el.nV, dtype=torch.float32, device="cuda")
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        z = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        z.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(z) / steps
+
+    out = {}
+
+    def uniform():
+        out["u"] = e.pagerank_precision(0.85, 1e-6, 1000, ranks_d.data_ptr(), sp)[1]
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms = timed(uniform, args.steps, args.warmup)
+    clocks = clk.summary()
+    st_u = out["u"]
+    r_uni = ranks_d.cpu().numpy()
+
+    def warm():  # the head's proposal, then the same iteration from it
+        e.pagerank_warm_start(warm_model, 0.85, init_d.data_ptr())
+        out["w"] = e.pagerank_precision_from(init_d.data_ptr(), 0.85, 1e-6, 1000, sp,
+                                             out=ranks_d.data_ptr())[1]
+
+    ms_warm = timed(warm, args.steps, 1)
+    st_w = out["w"]
+    r_warm = ranks_d.cpu().numpy()
+    # roofline: one profiled run (events around every iteration's slab pass)
+    e.set_profiling(True)
+    e.profile(reset=True)
+    e.pagerank_precision(0.85, 1e-6, 1000, ranks_d.data_ptr(), sp)
+    prof = e.profile()
+    e.set_profiling(False)
+    peak, peak_kind = measured_peaks()
+    achieved = prof.pagerank_bytes / (prof.pagerank_ms * 1e-3) / 1e9 if prof.pagerank_ms else 0
+    units = el.nE * st_u.iterations
+    res = {
+        "metric": PR_METRIC, "value": round(units / (ms * 1e-3) / 1e9, 4), "unit": "GTEPS",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (two-sum compensated gather) + f64 residual",
+        "data": "synthetic (seeded R-MAT)",
+        "config": {"workload": f"precision PageRank, R-MAT scale {scale}, edge factor "
+                               f"{EDGE_FACTOR}, directed, seed {PR_SEED}, d=0.85, L1 tol 1e-6",
+                   "V": el.nV, "E": el.nE, "iterations": st_u.iterations,
+                   "residual": st_u.residual,
+                   "l2": "inputs larger than L2"},
+        "warm_start": {"iterations": st_w.iterations, "ms": round(ms_warm, 3),
+                       "speedup": round(ms / ms_warm, 4),
+                       "l1_between_results": float(np.abs(r_uni.astype(np.float64) -
+                                                          r_warm).sum())},
+        "roofline": {"kernel": "k_pr_slab + k_pr_fixup (one PageRank iteration's slab pass)",
+                     "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": int(prof.pagerank_bytes /
+                                                         max(1, prof.pagerank_launches)),
+                     "avg_launch_ms": round(prof.pagerank_ms / max(1, prof.pagerank_launches), 4)},
+        "clocks": clocks,
+    }
+    if args.pr_check:
+        import oracle
+        t = time.time()
+        r64, it64, _ = oracle.pagerank_fp64(el.nV, el.src, el.dst, 0.85, 1e-6)
+        d = np.abs(r_uni.astype(np.float64) - r64)
+        res["error_vs_fp64_oracle"] = {"l1": float(d.sum()), "max_abs": float(d.max()),
+                                       "oracle_iterations": it64,
+                                       "oracle_seconds": round(time.time() - t, 1)}
+    return res
 
 
 # ---------------------------------------------------------------------------
@@ -646,7 +761,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--edges", default="device", choices=["device", "host"],
                     help="edge arrays in HBM or in pinned host memory (NVLink-C2C)")
-    ap.add_argument("--workload", default="sssp-cc", choices=["sssp-cc", "batched"])
+    ap.add_argument("--workload", default="sssp-cc", choices=["sssp-cc", "batched", "pagerank"])
+    ap.add_argument("--pr-scale", type=int, default=PR_SCALE)
+    ap.add_argument("--pr-check", action="store_true",
+                    help="compare with the FP64 oracle (single-threaded C, slow)")
     ap.add_argument("--batch-graphs", type=int, default=BATCH_GRAPHS)
     ap.add_argument("--launch-list", action="store_true",
                     help="run one device-resident step only (profiling)")
@@ -664,6 +782,10 @@ def main():
     if args.workload == "batched":
         if rank == 0:
             print(json.dumps(run_batched(args)), flush=True)
+        return
+    if args.workload == "pagerank":
+        if rank == 0:
+            print(json.dumps(run_pagerank(args)), flush=True)
         return
 
     if world > 1:

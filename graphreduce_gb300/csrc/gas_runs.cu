@@ -267,6 +267,14 @@ struct PrPol {
   __device__ __forceinline__ Val reduce(const Val &a, const Val &b) const {
     return two_sum_add(a, b);
   }
+  // Inside a 32-edge slab the contributions are summed as plain floats by
+  // the log-depth segmented scan (relative error <= 5 u of the slab's sum,
+  // the terms being non-negative); the slab sums of a row are combined with
+  // two-sum.
+  typedef float Scan;
+  __device__ __forceinline__ Scan to_scan(const Val &v) const { return v.s; }
+  __device__ __forceinline__ Val from_scan(Scan x) const { return PrVal{x, 0.0f}; }
+  __device__ __forceinline__ Scan scan_add(Scan a, Scan b) const { return __fadd_rn(a, b); }
   __device__ __forceinline__ Val map(int, int, int pos) const {
     return PrVal{__ldg(contrib + __ldg(csc_src + pos)), 0.0f};
   }

@@ -130,15 +130,23 @@ class GASEngineGPU:
                C.byref(st), _stream_ptr(stream))
         return st
 
-    def pagerank_precision(self, damping: float = 0.85, tol: float = 1e-6,
-                           max_iterations: int = 1000, out: np.ndarray | None = None,
-                           stream=None):
-        """Normalised PageRank with FP32 compensated gather and FP64 L1
-        residual; returns (ranks float32[nV], RunStats)."""
+    def _out_ptr(self, out):
+        """(host array or None, pointer) for a float32 result: out may be a
+        numpy array, a device pointer (int) or None (new host array)."""
+        if isinstance(out, int):
+            return None, out
         ranks = out if out is not None else np.zeros(self.nVertices, np.float32)
+        return ranks, ranks.ctypes.data
+
+    def pagerank_precision(self, damping: float = 0.85, tol: float = 1e-6,
+                           max_iterations: int = 1000, out=None, stream=None):
+        """Normalised PageRank with FP32 compensated gather and FP64 L1
+        residual; returns (ranks, RunStats), ranks None when out is a device
+        pointer."""
+        ranks, ptr = self._out_ptr(out)
         st = RunStats()
         L.call("gas_engine_pagerank_precision", self._h, damping, tol, max_iterations,
-               ranks.ctypes.data, C.byref(st), _stream_ptr(stream))
+               ptr, C.byref(st), _stream_ptr(stream))
         return ranks, st
 
     def vertex_data_device(self) -> int:
@@ -192,20 +200,23 @@ class GASEngineGPU:
                             out: np.ndarray | None = None) -> np.ndarray:
         """Initial PageRank vector proposed by the warm-start head, scaled to
         the fixed point's mass for this damping."""
-        init = out if out is not None else np.zeros(self.nVertices, np.float32)
-        L.call("gas_engine_pagerank_warm_start", self._h, mlp.handle, damping,
-               init.ctypes.data, None)
+        init, ptr = self._out_ptr(out)
+        L.call("gas_engine_pagerank_warm_start", self._h, mlp.handle, damping, ptr, None)
         return init
 
-    def pagerank_precision_from(self, init: np.ndarray | None, damping: float = 0.85,
-                                tol: float = 1e-6, max_iterations: int = 1000,
-                                stream=None):
-        ranks = np.zeros(self.nVertices, np.float32)
+    def pagerank_precision_from(self, init, damping: float = 0.85, tol: float = 1e-6,
+                                max_iterations: int = 1000, stream=None, out=None):
+        """From a given start vector (numpy array, device pointer or None for
+        the uniform 1/N) -> (ranks, RunStats)."""
+        ranks, ptr = self._out_ptr(out)
         st = RunStats()
-        ip = None if init is None else np.ascontiguousarray(init, np.float32)
+        if isinstance(init, int):
+            ip, iptr = None, init
+        else:
+            ip = None if init is None else np.ascontiguousarray(init, np.float32)
+            iptr = None if ip is None else ip.ctypes.data
         L.call("gas_engine_pagerank_precision_from", self._h, damping, tol, max_iterations,
-               None if ip is None else ip.ctypes.data, ranks.ctypes.data, C.byref(st),
-               _stream_ptr(stream))
+               iptr, ptr, C.byref(st), _stream_ptr(stream))
         return ranks, st
 
     def ppr_precision(self, seed: int, damping: float = 0.85, tol: float = 1e-6,

@@ -686,6 +686,32 @@ __device__ __forceinline__ typename Pol::Val slab_fold(const Pol &pol,
   }
 }
 
+// Policies whose Val carries compensation may declare a cheaper type for
+// the scan inside a slab: `typedef ... Scan;` with to_scan(Val),
+// from_scan(Scan) and scan_add(Scan, Scan).  A slab is then folded in that
+// type, and the carry from earlier slabs joins its first segment through
+// reduce() after the scan, so sums of many slabs stay compensated.
+template <class Pol, class = void>
+struct PlainScan { static constexpr bool value = false; };
+template <class Pol>
+struct PlainScan<Pol, decltype((void)sizeof(typename Pol::Scan), void())> {
+  static constexpr bool value = true;
+};
+
+template <class Pol>
+__device__ __forceinline__ typename Pol::Scan slab_fold_scan(const Pol &pol,
+                                                             typename Pol::Scan val,
+                                                             unsigned mask, int lane) {
+  const unsigned heads = mask | 1u;
+  const int seg_start = 31 - __clz(heads & ((2u << lane) - 1u));
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const typename Pol::Scan t = shfl_up_any(val, d);
+    if (lane - d >= seg_start) val = pol.scan_add(t, val);
+  }
+  return val;
+}
+
 // Pol as for tile_loop: Val, zero(), reduce(), map(seg, vertex, pos),
 // emit(seg, vertex, Val) when kReduce; visit(seg, vertex, pos) otherwise.
 // Two slabs are in flight per iteration so that their load chains overlap.
@@ -749,9 +775,14 @@ __device__ __forceinline__ void slab_loop(Pol &pol, const SlabSource src,
       } else {
         Val valA = A.valid ? pol.map(A.row, vA, posA) : pol.zero();
         Val valB = (two && B.valid) ? pol.map(B.row, vB, posB) : pol.zero();
-        // slab A
-        if (lane == 0 && have_carry) valA = pol.reduce(carry, valA);
-        valA = slab_fold(pol, valA, A.mask, lane);
+        // slab A (its first segment is row r)
+        if constexpr (PlainScan<Pol>::value) {
+          valA = pol.from_scan(slab_fold_scan(pol, pol.to_scan(valA), A.mask, lane));
+          if (have_carry && A.row == r) valA = pol.reduce(carry, valA);
+        } else {
+          if (lane == 0 && have_carry) valA = pol.reduce(carry, valA);
+          valA = slab_fold(pol, valA, A.mask, lane);
+        }
         {
           const bool to_first = A.ends_here && open_first && A.row == r_first;
           if (A.ends_here) {
@@ -769,8 +800,13 @@ __device__ __forceinline__ void slab_loop(Pol &pol, const SlabSource src,
           if (have_carry) carry = v_last;
         }
         if (two) {
-          if (lane == 0 && have_carry) valB = pol.reduce(carry, valB);
-          valB = slab_fold(pol, valB, B.mask, lane);
+          if constexpr (PlainScan<Pol>::value) {
+            valB = pol.from_scan(slab_fold_scan(pol, pol.to_scan(valB), B.mask, lane));
+            if (have_carry && B.row == A.r_next) valB = pol.reduce(carry, valB);
+          } else {
+            if (lane == 0 && have_carry) valB = pol.reduce(carry, valB);
+            valB = slab_fold(pol, valB, B.mask, lane);
+          }
           const bool to_first = B.ends_here && open_first && B.row == r_first;
           if (B.ends_here) {
             if (to_first) {
