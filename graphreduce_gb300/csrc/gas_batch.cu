@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kNT)
 
 // Pass 2: depths of the new lanes, visited, the next queue; clears next and
 // the touched bitmap.  level = counters.iteration + level_add.
-__global__ void __launch_bounds__(kNT)
+__global__ void __launch_bounds__(kNT, 5)
     k_ms_write(uint32_t *tbits, uint32_t *next, uint32_t *visited, const int32_t *csr_off,
                int nW, const int32_t *part, int L, const gas_counters *cnt, int level_add,
                int32_t *depth, int32_t *q_ids, int32_t *q_mask, int32_t *q_end,

@@ -234,7 +234,9 @@ __global__ void __launch_bounds__(kNT)
   }
 }
 
-__global__ void __launch_bounds__(kNT)
+// (at most 48 registers: 5 CTAs per SM, so a sparse iteration's mostly
+// empty bitmap tiles pass in fewer waves)
+__global__ void __launch_bounds__(kNT, 5)
     k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int32_t *part,
               const int32_t *vd, int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
               int32_t *q_delta, int32_t *snap, int32_t *hist, int32_t *chunk_row) {
