@@ -312,11 +312,13 @@ struct PushPol {
   __device__ Val reduce(Val a, Val) const { return a; }
   __device__ Val map(int, int, int) const { return 0; }
   __device__ void emit(int, int, Val) const {}
-  // The pre-check reads the state through L2 (ld.global.cg): a value read
-  // during the push lies between the iteration's start value and the final
-  // one, so cand < it means the vertex ends the iteration below its start
-  // value -- it changed -- and the bit is set without waiting for the
-  // atomic's result; both updates are fire-and-forget reductions.
+  // The pre-check is a plain (L1-cacheable) load: any value it returns was
+  // held by the vertex during this iteration (L1 starts each kernel empty),
+  // so it lies between the iteration's start value and the final one; cand
+  // >= it means cand cannot lower the vertex, and cand < it means the vertex
+  // ends the iteration below its start value -- it changed -- so the bit is
+  // set without waiting for the atomic's result; both updates are
+  // fire-and-forget reductions.
   struct Probe {
     int v, cand, cur;
   };
@@ -327,7 +329,7 @@ struct PushPol {
       int cand = __ldg(q_vals + a);
       if (kWeighted) cand += __ldg(csr_w + pos);
       p.cand = cand > zero_cap ? zero_cap : cand;
-      p.cur = __ldcg(vd + p.v);
+      p.cur = vd[p.v];
     }
     return p;
   }
@@ -350,9 +352,9 @@ struct BfsPushPol {
   __device__ Val reduce(Val a, Val) const { return a; }
   __device__ Val map(int, int, int) const { return 0; }
   __device__ void emit(int, int, Val) const {}
-  // Every writer of an iteration stores the same level, so an unreached
-  // vertex (seen through L2) is claimed with a plain store and its bit set
-  // with a reduction.
+  // Every writer of an iteration stores the same level, so a vertex seen
+  // unreached (a plain load: a stale -1 only repeats the same store) is
+  // claimed with a plain store and its bit set with a reduction.
   struct Probe {
     int v;
     bool unreached;
@@ -361,7 +363,7 @@ struct BfsPushPol {
     Probe p{0, false};
     if (valid) {
       p.v = __ldg(csr_dst + pos);
-      p.unreached = __ldcg(depth + p.v) == -1;
+      p.unreached = depth[p.v] == -1;
     }
     return p;
   }
