@@ -70,7 +70,7 @@ class Counters(C.Structure):
                 ("error", c_i32), ("iteration", c_i32), ("cond", c_i32),
                 ("n_changed", c_i32), ("max_iter", c_i32), ("mode", c_i32),
                 ("n_push", c_i32), ("n_pull", c_i32), ("pull_div", c_i32),
-                ("pad", c_i32 * 4)]
+                ("sched", c_i32), ("push_chunk_log2", c_i32), ("pad", c_i32 * 2)]
 
 
 GAS_BATCH_MAX_LANES = 32

@@ -900,7 +900,9 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
   GAS_TRY(dalloc(&e->zero_vid, zero_vid.size()));
   e->slab_cap = (int32_t)((E + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk + 1);
   GAS_TRY(dalloc(&e->slab_dpart, (size_t)e->slab_cap));
-  GAS_TRY(dalloc(&e->slab_qpart, (size_t)e->slab_cap));
+  // the push may cut its queue's edges into chunks as small as 64 edges
+  GAS_TRY(dalloc(&e->slab_qpart,
+                 (size_t)((E >> gasdev::kSlabChunkMinLog2) + 2)));
   GAS_TRY(dalloc(&e->slab_a0, (size_t)e->slab_cap));
   GAS_TRY(dalloc((uint8_t **)&e->slab_first, (size_t)e->slab_cap * 8));
   GAS_TRY(dalloc((uint8_t **)&e->slab_carry, (size_t)e->slab_cap * 8));

@@ -206,31 +206,89 @@ __global__ void __launch_bounds__(kNT)
   }
 }
 
-// Exclusive scan of the block pairs in one pass: thread t folds a run of
-// ceil(nb / kNT) consecutive blocks, one CTA scan, then the runs are
-// rewritten as prefixes.
-__global__ void __launch_bounds__(kNT)
-    k_q_spine(int32_t *part, int nb, gas_counters *cnt) {
-  const int per = (nb + kNT - 1) / kNT;
+// Exclusive scan of the block pairs in one pass: 1024 threads, thread t
+// holds a run of ceil(nb / 1024) consecutive pairs in registers (8-byte
+// loads, all issued before the first is used), one CTA scan, then the runs
+// are rewritten as prefixes.  Also picks the push's chunk size for the new
+// queue: 512 edges per warp chunk, halved (down to 64) while the queue's
+// edges would give fewer than two chunks per push warp, so that a small
+// frontier still spreads over the GPU instead of running as a few long
+// per-warp chains of dependent loads.
+constexpr int kSpineNT = 1024;
+constexpr int kSpineRegs = 8;
+
+__global__ void __launch_bounds__(kSpineNT)
+    k_q_spine(int32_t *part, int nb, gas_counters *cnt, int push_warps) {
+  int2 *p2 = reinterpret_cast<int2 *>(part);
+  const int per = (nb + kSpineNT - 1) / kSpineNT;
   const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
+  const bool in_regs = per <= kSpineRegs;
+  int2 x[kSpineRegs];
   int sq = 0, sd = 0;
-  for (int b = b0; b < b1; ++b) {
-    sq += part[2 * b];
-    sd += part[2 * b + 1];
+  if (in_regs) {
+#pragma unroll
+    for (int k = 0; k < kSpineRegs; ++k) x[k] = b0 + k < b1 ? p2[b0 + k] : make_int2(0, 0);
+#pragma unroll
+    for (int k = 0; k < kSpineRegs; ++k) {
+      sq += x[k].x;
+      sd += x[k].y;
+    }
+  } else {
+    for (int b = b0; b < b1; ++b) {
+      const int2 y = p2[b];
+      sq += y.x;
+      sd += y.y;
+    }
   }
-  int tq, td;
-  int pq = cta_excl_sum(sq, &tq);
-  int pd = cta_excl_sum(sd, &td);
-  for (int b = b0; b < b1; ++b) {
-    const int q = part[2 * b], d = part[2 * b + 1];
-    part[2 * b] = pq;
-    part[2 * b + 1] = pd;
-    pq += q;
-    pd += d;
+  // CTA exclusive scan of (sq, sd)
+  __shared__ int2 s_w[kSpineNT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int iq = sq, id = sd;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int oq = __shfl_up_sync(0xffffffffu, iq, d);
+    const int od = __shfl_up_sync(0xffffffffu, id, d);
+    if (lane >= d) {
+      iq += oq;
+      id += od;
+    }
+  }
+  if (lane == 31) s_w[warp] = make_int2(iq, id);
+  __syncthreads();
+  int pq = iq - sq, pd = id - sd, tq = 0, td = 0;
+#pragma unroll 8
+  for (int w = 0; w < kSpineNT / 32; ++w) {
+    const int2 t = s_w[w];
+    if (w < warp) {
+      pq += t.x;
+      pd += t.y;
+    }
+    tq += t.x;
+    td += t.y;
+  }
+  if (in_regs) {
+#pragma unroll
+    for (int k = 0; k < kSpineRegs; ++k) {
+      if (b0 + k < b1) {
+        p2[b0 + k] = make_int2(pq, pd);
+        pq += x[k].x;
+        pd += x[k].y;
+      }
+    }
+  } else {
+    for (int b = b0; b < b1; ++b) {
+      const int2 y = p2[b];
+      p2[b] = make_int2(pq, pd);
+      pq += y.x;
+      pd += y.y;
+    }
   }
   if (threadIdx.x == 0) {
     cnt->n_changed = tq;        // queue length (members with out-edges)
     cnt->n_scatter_edges = td;  // their out-edges
+    int cl = gasdev::kSlabChunkLog2;
+    while (cl > gasdev::kSlabChunkMinLog2 && (td >> cl) < 2 * push_warps) --cl;
+    cnt->push_chunk_log2 = cl;
   }
 }
 
@@ -239,7 +297,8 @@ __global__ void __launch_bounds__(kNT)
 __global__ void __launch_bounds__(kNT, 5)
     k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int32_t *part,
               const int32_t *vd, int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
-              int32_t *q_delta, int32_t *snap, int32_t *hist, int32_t *chunk_row) {
+              int32_t *q_delta, int32_t *snap, int32_t *hist, int32_t *chunk_row,
+              const gas_counters *cnt) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   __shared__ int s_hist[8];
   if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
@@ -259,6 +318,7 @@ __global__ void __launch_bounds__(kNT, 5)
   }
   __syncthreads();
   int bq = part[2 * blockIdx.x], bd = part[2 * blockIdx.x + 1];
+  const int cl = cnt->push_chunk_log2;
   for (int k = 0; k < warp; ++k) {
     bq += s_q[k];
     bd += s_d[k];
@@ -280,10 +340,9 @@ __global__ void __launch_bounds__(kNT, 5)
       q_delta[pos] = w.off[i] - (end - deg);
       snap[v] = val[i];
       if (hist) atomicAdd(&s_hist[gasfeat::degree_bucket(deg)], 1);
-      // the push's chunk partition: every kSlabChunk-edge chunk that starts
+      // the push's chunk partition: every (1 << cl)-edge chunk that starts
       // inside this entry's edge range starts in queue row pos
-      for (int c = (end - deg + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk;
-           c * gasdev::kSlabChunk < end; ++c)
+      for (int c = (end - deg + (1 << cl) - 1) >> cl; (c << cl) < end; ++c)
         chunk_row[c] = pos;
     }
     bq += __popc(qb);
@@ -459,7 +518,7 @@ struct LoopCtl {
 // more than 1/pull_div of all edges.  With tracing, records the iteration.
 __device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now) {
   const int lane = threadIdx.x & 31;
-  const int forced = cnt->pad[0];  // 0 auto, 1 push, 2 pull, 3 learned
+  const int forced = cnt->sched;  // 0 auto, 1 push, 2 pull, 3 learned
   const int it = cnt->iteration;   // the iteration being scheduled
   int mode;
   if (forced == 1) {
@@ -552,7 +611,7 @@ __global__ void k_fast_reset(gas_counters *cnt, int max_iter, int forced,
   cnt->max_iter = max_iter;
   cnt->n_push = 0;
   cnt->n_pull = 0;
-  cnt->pad[0] = forced;
+  cnt->sched = forced;
   cnt->pull_div = pull_div;
   cnt->mode = kModePush;
   cnt->n_changed = 0;  // no previous queue whose snapshots need resetting
@@ -592,12 +651,12 @@ int32_t snap_zero(const gas_engine *e) {
 gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c) {
   k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart,
                                          e->q_ids, e->snap, snap_zero(e), e->cnt);
-  k_q_spine<<<1, kNT, 0, cs>>>(e->qpart, c.n_qblocks, e->cnt);
+  k_q_spine<<<1, kSpineNT, 0, cs>>>(e->qpart, c.n_qblocks, e->cnt, c.push_grid * (kNT / 32));
   k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart,
                                          (const int32_t *)e->vd, e->q_ids, e->q_vals,
                                          e->q_end, e->q_delta, e->snap,
                                          (e->trace_on || e->sched_model) ? e->hist : nullptr,
-                                         e->slab_qpart);
+                                         e->slab_qpart, e->cnt);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -644,7 +703,7 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   const FastCtx &c = *static_cast<const FastCtx *>(vctx);
   const gasdev::SlabSource qsrc = gasdev::slab_source(
       e->q_end, e->q_ids, e->q_delta, 0, 0, &e->cnt->n_changed,
-      &e->cnt->n_scatter_edges, e->slab_qpart);
+      &e->cnt->n_scatter_edges, e->slab_qpart, &e->cnt->push_chunk_log2);
   const int grid = c.slab_grid;  // resident CTAs only (persistent warps)
   const int pgrid = c.push_grid;
   const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;

@@ -488,7 +488,9 @@ typedef struct {
   int32_t n_push;          /* fast runs: iterations run with push          */
   int32_t n_pull;          /* fast runs: iterations run with dense pull    */
   int32_t pull_div;        /* AUTO pulls when out-edges(C_k)*pull_div > E  */
-  int32_t pad[4];
+  int32_t sched;           /* fast runs: 0 auto, 1 push, 2 pull, 3 learned */
+  int32_t push_chunk_log2; /* fast runs: edges per push warp chunk (log2)  */
+  int32_t pad[2];
 } gas_counters;
 
 typedef struct {

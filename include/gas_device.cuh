@@ -535,7 +535,9 @@ __global__ void __launch_bounds__(kNT)
 // registers.  No shared memory and no CTA barriers.  Segments split across
 // chunks leave a per-chunk carry folded by slab_fixup_loop in chunk order.
 // ---------------------------------------------------------------------------
-constexpr int kSlabChunk = 32 * 16;  // edges per warp chunk
+constexpr int kSlabChunkLog2 = 9;
+constexpr int kSlabChunk = 1 << kSlabChunkLog2;  // edges per warp chunk
+constexpr int kSlabChunkMinLog2 = 6;             // the smallest chunk: one slab pair
 
 struct SlabSource {
   const int32_t *ends;     // [n_seg] exclusive end of segment k in the virtual
@@ -547,7 +549,13 @@ struct SlabSource {
   const int32_t *n_seg_p;  // device counters, or null
   const int32_t *n_edge_p;
   const int32_t *part;     // [n_chunks] segment holding each chunk's first edge
+  const int32_t *chunk_log2_p;  // device log2 of the chunk size, or null
+                                // (kSlabChunk)
 };
+
+__device__ __forceinline__ int slab_chunk_log2(const SlabSource &s) {
+  return s.chunk_log2_p ? *s.chunk_log2_p : kSlabChunkLog2;
+}
 
 __device__ __forceinline__ void slab_sizes(const SlabSource &s, int &nS, int &E) {
   nS = s.n_seg_p ? *s.n_seg_p : s.n_seg;
@@ -728,13 +736,14 @@ __device__ __forceinline__ void slab_loop(Pol &pol, const SlabSource src,
   constexpr bool kVert = NeedsVertex<Pol>::value;
   int nS, E;
   slab_sizes(src, nS, E);
-  const int nchunks = (E + kSlabChunk - 1) / kSlabChunk;
+  const int cl = slab_chunk_log2(src);
+  const int nchunks = (int)(((long long)E + (1 << cl) - 1) >> cl);
   const int lane = threadIdx.x & 31;
   const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   for (int c = gwarp; c < nchunks; c += nwarps) {
-    const int e0 = c * kSlabChunk;
-    const int e1 = e0 + kSlabChunk < E ? e0 + kSlabChunk : E;
+    const int e0 = c << cl;
+    const int e1 = E - e0 > (1 << cl) ? e0 + (1 << cl) : E;
     int r = __ldg(src.part + c);
     const int r_first = r;
     bool open_first = false;
@@ -855,7 +864,7 @@ __device__ __forceinline__ void slab_fixup_loop(Pol &pol, const SlabSource src,
     const int c = fix_list[i];
     const int row = ch_a0[c];
     const int start = row > 0 ? __ldg(src.ends + row - 1) : 0;
-    const int c_first = start / kSlabChunk;
+    const int c_first = start >> slab_chunk_log2(src);
     Val acc = pol.zero();
     for (int q = c_first; q < c; q += 32) {
       Val x = (q + lane < c) ? ch_carry[q + lane] : pol.zero();
@@ -877,7 +886,8 @@ __host__ __device__ inline SlabSource slab_source(const int32_t *ends, const int
                                                   const int32_t *delta, int n_seg,
                                                   int n_edge, const int32_t *n_seg_p,
                                                   const int32_t *n_edge_p,
-                                                  const int32_t *part) {
+                                                  const int32_t *part,
+                                                  const int32_t *chunk_log2_p = nullptr) {
   SlabSource s;
   s.ends = ends;
   s.vid = vid;
@@ -887,6 +897,7 @@ __host__ __device__ inline SlabSource slab_source(const int32_t *ends, const int
   s.n_seg_p = n_seg_p;
   s.n_edge_p = n_edge_p;
   s.part = part;
+  s.chunk_log2_p = chunk_log2_p;
   return s;
 }
 
