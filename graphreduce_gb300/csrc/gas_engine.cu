@@ -502,7 +502,7 @@ void free_graph(gas_engine *e) {
   e->host_ed = nullptr;
   e->edges_dirty = false;
   dfree(e->q_ids); dfree(e->q_vals); dfree(e->q_end); dfree(e->q_delta); dfree(e->snap);
-  dfree(e->qpart); dfree(e->cbits); dfree(e->mbits);
+  dfree(e->qpart); dfree(e->cbits);
   dfree(e->ne_vid); dfree(e->ne_end); dfree(e->zero_vid);
   dfree(e->slab_dpart); dfree(e->slab_qpart); dfree(e->slab_a0);
   dfree(e->slab_first); dfree(e->slab_carry); dfree(e->slab_fix); dfree(e->slab_fix_n);

@@ -81,7 +81,7 @@ struct gas_engine {
   // changed bitmap (being built), membership bitmap of C_k, snapshots
   int32_t *q_ids = nullptr, *q_vals = nullptr, *q_end = nullptr, *q_delta = nullptr;
   int32_t *snap = nullptr, *qpart = nullptr;
-  uint32_t *cbits = nullptr, *mbits = nullptr;
+  uint32_t *cbits = nullptr;
   int32_t pull_div = 4;
 
   // non-empty in-edge rows of the CSC (dense slab passes) and the rest

@@ -62,16 +62,17 @@ __device__ inline void mlp_eval(const float *wf, int n_in, int n_out, const floa
 // weight row is one coalesced 4-byte load per lane, and the rows are
 // unrolled by 8 so that their loads overlap; every lane returns both
 // logits.
-__device__ inline void mlp_warp_logits(const __nv_bfloat16 *w, int n_in, const float *x,
+template <int n_in>
+__device__ inline void mlp_warp_logits(const __nv_bfloat16 *w, const float *x,
                                        float *logits) {
-  const Layout L = layout(n_in, 2);
+  constexpr Layout L = layout(n_in, 2);
   const int lane = threadIdx.x & 31;
   const __nv_bfloat162 *w2v = reinterpret_cast<const __nv_bfloat162 *>(w);
   // element offsets of the layout are even, so row r, units (2l, 2l+1) is
   // the bf16 pair at (offset + r * 64) / 2 + l
   float2 h1 = __bfloat1622float2(w2v[L.b1 / 2 + lane]);
-#pragma unroll 8
-  for (int i = 0; i < n_in; ++i) {
+#pragma unroll
+  for (int i = 0; i < n_in; ++i) {  // x stays in registers
     const float2 wv = __bfloat1622float2(w2v[(L.w1 + (size_t)i * kH) / 2 + lane]);
     h1.x += x[i] * wv.x;
     h1.y += x[i] * wv.y;

@@ -111,15 +111,19 @@ __global__ void k_seed_finite(const int32_t *vd, int nV, int32_t zero_cap,
 }
 
 // ---------------------------------------------------------------------------
-// frontier compaction: changed bitmap -> queue of the members with out-edges
-// (id, value at the end of the iteration, end of its out-edge range in the
-// queue's edge space, CSR position offset), membership bitmap + snapshots of
-// all members for the dense pull.  One lane per vertex: each warp takes 8
-// bitmap words; a word's 32 lanes read their out-degrees coalesced, a ballot
-// gives queue positions, a warp scan gives edge offsets.
+// frontier compaction: changed bitmap -> queue of the members with out-edges,
+// in two parts.  Heavy rows [0, q_heavy) (more than kLightDeg out-edges) are
+// pushed by the warp slabs and hold (id, value at the end of the iteration,
+// end of the out-edge range in the heavy rows' edge space, CSR position
+// offset); light rows [q_heavy, n_changed) are pushed one thread per row and
+// hold (id, value, CSR start, out-degree).  Both parts are in vertex order.
+// Also the snapshots of all members for the dense pull.  One lane per vertex:
+// each warp takes 8 bitmap words; a word's 32 lanes read their out-degrees
+// coalesced, ballots give queue positions, a warp scan gives edge offsets.
 // ---------------------------------------------------------------------------
 constexpr int kQWordsPerWarp = 8;
 constexpr int kQWordsPerBlock = kQWordsPerWarp * (kNT / 32);  // 64 words
+constexpr int kLightDeg = 8;  // rows with at most this many out-edges are light
 
 __device__ __forceinline__ int warp_incl_sum_i(int v) {
   const int lane = threadIdx.x & 31;
@@ -129,6 +133,10 @@ __device__ __forceinline__ int warp_incl_sum_i(int v) {
     if (lane >= d) v += o;
   }
   return v;
+}
+
+__device__ __forceinline__ int4 add4(int4 a, int4 b) {
+  return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
 
 // A warp owns 8 bitmap words; lane l takes vertex 32 w + l of each word, so
@@ -157,151 +165,82 @@ __device__ __forceinline__ void q_warp_load(const uint32_t *cbits, const int32_t
   }
 }
 
-__device__ __forceinline__ void q_warp_totals(const QWarp &w, int *cq, int *cd) {
-  int q = 0, d = 0;
+// The warp's (heavy rows, heavy edges, light rows, light edges).
+__device__ __forceinline__ int4 q_warp_totals(const QWarp &w) {
+  int hq = 0, hd = 0, lq = 0, ld = 0;
 #pragma unroll
   for (int i = 0; i < kQWordsPerWarp; ++i) {
-    q += w.deg[i] > 0;
-    d += w.deg[i];
+    const int d = w.deg[i];
+    if (d > kLightDeg) {
+      ++hq;
+      hd += d;
+    } else if (d > 0) {
+      ++lq;
+      ld += d;
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    q += __shfl_xor_sync(0xffffffffu, q, o);
-    d += __shfl_xor_sync(0xffffffffu, d, o);
+    hq += __shfl_xor_sync(0xffffffffu, hq, o);
+    hd += __shfl_xor_sync(0xffffffffu, hd, o);
+    lq += __shfl_xor_sync(0xffffffffu, lq, o);
+    ld += __shfl_xor_sync(0xffffffffu, ld, o);
   }
-  *cq = q;
-  *cd = d;
+  return make_int4(hq, hd, lq, ld);
 }
 
-// Counts per block; first resets the snapshots of the previous queue (its
-// length is still in the counters) to Program::gatherZero.
+// Counts per block, and the queue's out-degree histogram (schedule
+// features).  The snapshots are written only for a queue that a dense pull
+// reads: after a pull iteration (mode still says so here) the previous
+// queue's snapshots (its length is still in the counters) go back to
+// Program::gatherZero first.
 __global__ void __launch_bounds__(kNT)
     k_q_count(const uint32_t *cbits, const int32_t *csr_off, int nW,
-              int32_t *part, const int32_t *q_ids, int32_t *snap, int32_t zero,
-              const gas_counters *cnt) {
-  const int n_old = cnt->n_changed;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old;
-       i += gridDim.x * blockDim.x)
-    snap[q_ids[i]] = zero;
-  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
+              int4 *part, const int32_t *q_ids, int32_t *snap, int32_t zero,
+              int32_t *hist, const gas_counters *cnt) {
+  if (cnt->mode == kModePull) {
+    const int n_old = cnt->n_changed;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old;
+         i += gridDim.x * blockDim.x)
+      snap[q_ids[i]] = zero;
+  }
+  __shared__ int4 s_t[kNT / 32];
+  __shared__ int s_hist[8];
+  if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
   QWarp w;
   q_warp_load(cbits, csr_off, nW, w0, w);
-  int cq, cd;
-  q_warp_totals(w, &cq, &cd);
-  if (lane == 0) {
-    s_q[warp] = cq;
-    s_d[warp] = cd;
-  }
+  const int4 t = q_warp_totals(w);
+  if (lane == 0) s_t[warp] = t;
   __syncthreads();
+  if (hist) {
+#pragma unroll
+    for (int i = 0; i < kQWordsPerWarp; ++i)
+      if (w.deg[i] > 0) atomicAdd(&s_hist[gasfeat::degree_bucket(w.deg[i])], 1);
+  }
   if (threadIdx.x == 0) {
-    int tq = 0, td = 0;
-    for (int k = 0; k < kNT / 32; ++k) {
-      tq += s_q[k];
-      td += s_d[k];
-    }
-    part[2 * blockIdx.x] = tq;
-    part[2 * blockIdx.x + 1] = td;
+    int4 b = make_int4(0, 0, 0, 0);
+    for (int k = 0; k < kNT / 32; ++k) b = add4(b, s_t[k]);
+    part[blockIdx.x] = b;
+  }
+  if (hist) {
+    __syncthreads();
+    if (threadIdx.x < 8 && s_hist[threadIdx.x]) atomicAdd(hist + threadIdx.x, s_hist[threadIdx.x]);
   }
 }
 
-// Exclusive scan of the block pairs in one pass: 1024 threads, thread t
-// holds a run of ceil(nb / 1024) consecutive pairs in registers (8-byte
-// loads, all issued before the first is used), one CTA scan, then the runs
-// are rewritten as prefixes.  Also picks the push's chunk size for the new
-// queue: 512 edges per warp chunk, halved (down to 64) while the queue's
-// edges would give fewer than two chunks per push warp, so that a small
-// frontier still spreads over the GPU instead of running as a few long
-// per-warp chains of dependent loads.
-constexpr int kSpineNT = 1024;
-constexpr int kSpineRegs = 8;
-
-__global__ void __launch_bounds__(kSpineNT)
-    k_q_spine(int32_t *part, int nb, gas_counters *cnt, int push_warps) {
-  int2 *p2 = reinterpret_cast<int2 *>(part);
-  const int per = (nb + kSpineNT - 1) / kSpineNT;
-  const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
-  const bool in_regs = per <= kSpineRegs;
-  int2 x[kSpineRegs];
-  int sq = 0, sd = 0;
-  if (in_regs) {
-#pragma unroll
-    for (int k = 0; k < kSpineRegs; ++k) x[k] = b0 + k < b1 ? p2[b0 + k] : make_int2(0, 0);
-#pragma unroll
-    for (int k = 0; k < kSpineRegs; ++k) {
-      sq += x[k].x;
-      sd += x[k].y;
-    }
-  } else {
-    for (int b = b0; b < b1; ++b) {
-      const int2 y = p2[b];
-      sq += y.x;
-      sd += y.y;
-    }
-  }
-  // CTA exclusive scan of (sq, sd)
-  __shared__ int2 s_w[kSpineNT / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int iq = sq, id = sd;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int oq = __shfl_up_sync(0xffffffffu, iq, d);
-    const int od = __shfl_up_sync(0xffffffffu, id, d);
-    if (lane >= d) {
-      iq += oq;
-      id += od;
-    }
-  }
-  if (lane == 31) s_w[warp] = make_int2(iq, id);
-  __syncthreads();
-  int pq = iq - sq, pd = id - sd, tq = 0, td = 0;
-#pragma unroll 8
-  for (int w = 0; w < kSpineNT / 32; ++w) {
-    const int2 t = s_w[w];
-    if (w < warp) {
-      pq += t.x;
-      pd += t.y;
-    }
-    tq += t.x;
-    td += t.y;
-  }
-  if (in_regs) {
-#pragma unroll
-    for (int k = 0; k < kSpineRegs; ++k) {
-      if (b0 + k < b1) {
-        p2[b0 + k] = make_int2(pq, pd);
-        pq += x[k].x;
-        pd += x[k].y;
-      }
-    }
-  } else {
-    for (int b = b0; b < b1; ++b) {
-      const int2 y = p2[b];
-      p2[b] = make_int2(pq, pd);
-      pq += y.x;
-      pd += y.y;
-    }
-  }
-  if (threadIdx.x == 0) {
-    cnt->n_changed = tq;        // queue length (members with out-edges)
-    cnt->n_scatter_edges = td;  // their out-edges
-    int cl = gasdev::kSlabChunkLog2;
-    while (cl > gasdev::kSlabChunkMinLog2 && (td >> cl) < 2 * push_warps) --cl;
-    cnt->push_chunk_log2 = cl;
-  }
-}
+constexpr int kSpineNT = 1024;  // k_q_spine (with the loop control, below)
+constexpr int kSpineRegs = 4;
 
 // (at most 48 registers: 5 CTAs per SM, so a sparse iteration's mostly
 // empty bitmap tiles pass in fewer waves)
 __global__ void __launch_bounds__(kNT, 5)
-    k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int32_t *part,
+    k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int4 *part,
               const int32_t *vd, int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
-              int32_t *q_delta, int32_t *snap, int32_t *hist, int32_t *chunk_row,
+              int32_t *q_delta, int32_t *snap, int32_t *chunk_row,
               const gas_counters *cnt) {
-  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
-  __shared__ int s_hist[8];
-  if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
+  __shared__ int4 s_t[kNT / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
   QWarp w;
@@ -310,47 +249,50 @@ __global__ void __launch_bounds__(kNT, 5)
 #pragma unroll
   for (int i = 0; i < kQWordsPerWarp; ++i)
     val[i] = w.deg[i] > 0 ? vd[(w0 + i) * 32 + lane] : 0;
-  int cq, cd;
-  q_warp_totals(w, &cq, &cd);
-  if (lane == 0) {
-    s_q[warp] = cq;
-    s_d[warp] = cd;
-  }
+  const int4 t = q_warp_totals(w);
+  if (lane == 0) s_t[warp] = t;
   __syncthreads();
-  int bq = part[2 * blockIdx.x], bd = part[2 * blockIdx.x + 1];
+  int4 base = part[blockIdx.x];
+  for (int k = 0; k < warp; ++k) base = add4(base, s_t[k]);
+  int bq = base.x, bd = base.y, lq = cnt->q_heavy + base.z;
   const int cl = cnt->push_chunk_log2;
-  for (int k = 0; k < warp; ++k) {
-    bq += s_q[k];
-    bd += s_d[k];
-  }
+  const bool want_snap = cnt->mode == kModePull;  // the next iteration's mode
   if (w.myword) cbits[w0 + lane] = 0u;
+  const unsigned below = (1u << lane) - 1u;
 #pragma unroll
   for (int i = 0; i < kQWordsPerWarp; ++i) {
     const int deg = w.deg[i];
-    const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
-    if (!qb) continue;  // warp-uniform
-    const int incl = warp_incl_sum_i(deg);
-    if (deg > 0) {
-      const int v = (w0 + i) * 32 + lane;
-      const int pos = bq + __popc(qb & ((1u << lane) - 1u));
-      const int end = bd + incl;
+    const bool heavy = deg > kLightDeg;
+    const unsigned hb = __ballot_sync(0xffffffffu, heavy);
+    const unsigned lb = __ballot_sync(0xffffffffu, deg > 0 && !heavy);
+    if (!(hb | lb)) continue;  // warp-uniform
+    const int v = (w0 + i) * 32 + lane;
+    if (hb) {  // warp-uniform
+      const int incl = warp_incl_sum_i(heavy ? deg : 0);
+      if (heavy) {
+        const int pos = bq + __popc(hb & below);
+        const int end = bd + incl;
+        q_ids[pos] = v;
+        q_vals[pos] = val[i];
+        q_end[pos] = end;
+        q_delta[pos] = w.off[i] - (end - deg);
+        // the push's chunk partition: every (1 << cl)-edge chunk that
+        // starts inside this row's heavy-edge range starts in row pos
+        for (int c = (end - deg + (1 << cl) - 1) >> cl; (c << cl) < end; ++c)
+          chunk_row[c] = pos;
+      }
+      bq += __popc(hb);
+      bd += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (deg > 0 && !heavy) {
+      const int pos = lq + __popc(lb & below);
       q_ids[pos] = v;
       q_vals[pos] = val[i];
-      q_end[pos] = end;
-      q_delta[pos] = w.off[i] - (end - deg);
-      snap[v] = val[i];
-      if (hist) atomicAdd(&s_hist[gasfeat::degree_bucket(deg)], 1);
-      // the push's chunk partition: every (1 << cl)-edge chunk that starts
-      // inside this entry's edge range starts in queue row pos
-      for (int c = (end - deg + (1 << cl) - 1) >> cl; (c << cl) < end; ++c)
-        chunk_row[c] = pos;
+      q_end[pos] = deg;
+      q_delta[pos] = w.off[i];
     }
-    bq += __popc(qb);
-    bd += __shfl_sync(0xffffffffu, incl, 31);
-  }
-  if (hist) {
-    __syncthreads();
-    if (threadIdx.x < 8 && s_hist[threadIdx.x]) atomicAdd(hist + threadIdx.x, s_hist[threadIdx.x]);
+    lq += __popc(lb);
+    if (want_snap && deg > 0) snap[v] = val[i];
   }
 }
 
@@ -434,11 +376,64 @@ struct BfsPushPol {
   }
 };
 
+// Light queue rows [q_heavy, n_changed): a warp takes 32 consecutive rows
+// (their CSR start and out-degree, at most kLightDeg, in registers; in the
+// queue arrays a light row holds its CSR start in q_delta and its
+// out-degree in q_end), lays their edges end to end -- at most 32 * kLightDeg
+// of them -- and walks them 32 at a time, two rounds in flight: a ballot of
+// the row starts gives each lane its row, a shuffle its CSR position.  When
+// the rows are CSR neighbours (a dense frontier) the edge loads are
+// coalesced; no per-edge global loads beyond the policy's own.
+template <class Pol>
+__device__ __forceinline__ void light_loop(const Pol &pol, const int32_t *q_start,
+                                           const int32_t *q_deg, const gas_counters *cnt) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int n0 = cnt->q_heavy, n1 = cnt->n_changed;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int base = n0 + gwarp * 32; base < n1; base += nwarps * 32) {
+    const int i = base + lane;
+    const bool ok = i < n1;
+    const int start = ok ? __ldg(q_start + i) : 0;
+    const int deg = ok ? __ldg(q_deg + i) : 0;
+    const int incl = warp_incl_sum_i(deg);
+    const int excl = incl - deg;       // the row's first edge in the warp's run
+    const int shift = start - excl;    // CSR position - run index, per row
+    const int T = __shfl_sync(FULL, incl, 31);
+    for (int r = 0; r < T; r += 64) {
+      int pos[2], row[2];
+      bool valid[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r0 = r + 32 * h;
+        // row of edge r0: the last row starting at or before it
+        const int row0 = __popc(__ballot_sync(FULL, ok && excl <= r0)) - 1;
+        const int k = excl - r0;  // rows starting inside the round
+        const unsigned starts =
+            __reduce_or_sync(FULL, (ok && k >= 1 && k < 32) ? (1u << k) : 0u);
+        int rw = row0 + __popc(starts & ((2u << lane) - 1u));
+        rw = rw < 0 ? 0 : (rw > 31 ? 31 : rw);
+        const int e = r0 + lane;
+        valid[h] = e < T;
+        row[h] = rw;
+        pos[h] = e + __shfl_sync(FULL, shift, rw);
+      }
+      const typename Pol::Probe pa = pol.probe(valid[0], base + row[0], 0, pos[0]);
+      const typename Pol::Probe pb = pol.probe(valid[1], base + row[1], 0, pos[1]);
+      pol.commit(pa);
+      pol.commit(pb);
+    }
+  }
+}
+
+// The queue's heavy rows by warp slabs, then its light rows.
 template <class Pol>
 __global__ void __launch_bounds__(kNT)
     k_push(Pol pol, gasdev::SlabSource src, const gas_counters *cnt) {
   if (cnt->mode != kModePush) return;
   gasdev::slab_loop<Pol, false>(pol, src, nullptr, nullptr, nullptr, nullptr, nullptr);
+  light_loop(pol, src.delta, src.ends, cnt);
 }
 
 __global__ void __launch_bounds__(kNT)
@@ -447,6 +442,7 @@ __global__ void __launch_bounds__(kNT)
   pol.level = cnt->iteration;
   gasdev::slab_loop<BfsPushPol, false>(pol, src, nullptr, nullptr, nullptr, nullptr,
                                        nullptr);
+  light_loop(pol, src.delta, src.ends, cnt);
 }
 
 // ---------------------------------------------------------------------------
@@ -539,7 +535,7 @@ __device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now
     float f[GAS_SCHED_FEATURES], lg[2];
     gasfeat::schedule_features(cnt->n_changed, cnt->n_scatter_edges, c.hist, it, c.nV,
                                c.nE, c.weighted, f);
-    gaslearn::mlp_warp_logits(s_w, GAS_SCHED_FEATURES, f, lg);
+    gaslearn::mlp_warp_logits<GAS_SCHED_FEATURES>(s_w, f, lg);
     mode = lg[1] > lg[0] ? kModePull : kModePush;
   } else {
     mode = ((long long)cnt->n_scatter_edges * cnt->pull_div > (long long)c.nE)
@@ -569,40 +565,108 @@ __device__ __forceinline__ long long global_ns() {
   return (long long)t;
 }
 
-// seeded: the prologue only built the iteration-0 sender set, iteration 0
-// itself runs in the loop (and always exists: A_0 = V is not empty).
-__global__ void k_fast_precond(gas_counters *cnt, LoopCtl c, int seeded) {
+// Exclusive scan of the block totals in one pass: 1024 threads, thread t
+// holds a run of ceil(nb / 1024) consecutive blocks in registers (16-byte
+// loads, all issued before the first is used), one CTA scan, then the runs
+// are rewritten as prefixes.  Also picks the push's chunk size for the new
+// queue: 512 heavy edges per warp chunk, halved (down to 64) while the heavy
+// edges would give fewer than two chunks per push warp, so that a small
+// frontier still spreads over the GPU instead of running as a few long
+// per-warp chains of dependent loads.  Then the loop control, once per
+// iteration: counters, the WHILE condition and the next iteration's mode.
+// phase 0: the prologue's queue (seeded: iteration 0 itself runs in the
+// loop, and always exists: A_0 = V is not empty); phase 1: the queue an
+// iteration built.
+__global__ void __launch_bounds__(kSpineNT)
+    k_q_spine(int4 *part, int nb, gas_counters *cnt, int push_warps, LoopCtl c,
+              int phase, int seeded) {
   const long long now = global_ns();
-  if (threadIdx.x == 0) {
-    const int done = seeded ? 0 : 1;  // iterations run by the prologue
-    cnt->iteration = done;
-    const bool more = seeded ? true : cnt->n_scatter_edges > 0;
-    if (more && done >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
-    cnt->cond = (more && done < cnt->max_iter) ? 1 : 0;
+  const int per = (nb + kSpineNT - 1) / kSpineNT;
+  const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
+  const bool in_regs = per <= kSpineRegs;
+  int4 x[kSpineRegs];
+  int4 sum = make_int4(0, 0, 0, 0);
+  if (in_regs) {
+#pragma unroll
+    for (int k = 0; k < kSpineRegs; ++k)
+      x[k] = b0 + k < b1 ? part[b0 + k] : make_int4(0, 0, 0, 0);
+#pragma unroll
+    for (int k = 0; k < kSpineRegs; ++k) sum = add4(sum, x[k]);
+  } else {
+    for (int b = b0; b < b1; ++b) sum = add4(sum, part[b]);
   }
-  __syncwarp();
-  schedule_next(cnt, c, now);
-  if (threadIdx.x == 0 && c.in_graph) cudaGraphSetConditional(c.h, cnt->cond);
+  // CTA exclusive scan of the four sums
+  __shared__ int4 s_warp[kSpineNT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int4 incl = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int4 o;
+    o.x = __shfl_up_sync(0xffffffffu, incl.x, d);
+    o.y = __shfl_up_sync(0xffffffffu, incl.y, d);
+    o.z = __shfl_up_sync(0xffffffffu, incl.z, d);
+    o.w = __shfl_up_sync(0xffffffffu, incl.w, d);
+    if (lane >= d) incl = add4(incl, o);
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  int4 pre = make_int4(incl.x - sum.x, incl.y - sum.y, incl.z - sum.z, incl.w - sum.w);
+  int4 tot = make_int4(0, 0, 0, 0);
+#pragma unroll 8
+  for (int w = 0; w < kSpineNT / 32; ++w) {
+    const int4 t = s_warp[w];
+    if (w < warp) pre = add4(pre, t);
+    tot = add4(tot, t);
+  }
+  if (in_regs) {
+#pragma unroll
+    for (int k = 0; k < kSpineRegs; ++k) {
+      if (b0 + k < b1) {
+        part[b0 + k] = pre;
+        pre = add4(pre, x[k]);
+      }
+    }
+  } else {
+    for (int b = b0; b < b1; ++b) {
+      const int4 y = part[b];
+      part[b] = pre;
+      pre = add4(pre, y);
+    }
+  }
+  if (threadIdx.x == 0) {
+    cnt->n_changed = tot.x + tot.z;        // queue length (members with out-edges)
+    cnt->n_scatter_edges = tot.y + tot.w;  // their out-edges
+    cnt->q_heavy = tot.x;
+    cnt->q_heavy_edges = tot.y;
+    int cl = gasdev::kSlabChunkLog2;
+    while (cl > gasdev::kSlabChunkMinLog2 && (tot.y >> cl) < 2 * push_warps) --cl;
+    cnt->push_chunk_log2 = cl;
+    const bool edges = tot.y + tot.w > 0;
+    if (phase == 0) {
+      const int done = seeded ? 0 : 1;  // iterations run by the prologue
+      cnt->iteration = done;
+      const bool more = seeded ? true : edges;
+      if (more && done >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
+      cnt->cond = (more && done < cnt->max_iter) ? 1 : 0;
+    } else {
+      *c.fix_n = 0;  // the pull fixup of this iteration has run
+      if (cnt->mode == kModePush)
+        ++cnt->n_push;
+      else
+        ++cnt->n_pull;
+      if (c.trace && cnt->iteration < GAS_TRACE_CAP) c.trace[cnt->iteration].t_end_ns = now;
+      const int it = ++cnt->iteration;
+      if (edges && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
+      cnt->cond = (edges && it < cnt->max_iter) ? 1 : 0;
+    }
+  }
+  if (warp == 0) {
+    __syncwarp();
+    schedule_next(cnt, c, now);
+    if (lane == 0 && c.in_graph) cudaGraphSetConditional(c.h, cnt->cond);
+  }
 }
 
-__global__ void k_fast_cond(gas_counters *cnt, LoopCtl c) {
-  const long long now = global_ns();
-  if (threadIdx.x == 0) {
-    *c.fix_n = 0;  // the pull fixup of this iteration has run
-    if (cnt->mode == kModePush)
-      ++cnt->n_push;
-    else
-      ++cnt->n_pull;
-    if (c.trace && cnt->iteration < GAS_TRACE_CAP) c.trace[cnt->iteration].t_end_ns = now;
-    const int it = ++cnt->iteration;
-    const bool more = cnt->n_scatter_edges > 0;
-    if (more && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
-    cnt->cond = (more && it < cnt->max_iter) ? 1 : 0;
-  }
-  __syncwarp();
-  schedule_next(cnt, c, now);
-  if (threadIdx.x == 0 && c.in_graph) cudaGraphSetConditional(c.h, cnt->cond);
-}
 
 __global__ void k_fast_reset(gas_counters *cnt, int max_iter, int forced,
                              int pull_div) {
@@ -648,15 +712,20 @@ int32_t snap_zero(const gas_engine *e) {
   return e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
 }
 
-gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c) {
-  k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart,
-                                         e->q_ids, e->snap, snap_zero(e), e->cnt);
-  k_q_spine<<<1, kSpineNT, 0, cs>>>(e->qpart, c.n_qblocks, e->cnt, c.push_grid * (kNT / 32));
-  k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, e->qpart,
+// The queue of the changed set, then the loop control (phase as for
+// k_q_spine).
+gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c,
+                        cudaGraphConditionalHandle h, int phase) {
+  int4 *part = reinterpret_cast<int4 *>(e->qpart);
+  int32_t *hist = (e->trace_on || e->sched_model) ? e->hist : nullptr;
+  k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, part, e->q_ids,
+                                         e->snap, snap_zero(e), hist, e->cnt);
+  k_q_spine<<<1, kSpineNT, 0, cs>>>(part, c.n_qblocks, e->cnt, c.push_grid * (kNT / 32),
+                                    loop_ctl(e, h), phase, c.seeded ? 1 : 0);
+  k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, part,
                                          (const int32_t *)e->vd, e->q_ids, e->q_vals,
-                                         e->q_end, e->q_delta, e->snap,
-                                         (e->trace_on || e->sched_model) ? e->hist : nullptr,
-                                         e->slab_qpart, e->cnt);
+                                         e->q_end, e->q_delta, e->snap, e->slab_qpart,
+                                         e->cnt);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -671,7 +740,8 @@ __global__ void k_fill(int32_t *p, int32_t v, int n) {
     p[i] = v;
 }
 
-gas_status_t prologue(gas_engine *e, cudaStream_t cs, void *vctx) {
+gas_status_t prologue(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
+                      void *vctx) {
   const FastCtx &c = *static_cast<const FastCtx *>(vctx);
   k_fill<<<2 * e->num_sms, kNT, 0, cs>>>(e->snap, snap_zero(e), e->nV);
   if (c.seeded) {
@@ -680,7 +750,7 @@ gas_status_t prologue(gas_engine *e, cudaStream_t cs, void *vctx) {
                                                   zero_cap, e->cbits);
     CUDA_TRY(cudaGetLastError());
     gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, cs>>>(dense_csc(e), e->slab_dpart);
-    return compaction(e, cs, c);
+    return compaction(e, cs, c, h, 0);
   }
   // iteration 0: the generic kernels on the caller's active set
   e->level_from_counters = true;
@@ -695,15 +765,15 @@ gas_status_t prologue(gas_engine *e, cudaStream_t cs, void *vctx) {
   CUDA_TRY(cudaGetLastError());
   if (e->prog != GAS_PROG_BFS)  // chunk boundaries of the dense pull
     gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, cs>>>(dense_csc(e), e->slab_dpart);
-  return compaction(e, cs, c);
+  return compaction(e, cs, c, h, 0);
 }
 
 gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
                   void *vctx) {
   const FastCtx &c = *static_cast<const FastCtx *>(vctx);
   const gasdev::SlabSource qsrc = gasdev::slab_source(
-      e->q_end, e->q_ids, e->q_delta, 0, 0, &e->cnt->n_changed,
-      &e->cnt->n_scatter_edges, e->slab_qpart, &e->cnt->push_chunk_log2);
+      e->q_end, e->q_ids, e->q_delta, 0, 0, &e->cnt->q_heavy,
+      &e->cnt->q_heavy_edges, e->slab_qpart, &e->cnt->push_chunk_log2);
   const int grid = c.slab_grid;  // resident CTAs only (persistent warps)
   const int pgrid = c.push_grid;
   const int32_t zero_cap = e->prog == GAS_PROG_SSSP ? INT_MAX - 100000 : INT_MAX;
@@ -746,10 +816,7 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   }
   CUDA_TRY(cudaGetLastError());
   gas::prof_end(e, cs);
-  GAS_TRY(compaction(e, cs, c));
-  k_fast_cond<<<1, 32, 0, cs>>>(e->cnt, loop_ctl(e, h));
-  CUDA_TRY(cudaGetLastError());
-  return GAS_OK;
+  return compaction(e, cs, c, h, 1);
 }
 
 gas_status_t ensure_fast_buffers(gas_engine *e) {
@@ -762,10 +829,8 @@ gas_status_t ensure_fast_buffers(gas_engine *e) {
   CUDA_TRY(cudaMalloc(&e->q_delta, (V ? V : 1) * 4));
   CUDA_TRY(cudaMalloc(&e->snap, (V ? V : 1) * 4));
   CUDA_TRY(cudaMalloc(&e->cbits, (nW ? nW : 1) * 4));
-  CUDA_TRY(cudaMalloc(&e->mbits, (nW ? nW : 1) * 4));
-  CUDA_TRY(cudaMalloc(&e->qpart, 2 * (nqb ? nqb : 1) * 4));
+  CUDA_TRY(cudaMalloc(&e->qpart, (nqb ? nqb : 1) * sizeof(int4)));
   CUDA_TRY(cudaMemset(e->cbits, 0, (nW ? nW : 1) * 4));
-  CUDA_TRY(cudaMemset(e->mbits, 0, (nW ? nW : 1) * 4));
   return GAS_OK;
 }
 
@@ -793,12 +858,7 @@ static gas_status_t build_fast_graph(gas_engine *e, FastCtx *ctx,
   }
   e->capturing = true;
   e->in_graph = true;
-  st = prologue(e, cs, ctx);
-  if (st == GAS_OK) {
-    k_fast_precond<<<1, 32, 0, cs>>>(e->cnt, loop_ctl(e, h), ctx->seeded ? 1 : 0);
-    ce = cudaGetLastError();
-    if (ce != cudaSuccess) st = fail(GAS_ERR_CUDA, "precond: %s", cudaGetErrorString(ce));
-  }
+  st = prologue(e, cs, h, ctx);
   if (st == GAS_OK) {
     cudaStreamCaptureStatus cst;
     const cudaGraphNode_t *d = nullptr;
@@ -891,11 +951,7 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     if (ce == cudaSuccess) {
       e->capturing = true;
       e->in_graph = false;
-      gas_status_t pst = prologue(e, S(stream), &ctx);
-      if (pst == GAS_OK) {
-        k_fast_precond<<<1, 32, 0, S(stream)>>>(e->cnt, loop_ctl(e, 0), ctx.seeded ? 1 : 0);
-        ce = cudaGetLastError();
-      }
+      gas_status_t pst = prologue(e, S(stream), 0, &ctx);
       e->capturing = false;
       if (pst != GAS_OK) return pst;
       if (ce == cudaSuccess) GAS_TRY(run_host_loop(e, body, &ctx, stream));
@@ -916,12 +972,12 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     stats->iterations = c.iteration;
     stats->push_iters = c.n_push;
     stats->pull_iters = c.n_pull;
-    // prologue (gather/apply, fixup, commit | bfs apply; seed; 3 compaction;
-    // precond) + per iteration (push, pull, pull fixup | bfs push;
-    // 3 compaction, which also partitions the next push; cond) + reset +
-    // finish
-    const int pro = e->prog == GAS_PROG_BFS ? 7 : (ctx.seeded ? 7 : 11);
-    const int per = e->prog == GAS_PROG_BFS ? 5 : 7;
+    // prologue (snapshot fill; gather/apply, fixup, commit | bfs apply;
+    // seed; partition of the dense pull; 3 compaction, the last two also
+    // the loop control and the next push's partition) + per iteration
+    // (push, pull, pull fixup | bfs push; 3 compaction) + reset + finish
+    const int pro = e->prog == GAS_PROG_BFS ? 6 : (ctx.seeded ? 6 : 10);
+    const int per = e->prog == GAS_PROG_BFS ? 4 : 6;
     const int loop_iters = ctx.seeded ? c.iteration : (c.iteration > 0 ? c.iteration - 1 : 0);
     stats->kernel_launches = pro + per * loop_iters + 2;
   }

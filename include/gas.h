@@ -490,7 +490,9 @@ typedef struct {
   int32_t pull_div;        /* AUTO pulls when out-edges(C_k)*pull_div > E  */
   int32_t sched;           /* fast runs: 0 auto, 1 push, 2 pull, 3 learned */
   int32_t push_chunk_log2; /* fast runs: edges per push warp chunk (log2)  */
-  int32_t pad[2];
+  int32_t q_heavy;         /* fast runs: queue rows [0, q_heavy) have more */
+                           /* out-edges than a thread takes alone          */
+  int32_t q_heavy_edges;   /* fast runs: out-edges of those rows           */
 } gas_counters;
 
 typedef struct {
