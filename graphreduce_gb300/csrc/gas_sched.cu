@@ -296,6 +296,15 @@ __global__ void __launch_bounds__(kNT, 5)
   }
 }
 
+// Edge-stream load that does not allocate in L1: the edge arrays are read
+// once per iteration, and L1 is kept for the vertex state the pre-checks
+// gather.
+__device__ __forceinline__ int32_t ld_stream(const int32_t *p) {
+  int32_t v;
+  asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // push (SSSP / CC) and BFS push
 // ---------------------------------------------------------------------------
@@ -326,9 +335,9 @@ struct PushPol {
   __device__ __forceinline__ Probe probe(bool valid, int a, int, int pos) const {
     Probe p{0, 0, INT_MIN};
     if (valid) {
-      p.v = __ldg(csr_dst + pos);
+      p.v = ld_stream(csr_dst + pos);
       int cand = __ldg(q_vals + a);
-      if (kWeighted) cand += __ldg(csr_w + pos);
+      if (kWeighted) cand += ld_stream(csr_w + pos);
       p.cand = cand > zero_cap ? zero_cap : cand;
       p.cur = vd[p.v];
     }
@@ -363,7 +372,7 @@ struct BfsPushPol {
   __device__ __forceinline__ Probe probe(bool valid, int, int, int pos) const {
     Probe p{0, false};
     if (valid) {
-      p.v = __ldg(csr_dst + pos);
+      p.v = ld_stream(csr_dst + pos);
       p.unreached = depth[p.v] == -1;
     }
     return p;
@@ -937,6 +946,13 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_push<PushPol<false>>, kNT, 0);
     ctx.push_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);
+    // the pushes use no shared memory: all of the SM's L1/shared storage
+    // as L1 for the state gathers
+    cudaFuncSetAttribute(k_bfs_push, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaFuncSetAttribute(k_push<PushPol<true>>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         0);
+    cudaFuncSetAttribute(k_push<PushPol<false>>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, 0);
   }
   ctx.seeded = e->prog != GAS_PROG_BFS && e->active_full && !e->counts_dirty &&
                e->n_active == e->nV;
