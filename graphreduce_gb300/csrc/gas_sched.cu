@@ -518,40 +518,101 @@ struct LoopCtl {
   int32_t *fix_n;
 };
 
-// Mode of the next iteration (one warp): forced push / pull, the learned
-// head, or the fixed heuristic -- pull when the frontier's out-edges are
-// more than 1/pull_div of all edges.  With tracing, records the iteration.
-__device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now) {
-  const int lane = threadIdx.x & 31;
+// The schedule head's weights (10.5 KB, BF16) staged in shared memory by
+// the spine kernel at its start, while the block totals are still loading.
+constexpr int kSchedW = (int)gaslearn::layout(GAS_SCHED_FEATURES, 2).total;
+struct SchedSmem {
+  __nv_bfloat16 w[kSchedW];
+  float f[GAS_SCHED_FEATURES];
+  float h1[gaslearn::kH];
+  float h2p[4][gaslearn::kH];
+  float h2[gaslearn::kH];
+};
+
+__device__ __forceinline__ void sched_stage_weights(SchedSmem &sm, const __nv_bfloat16 *model) {
+  const uint4 *src = reinterpret_cast<const uint4 *>(model);
+  uint4 *dst = reinterpret_cast<uint4 *>(sm.w);
+  constexpr int kVec = kSchedW * 2 / 16;
+  for (int i = threadIdx.x; i < kVec; i += blockDim.x) dst[i] = src[i];
+  for (int i = kVec * 8 + threadIdx.x; i < kSchedW; i += blockDim.x) sm.w[i] = model[i];
+}
+
+// The head's two logits, evaluated by the whole CTA (at least 256 threads,
+// every thread calls): layer 1 one unit per thread, layer 2 four partial
+// sums per unit, the output layer by warp 0.  FP32 accumulation of the BF16
+// weights; the result is in lg[] of warp 0.
+__device__ __forceinline__ void sched_logits_cta(SchedSmem &sm, float *lg) {
+  constexpr gaslearn::Layout L = gaslearn::layout(GAS_SCHED_FEATURES, 2);
+  constexpr int kH = gaslearn::kH;
+  const int t = threadIdx.x;
+  if (t < kH) {
+    float a = __bfloat162float(sm.w[L.b1 + t]);
+#pragma unroll
+    for (int i = 0; i < GAS_SCHED_FEATURES; ++i) a += sm.f[i] * __bfloat162float(sm.w[L.w1 + i * kH + t]);
+    sm.h1[t] = a > 0.f ? a : 0.f;
+  }
+  __syncthreads();
+  if (t < 4 * kH) {
+    const int j = t % kH, q = t / kH;
+    float a = 0.f;
+#pragma unroll
+    for (int i = q * (kH / 4); i < (q + 1) * (kH / 4); ++i)
+      a += sm.h1[i] * __bfloat162float(sm.w[L.w2 + i * kH + j]);
+    sm.h2p[q][j] = a;
+  }
+  __syncthreads();
+  if (t < kH) {
+    const float a = __bfloat162float(sm.w[L.b2 + t]) + sm.h2p[0][t] + sm.h2p[1][t] +
+                    sm.h2p[2][t] + sm.h2p[3][t];
+    sm.h2[t] = a > 0.f ? a : 0.f;
+  }
+  __syncthreads();
+  if (t < 32) {
+    float o0 = 0.f, o1 = 0.f;
+#pragma unroll
+    for (int j = t; j < kH; j += 32) {
+      o0 += sm.h2[j] * __bfloat162float(sm.w[L.w3 + 2 * j]);
+      o1 += sm.h2[j] * __bfloat162float(sm.w[L.w3 + 2 * j + 1]);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      o0 += __shfl_xor_sync(0xffffffffu, o0, d);
+      o1 += __shfl_xor_sync(0xffffffffu, o1, d);
+    }
+    lg[0] = o0 + __bfloat162float(sm.w[L.b3]);
+    lg[1] = o1 + __bfloat162float(sm.w[L.b3 + 1]);
+  }
+}
+
+// Mode of the next iteration (every thread of the spine CTA calls; the
+// counters of the new queue are written): forced push / pull, the learned
+// head (weights already staged when `learned`), or the fixed heuristic --
+// pull when the frontier's out-edges are more than 1/pull_div of all edges.
+// With tracing, records the iteration.
+__device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now,
+                              SchedSmem &sm, bool learned) {
+  const int t = threadIdx.x;
   const int forced = cnt->sched;  // 0 auto, 1 push, 2 pull, 3 learned
   const int it = cnt->iteration;   // the iteration being scheduled
-  int mode;
-  if (forced == 1) {
-    mode = kModePush;
-  } else if (forced == 2) {
-    mode = kModePull;
-  } else if (forced == 3 && c.model) {
-    // the schedule head's weights (10.5 KB) into shared memory in one round
-    // of independent 16-byte loads, then the warp evaluates from there
-    constexpr int kW = (int)gaslearn::layout(GAS_SCHED_FEATURES, 2).total;
-    __shared__ __align__(16) __nv_bfloat16 s_w[kW];
-    const uint4 *src = reinterpret_cast<const uint4 *>(c.model);
-    uint4 *dst = reinterpret_cast<uint4 *>(s_w);
-    constexpr int kVec = kW * 2 / 16;
-    for (int i = lane; i < kVec; i += 32) dst[i] = src[i];
-    for (int i = kVec * 8 + lane; i < kW; i += 32) s_w[i] = c.model[i];
-    __syncwarp();
-    float f[GAS_SCHED_FEATURES], lg[2];
-    gasfeat::schedule_features(cnt->n_changed, cnt->n_scatter_edges, c.hist, it, c.nV,
-                               c.nE, c.weighted, f);
-    gaslearn::mlp_warp_logits<GAS_SCHED_FEATURES>(s_w, f, lg);
-    mode = lg[1] > lg[0] ? kModePull : kModePush;
-  } else {
-    mode = ((long long)cnt->n_scatter_edges * cnt->pull_div > (long long)c.nE)
-               ? kModePull : kModePush;
+  float lg[2] = {0.f, 0.f};
+  if (learned) {  // CTA-uniform
+    if (t == 0)
+      gasfeat::schedule_features(cnt->n_changed, cnt->n_scatter_edges, c.hist, it, c.nV,
+                                 c.nE, c.weighted, sm.f);
+    __syncthreads();
+    sched_logits_cta(sm, lg);
   }
-  __syncwarp();
-  if (lane == 0) {
+  if (t == 0) {
+    int mode;
+    if (forced == 1)
+      mode = kModePush;
+    else if (forced == 2)
+      mode = kModePull;
+    else if (learned)
+      mode = lg[1] > lg[0] ? kModePull : kModePush;
+    else
+      mode = ((long long)cnt->n_scatter_edges * cnt->pull_div > (long long)c.nE)
+                 ? kModePull : kModePush;
     cnt->mode = mode;
     if (c.trace && it < GAS_TRACE_CAP && cnt->cond) {
       gas_trace_record &r = c.trace[it];
@@ -563,9 +624,10 @@ __device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now
       r.t_start_ns = now;
       r.t_end_ns = 0;
     }
+    if (c.hist)
+      for (int b = 0; b < 8; ++b) c.hist[b] = 0;
+    if (c.in_graph) cudaGraphSetConditional(c.h, cnt->cond);
   }
-  __syncwarp();
-  if (lane < 8 && c.hist) c.hist[lane] = 0;
 }
 
 __device__ __forceinline__ long long global_ns() {
@@ -590,6 +652,9 @@ __global__ void __launch_bounds__(kSpineNT)
     k_q_spine(int4 *part, int nb, gas_counters *cnt, int push_warps, LoopCtl c,
               int phase, int seeded) {
   const long long now = global_ns();
+  __shared__ __align__(16) SchedSmem sm;
+  const bool learned = cnt->sched == 3 && c.model != nullptr;
+  if (learned) sched_stage_weights(sm, c.model);
   const int per = (nb + kSpineNT - 1) / kSpineNT;
   const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
   const bool in_regs = per <= kSpineRegs;
@@ -669,11 +734,8 @@ __global__ void __launch_bounds__(kSpineNT)
       cnt->cond = (edges && it < cnt->max_iter) ? 1 : 0;
     }
   }
-  if (warp == 0) {
-    __syncwarp();
-    schedule_next(cnt, c, now);
-    if (lane == 0 && c.in_graph) cudaGraphSetConditional(c.h, cnt->cond);
-  }
+  __syncthreads();  // the counters above, and the staged weights
+  schedule_next(cnt, c, now, sm, learned);
 }
 
 
