@@ -12,11 +12,20 @@ Metric: GTEPS with the reference's definition (sssp.cu:202-211): for every
 run, the sum of out-degrees of the vertices it reached, divided by time
 (for CC every vertex is reached, so a run counts all its edges).
 
+The engine under test is the learned-schedule, batched one: the 8 SSSP
+sources run as the 8 lanes of one multi-source SSSP launch (per lane
+bit-exact with, and as many iterations as, one run per source; checked
+every time the bench starts), CC runs through the engine with the learned
+schedule.  The same step with one SSSP run per source ("comparisons") and
+the plain fixed-heuristic form ("plain") are timed beside it.
+
   value  -- device-resident: graph and initial vertex states already in HBM,
             timed with CUDA events on the engine's stream.
-  e2e    -- through the public Python API with pinned host buffers: each
-            run uploads its initial vertex data and downloads its result
-            inside the timed region.
+  e2e    -- through the public Python API with pinned host buffers: every
+            input goes up (the CC labels; the SSSP source ids -- the batched
+            run builds its initial distances on the device) and every result
+            comes down (the [V][8] distances, the CC labels) inside the
+            timed region.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -46,14 +55,14 @@ N_SOURCES = 8
 N_ISLANDS, ISLAND_SIDE = 4096, 32
 METRIC = "GTEPS (SSSP x8 + CC, R-MAT scale 22)"
 MAX_ITERS = 20000  # far above any run of this workload; bounds a device loop
-# DRAM bytes (read + write) per launch of the push kernel on this workload
-# (scale 22, learned schedule, edges in HBM): one-pass ncu metrics
-# dram__bytes_read.sum + dram__bytes_write.sum over all 145 k_push launches of
-# one step, captured with
+# Per-launch DRAM bytes (read + write) of the dominant kernel, by (kernel,
+# scale, edge placement, schedule): one-pass ncu metrics over every launch of
+# that kernel in one step, captured with
 #   GAS_HOST_LOOP=1 ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,\
-#     dram__bytes_write.sum --clock-control none -k regex:^k_push$ \
+#     dram__bytes_write.sum --clock-control none --csv --log-file launches.csv \
 #     python bench.py --launch-list --no-cpu-baseline
-PUSH_TRAFFIC_S22 = 208.4e6
+# (k_mss_push: 11 launches, 8.98 GB in all).
+PUSH_TRAFFIC = {("mss_push", 22, "device", "learned"): 816.0e6}
 
 
 def log(*a):
@@ -170,6 +179,7 @@ def run_ours(args, rank, world):
     ssp, sources, ccg = make_workload(args.scale)
     out_sssp = ssp.out_degree()
     out_cc = ccg.out_degree()
+    batched = args.sssp == "batched"
 
     model = None
     if args.schedule == "learned":
@@ -185,7 +195,13 @@ def run_ours(args, rank, world):
     e_s.setGraph(ssp.nV, vd_s, ssp.nE, ssp.weights, ssp.src, ssp.dst, sp)
     vd_c = initial_vertex_data("cc", ccg.nV)
     e_c.setGraph(ccg.nV, vd_c, ccg.nE, None, ccg.src, ccg.dst, sp)
-    log(f"setGraph (host CSR/CSC build + upload) {time.time() - t:.1f}s")
+    bat = None
+    if batched:
+        # the 8 sources as the 8 lanes of one multi-source SSSP run
+        bat = gg.Batch()
+        bat.add_graph(ssp.nV, ssp.src, ssp.dst, ssp.weights)
+        bat.build(sp)
+    log(f"setGraph (CSR/CSC build + upload) {time.time() - t:.1f}s")
     if model is not None:
         e_s.set_schedule_model(model)
         e_c.set_schedule_model(model)
@@ -199,13 +215,21 @@ def run_ours(args, rank, world):
     pin_c = init_c.pin_memory()
     res_s = [torch.empty(ssp.nV, dtype=torch.int32).pin_memory() for _ in sources]
     res_c = torch.empty(ccg.nV, dtype=torch.int32).pin_memory()
+    lane_src = np.asarray(sources, np.int32)[None, :]
+    dist_dev = torch.empty((ssp.nV, len(sources)), dtype=torch.int32, device=dev)
+    dist_pin = torch.empty((ssp.nV, len(sources)), dtype=torch.int32).pin_memory()
     torch.cuda.synchronize()
 
     launches = [0]
     iters = {"sssp": [], "cc": 0}
 
-    def one_step(e2e, schedule=args.schedule):
-        launches[0] = 0
+    def sssp_batched(e2e):
+        r = bat.run(sssp_sources=lane_src, max_sssp_iterations=MAX_ITERS,
+                    dist_out=(dist_pin if e2e else dist_dev).data_ptr(), stream=sp)
+        iters["sssp"] = [int(r.stats.sssp_lane_iterations[k]) for k in range(len(sources))]
+        launches[0] += r.stats.kernel_launches
+
+    def sssp_sequential(e2e, schedule):
         iters["sssp"] = []
         for k in range(len(sources)):
             e_s.upload_vertex_data_ptr(pin_s[k].data_ptr() if e2e else dev_s[k].data_ptr(), sp)
@@ -215,6 +239,13 @@ def run_ours(args, rank, world):
             launches[0] += st.kernel_launches + 1
             if e2e:
                 e_s.download_vertex_data_ptr(res_s[k].data_ptr(), sp)
+
+    def one_step(e2e, schedule=args.schedule, use_batch=batched):
+        launches[0] = 0
+        if use_batch:
+            sssp_batched(e2e)
+        else:
+            sssp_sequential(e2e, schedule)
         e_c.upload_vertex_data_ptr(pin_c.data_ptr() if e2e else dev_c.data_ptr(), sp)
         e_c.setActive(0, ccg.nV, sp)
         st = e_c.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
@@ -232,15 +263,25 @@ def run_ours(args, rank, world):
     # correctness of this exact workload + units per step
     one_step(e2e=True)
     torch.cuda.synchronize()
+    if batched:
+        for k in range(len(sources)):
+            res_s[k].copy_(dist_pin[:, k])
     ev_units = 0
     for k in range(len(sources)):
         ev_units += edges_visited(out_sssp, res_s[k].numpy(), SSSP_GATHER_ZERO)
     ev_units += edges_visited(out_cc, res_c.numpy(), -12345)  # every CC vertex is reached
     first_sssp = res_s[0].numpy().copy()
+    if batched:
+        # the lanes equal one SSSP per source through the engine (bit-exact)
+        one_step(e2e=True, use_batch=False)
+        torch.cuda.synchronize()
+        for k in range(len(sources)):
+            if not np.array_equal(res_s[k].numpy(), dist_pin[:, k].numpy()):
+                raise SystemExit(f"batched SSSP lane {k} differs from the single-source run")
 
-    def timed(e2e, steps, warmup, schedule=args.schedule):
+    def timed(e2e, steps, warmup, schedule=args.schedule, use_batch=batched):
         for _ in range(warmup):
-            one_step(e2e, schedule)
+            one_step(e2e, schedule, use_batch)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -250,7 +291,7 @@ def run_ours(args, rank, world):
         t0 = time.perf_counter()
         start.record(stream)
         for _ in range(steps):
-            one_step(e2e, schedule)
+            one_step(e2e, schedule, use_batch)
         end.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -265,29 +306,43 @@ def run_ours(args, rank, world):
     with ClockSampler(torch.cuda.current_device()) as clk:
         ms_step, _ = timed(False, args.steps, args.warmup)
     clocks = clk.summary()
-    ms_e2e, _ = timed(True, max(1, args.steps), 1)
     launches_per_step = launches[0]
-    plain = None
-    if args.schedule != "auto":
-        # the same step under the fixed heuristic (AUTO), device-resident
-        ms_plain, _ = timed(False, args.steps, args.warmup, "auto")
-        plain = {"schedule": "auto (fixed heuristic)", "ms_per_step": round(ms_plain, 3),
-                 "value": round(world * ev_units / (ms_plain * 1e-3) / 1e9, 4),
-                 "speedup_of_headline": round(ms_plain / ms_step, 4)}
+    iters_step = {"sssp": list(iters["sssp"]), "cc": iters["cc"]}
+    ms_e2e, _ = timed(True, max(1, args.steps), 1)
+    comparisons = {}
+    # the same step with one SSSP run per source (learned schedule), and the
+    # plain form: one run per source under the fixed heuristic (AUTO)
+    if batched:
+        ms_seq, _ = timed(False, args.steps, args.warmup, args.schedule, False)
+        comparisons["sequential_sources"] = {
+            "schedule": args.schedule, "ms_per_step": round(ms_seq, 3),
+            "value": round(world * ev_units / (ms_seq * 1e-3) / 1e9, 4),
+            "speedup_of_headline": round(ms_seq / ms_step, 4)}
+    ms_plain, _ = timed(False, args.steps, args.warmup, "auto", False)
+    plain = {"schedule": "auto (fixed heuristic), one SSSP run per source",
+             "ms_per_step": round(ms_plain, 3),
+             "value": round(world * ev_units / (ms_plain * 1e-3) / 1e9, 4),
+             "speedup_of_headline": round(ms_plain / ms_step, 4)}
 
     value = world * ev_units / (ms_step * 1e-3) / 1e9
     e2e = world * ev_units / (ms_e2e * 1e-3) / 1e9
-    h2d = (len(sources) * ssp.nV + ccg.nV) * 4
-    d2h = h2d
+    if batched:  # sources in, the [V][8] distances and the CC labels out
+        h2d = len(sources) * 4 + ccg.nV * 4
+        d2h = (len(sources) * ssp.nV + ccg.nV) * 4
+    else:
+        h2d = (len(sources) * ssp.nV + ccg.nV) * 4
+        d2h = h2d
 
     # per-algorithm split and the dominant kernel's roofline (untimed pass)
-    split = per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources,
-                           args.schedule, sp, stream)
-    roof = kernel_roofline(e_s, e_c, dev_s, dev_c, ssp, ccg, args.schedule, sp)
-    if (roof["kernel"].startswith("k_push") and args.scale == SCALE and args.edges == "device"
-            and args.schedule in ("learned", "push")):
-        roof["traffic"] = PUSH_TRAFFIC_S22
-        roof["traffic_source"] = "ncu dram bytes per k_push launch, same workload"
+    split = per_algo_split(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, out_sssp, sources,
+                           lane_src, dist_dev, args.schedule, sp, stream)
+    roof = kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev,
+                           args.schedule, sp)
+    traffic = PUSH_TRAFFIC.get((roof["kernel_key"], args.scale, args.edges, args.schedule))
+    if traffic:
+        roof["traffic"] = traffic
+        roof["traffic_source"] = "ncu dram bytes per launch of this kernel, same workload"
+    del roof["kernel_key"]
     peak, peak_kind = measured_peaks()
     roof["peak"] = peak
     roof["frac"] = roof["achieved"] / peak
@@ -299,30 +354,39 @@ def run_ours(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded R-MAT + grid islands; reference datasets unavailable)",
         "config": config_dict(args.scale, {"schedule": args.schedule, "edges": args.edges,
+                                           "sssp": ("8 sources as 8 lanes of one batched "
+                                                    "multi-source run" if batched else
+                                                    "one run per source"),
                                            "edges_visited_per_step": ev_units,
-                                           "iterations": {"sssp": iters["sssp"],
-                                                          "cc": iters["cc"]}}),
+                                           "iterations": iters_step}),
         "e2e": {"value": round(e2e, 4), "unit": "GTEPS", "ms_per_step": round(ms_e2e, 3),
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roof,
         "algos": split,
         "plain": plain,
+        "comparisons": comparisons,
         "clocks": clocks,
     }
     return result, (ssp, sources, out_sssp, first_sssp)
 
 
-def per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources, schedule, sp,
-                   stream):
+def per_algo_split(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, out_sssp, sources, lane_src,
+                   dist_dev, schedule, sp, stream):
     import torch
     out = {}
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)
     host = np.empty(ssp.nV, np.int32)
+    ev = 0
+    for k in range(len(sources)):
+        e_s.upload_vertex_data_ptr(dev_s[k].data_ptr(), sp)
+        e_s.setActive(0, ssp.nV, sp)
+        e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
+        e_s.download_vertex_data(host, sp)
+        ev += edges_visited(out_sssp, host, 2**31 - 1 - 100000)
     torch.cuda.synchronize()
     a.record(stream)
-    ev = 0
     its = []
     for k in range(len(sources)):
         e_s.upload_vertex_data_ptr(dev_s[k].data_ptr(), sp)
@@ -331,14 +395,19 @@ def per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources, 
     b.record(stream)
     torch.cuda.synchronize()
     ms = a.elapsed_time(b)
-    for k in range(len(sources)):
-        e_s.upload_vertex_data_ptr(dev_s[k].data_ptr(), sp)
-        e_s.setActive(0, ssp.nV, sp)
-        e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
-        e_s.download_vertex_data(host, sp)
-        ev += edges_visited(out_sssp, host, 2**31 - 1 - 100000)
-    out["sssp"] = {"ms_per_source": round(ms / len(sources), 3),
-                   "gteps": round(ev / (ms * 1e-3) / 1e9, 4), "iterations": its}
+    out["sssp_sequential"] = {"ms_per_source": round(ms / len(sources), 3),
+                              "gteps": round(ev / (ms * 1e-3) / 1e9, 4), "iterations": its}
+    if bat is not None:
+        a.record(stream)
+        r = bat.run(sssp_sources=lane_src, max_sssp_iterations=MAX_ITERS,
+                    dist_out=dist_dev.data_ptr(), stream=sp)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        out["sssp_batched"] = {"ms_8_sources": round(ms, 3),
+                               "gteps": round(ev / (ms * 1e-3) / 1e9, 4),
+                               "iterations": r.stats.sssp_iterations,
+                               "union_edges_pushed": int(r.stats.sssp_edges)}
     a.record(stream)
     e_c.upload_vertex_data_ptr(dev_c.data_ptr(), sp)
     e_c.setActive(0, ccg.nV, sp)
@@ -351,38 +420,63 @@ def per_algo_split(e_s, e_c, dev_s, dev_c, ssp, ccg, out_sssp, out_cc, sources, 
     return out
 
 
-def kernel_roofline(e_s, e_c, dev_s, dev_c, ssp, ccg, schedule, sp):
-    """One extra pass of the step's runs with kernel profiling on: the engine
-    brackets every push / dense-pull launch with CUDA events on the run's
-    stream and accumulates its algorithmic bytes (per edge: index, weight for
-    SSSP, and the state or membership word it reads; per frontier entry or
-    row: 16 B).  The dominant kernel is the one with the larger total time."""
+def kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev, schedule, sp):
+    """One extra pass of the step's runs with kernel profiling on: the
+    engines bracket every push / dense-pull launch (and the batch every
+    multi-source SSSP push) with CUDA events on the run's stream and
+    accumulate its algorithmic bytes (per edge: index, weight for SSSP, and
+    the state, row or membership word it reads; per frontier entry or row:
+    its offsets and state).  The dominant kernel is the one with the largest
+    total time."""
     import torch
-    for e in (e_s, e_c):
-        e.set_profiling(True)
-        e.profile(reset=True)
-    for k in range(len(dev_s)):
-        e_s.upload_vertex_data_ptr(dev_s[k].data_ptr(), sp)
-        e_s.setActive(0, ssp.nV, sp)
-        e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
+    kinds = {}
+
+    def add(key, p, name):
+        ms, by, n = (getattr(p, f"{name}_ms"), getattr(p, f"{name}_bytes"),
+                     getattr(p, f"{name}_launches"))
+        k = kinds.setdefault(key, {"ms": 0.0, "bytes": 0, "launches": 0})
+        k["ms"] += ms
+        k["bytes"] += by
+        k["launches"] += n
+
+    if bat is None:  # one SSSP run per source through the engine
+        e_s.set_profiling(True)
+        e_s.profile(reset=True)
+        for k in range(len(dev_s)):
+            e_s.upload_vertex_data_ptr(dev_s[k].data_ptr(), sp)
+            e_s.setActive(0, ssp.nV, sp)
+            e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
+        torch.cuda.synchronize()
+        ps = e_s.profile()
+        e_s.set_profiling(False)
+        add("push", ps, "push")
+        add("pull", ps, "pull")
+    e_c.set_profiling(True)
+    e_c.profile(reset=True)
     e_c.upload_vertex_data_ptr(dev_c.data_ptr(), sp)
     e_c.setActive(0, ccg.nV, sp)
     e_c.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
     torch.cuda.synchronize()
-    ps, pc = e_s.profile(), e_c.profile()
-    for e in (e_s, e_c):
-        e.set_profiling(False)
-    kinds = {}
-    for name in ("push", "pull"):
-        ms = getattr(ps, f"{name}_ms") + getattr(pc, f"{name}_ms")
-        by = getattr(ps, f"{name}_bytes") + getattr(pc, f"{name}_bytes")
-        n = getattr(ps, f"{name}_launches") + getattr(pc, f"{name}_launches")
-        kinds[name] = {"ms": ms, "bytes": by, "launches": n,
-                       "achieved_gbs": (by / (ms * 1e-3) / 1e9) if ms > 0 else 0.0}
+    pc = e_c.profile()
+    e_c.set_profiling(False)
+    add("push", pc, "push")
+    add("pull", pc, "pull")
+    if bat is not None:
+        bat.set_profiling(True)
+        bat.profile(reset=True)
+        bat.run(sssp_sources=lane_src, max_sssp_iterations=MAX_ITERS,
+                dist_out=dist_dev.data_ptr(), stream=sp)
+        torch.cuda.synchronize()
+        add("mss_push", bat.profile(), "push")
+        bat.set_profiling(False)
+    for k in kinds.values():
+        k["achieved_gbs"] = (k["bytes"] / (k["ms"] * 1e-3) / 1e9) if k["ms"] > 0 else 0.0
     dom = max(kinds, key=lambda k: kinds[k]["ms"])
     d = kinds[dom]
-    return {"kernel": {"pull": "k_pull (dense pull, warp-slab)",
-                       "push": "k_push (frontier push, warp-slab)"}[dom],
+    return {"kernel": {"pull": "k_pull (CC dense pull, warp-slab)",
+                       "push": "k_push (frontier push, warp-slab)",
+                       "mss_push": "k_mss_push (8-lane multi-source SSSP push, warp-slab)"}[dom],
+            "kernel_key": dom,
             "bound": "hbm", "achieved": round(d["achieved_gbs"], 1), "unit": "GB/s",
             "traffic": None, "launches": d["launches"],
             "algorithmic_bytes_per_launch": int(d["bytes"] / max(1, d["launches"])),
@@ -766,6 +860,8 @@ def main():
     ap.add_argument("--pr-check", action="store_true",
                     help="compare with the FP64 oracle (single-threaded C, slow)")
     ap.add_argument("--batch-graphs", type=int, default=BATCH_GRAPHS)
+    ap.add_argument("--sssp", default="batched", choices=["batched", "sequential"],
+                    help="the 8 SSSP sources as lanes of one batched run, or one run each")
     ap.add_argument("--launch-list", action="store_true",
                     help="run one device-resident step only (profiling)")
     args = ap.parse_args()

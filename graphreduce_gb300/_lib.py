@@ -81,14 +81,16 @@ class BatchJob(C.Structure):
     _fields_ = [("bfs_lanes", c_i32), ("bfs_sources", c_vp), ("ppr_lanes", c_i32),
                 ("ppr_seeds", c_vp), ("damping", c_dbl), ("tol", c_dbl),
                 ("max_bfs_levels", c_i32), ("max_ppr_iterations", c_i32),
-                ("piece_edges", c_i32)]
+                ("piece_edges", c_i32), ("sssp_lanes", c_i32), ("sssp_sources", c_vp),
+                ("max_sssp_iterations", c_i32)]
 
 
 class BatchStats(C.Structure):
     _fields_ = [("bfs_iterations", c_i32), ("ppr_iterations", c_i32), ("bfs_edges", c_i64),
                 ("ppr_residual", c_dbl), ("piece_edges", c_i32), ("kernel_launches", c_i32),
-                ("graph_launches", c_i32), ("pad", c_i32),
-                ("ppr_lane_residual", c_dbl * GAS_BATCH_MAX_LANES)]
+                ("graph_launches", c_i32), ("sssp_iterations", c_i32),
+                ("ppr_lane_residual", c_dbl * GAS_BATCH_MAX_LANES), ("sssp_edges", c_i64),
+                ("sssp_lane_iterations", c_i32 * GAS_BATCH_MAX_LANES)]
 
 
 # name -> (restype, argtypes); restype "status" means gas_status_t checked.
@@ -160,13 +162,17 @@ _SIGS = {
     "gas_batch_create": ("status", [C.POINTER(c_vp)]),
     "gas_batch_destroy": (None, [c_vp]),
     "gas_batch_add_graph": ("status", [c_vp, c_i32, c_i64, c_vp, c_vp, C.POINTER(c_i32)]),
+    "gas_batch_add_graph_weighted": ("status", [c_vp, c_i32, c_i64, c_vp, c_vp, c_vp,
+                                                C.POINTER(c_i32)]),
     "gas_batch_build": ("status", [c_vp, c_vp]),
     "gas_batch_num_graphs": (c_i32, [c_vp]),
     "gas_batch_num_vertices": (c_i32, [c_vp]),
     "gas_batch_num_edges": (c_i64, [c_vp]),
     "gas_batch_vertex_offset": (c_i32, [c_vp, c_i32]),
-    "gas_batch_run": ("status", [c_vp, C.POINTER(BatchJob), c_vp, c_vp,
+    "gas_batch_run": ("status", [c_vp, C.POINTER(BatchJob), c_vp, c_vp, c_vp,
                                  C.POINTER(BatchStats), c_vp]),
+    "gas_batch_set_profiling": ("status", [c_vp, c_i32]),
+    "gas_batch_get_profile": ("status", [c_vp, C.POINTER(KernelProfile), c_i32]),
     "gas_batch_tune": ("status", [c_vp, c_i32, c_dbl, c_i32, C.POINTER(c_i32),
                                   C.POINTER(C.c_float), c_vp]),
     "gas_engine_set_edge_placement": ("status", [c_vp, c_i32]),

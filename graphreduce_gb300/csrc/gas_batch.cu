@@ -13,6 +13,16 @@
 //     depth[v][l] for every new lane, folds the lanes into visited and
 //     builds the next queue (vertex, lane mask, inclusive out-edge ends).
 //     Depths equal those of one BFS per source.
+//   * multi-source SSSP (integer weights, unweighted graphs count 1 per
+//     edge): dist[v][l] rows of LS = L rounded up to 4 lanes, cmask[v] the
+//     lanes of v that changed in the current iteration.  One bulk-synchronous
+//     iteration pushes every queued vertex's changed lanes along its
+//     out-edges: the destination's whole row is read once (16-byte loads)
+//     for all lanes, a lane improves with atomicMin when its candidate is
+//     below the value read, and the improved lanes go into cmask (atomicOr,
+//     the first marking the vertex as touched).  The compaction snapshots
+//     each queued vertex's row.  Per lane, distances and iteration counts
+//     equal those of one SSSP per source.
 //   * multi-seed personalized PageRank, r_l = (1-d) e_{s_l} + d A^T D^-1 r_l
 //     for every lane l at once: ranks and contributions are [V][L] rows, so
 //     the L lanes of an in-edge's source are one contiguous 4L-byte read.
@@ -23,8 +33,8 @@
 //     pass folds in piece order.  The sums are deterministic.  The loop runs
 //     until the largest per-lane FP64 L1 residual is <= tol.
 //
-// Both loops are WHILE nodes of one CUDA graph (BFS loop, then PPR loop),
-// each preceded by its prologue; a run is one cudaGraphLaunch.
+// The loops are WHILE nodes of one CUDA graph (BFS, SSSP, then PPR), each
+// preceded by its prologue; a run is one cudaGraphLaunch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,6 +67,8 @@ struct BatchParams {
   int32_t bfs_max_iter;
   int32_t ppr_max_iter;
   int32_t n_sources;  // G * bfs_lanes
+  int32_t sssp_max_iter;
+  int32_t n_sssp_sources;  // G * sssp_lanes
   int32_t pad;
 };
 
@@ -101,7 +113,8 @@ __global__ void k_b_reset(gas_counters *cnt, const BatchParams *prm, int which,
   cnt->cond = 0;
   cnt->n_changed = 0;
   cnt->n_scatter_edges = 0;
-  cnt->max_iter = which == 0 ? prm->bfs_max_iter : prm->ppr_max_iter;
+  cnt->max_iter = which == 0 ? prm->bfs_max_iter
+                 : which == 1 ? prm->ppr_max_iter : prm->sssp_max_iter;
   if (edges) *edges = 0ull;
 }
 
@@ -179,7 +192,7 @@ __device__ __forceinline__ void ms_load(const uint32_t *tbits, const uint32_t *n
     w.deg[i] = 0;
     if ((word >> lane) & 1u) {
       const int v = (w0 + i) * 32 + lane;
-      w.nw[i] = next[v] & ~visited[v];
+      w.nw[i] = visited ? next[v] & ~visited[v] : next[v];
       w.off[i] = csr_off[v];
       w.deg[i] = csr_off[v + 1] - w.off[i];
     }
@@ -331,6 +344,242 @@ __global__ void k_ms_precond(gas_counters *cnt, unsigned long long *edges,
 __global__ void k_ms_cond(gas_counters *cnt, unsigned long long *edges,
                           cudaGraphConditionalHandle h, int in_graph) {
   const int it = ++cnt->iteration;
+  set_cond(cnt, cnt->n_scatter_edges > 0, it, h, in_graph);
+  if (cnt->cond) *edges += (unsigned long long)cnt->n_scatter_edges;
+}
+
+// ---------------------------------------------------------------------------
+// multi-source SSSP
+// ---------------------------------------------------------------------------
+constexpr int32_t kSsspInf = INT_MAX - 100000;  // the SSSP Program's gatherZero
+
+struct MssPushPol {
+  typedef int32_t Val;
+  static constexpr bool kMapNeedsVertex = false;
+  const int32_t *csr_dst;
+  const int32_t *csr_w;   // null: every edge weighs 1
+  const int32_t *q_mask;  // [queue] lanes that changed
+  const int32_t *q_vals;  // [queue][LS] row at the end of the last iteration
+  int32_t *dist;          // [V][LS]
+  uint32_t *cmask;        // [V] lanes changed in this iteration
+  uint32_t *tbits;
+  int LS;
+  __device__ Val zero() const { return 0; }
+  __device__ Val reduce(Val a, Val) const { return a; }
+  __device__ Val map(int, int, int) const { return 0; }
+  __device__ void emit(int, int, Val) const {}
+  // The row read is a plain load: a value it returns was held by the lane
+  // during this iteration, so a candidate below it lowers the lane's final
+  // value under its start value (the lane changed) and a candidate at or
+  // above it cannot lower the final value.
+  __device__ __forceinline__ void visit(int a, int, int pos) const {
+    const int v = __ldg(csr_dst + pos);
+    const long long w = csr_w ? __ldg(csr_w + pos) : 1;
+    const uint32_t m = (uint32_t)__ldg(q_mask + a);
+    const int4 *cur4 = reinterpret_cast<const int4 *>(dist + (size_t)v * LS);
+    const int4 *qv4 = reinterpret_cast<const int4 *>(q_vals + (size_t)a * LS);
+    int32_t *row = dist + (size_t)v * LS;
+    uint32_t nb = 0u;
+    for (int c = 0; c < (LS >> 2); ++c) {
+      const uint32_t mc = (m >> (4 * c)) & 0xFu;
+      if (!mc) continue;
+      const int4 cu = cur4[c];
+      const int4 qv = __ldg(qv4 + c);
+      const int cur[4] = {cu.x, cu.y, cu.z, cu.w};
+      const int val[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (!((mc >> k) & 1u)) continue;
+        const long long cl = (long long)val[k] + w;
+        const int cand = cl > kSsspInf ? kSsspInf : (int)cl;
+        if (cand < cur[k]) {
+          atomicMin(row + 4 * c + k, cand);
+          nb |= 1u << (4 * c + k);
+        }
+      }
+    }
+    if (nb && (cmask[v] & nb) != nb) {
+      const uint32_t old = atomicOr(cmask + v, nb);
+      if (old == 0u) atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
+    }
+  }
+};
+
+// Rows of at most 8 lanes (NC = 1 or 2 16-byte chunks): the same push split
+// into probe (the edge's loads and the destination row) and commit, so that
+// both slabs' row reads are in flight before either slab's updates.  Every
+// lane of the row is tried, not only the changed ones: a lane of u that did
+// not change in the last iteration already pushed its value along this edge
+// when it last changed, so its candidate is at or above the destination's
+// value at the start of this iteration (and of any value read during it)
+// and changes nothing.  Weights are at most 100000, as the SSSP Program's
+// gatherZero assumes, so val + w does not overflow.
+template <int NC>
+struct MssPushPolStaged {
+  typedef int32_t Val;
+  static constexpr bool kMapNeedsVertex = false;
+  const int32_t *csr_dst;
+  const int32_t *csr_w;
+  const int32_t *q_vals;
+  int32_t *dist;
+  uint32_t *cmask;
+  uint32_t *tbits;
+  __device__ Val zero() const { return 0; }
+  __device__ Val reduce(Val a, Val) const { return a; }
+  __device__ Val map(int, int, int) const { return 0; }
+  __device__ void emit(int, int, Val) const {}
+  struct Probe {
+    int v, w, a;  // v < 0: no edge
+    int4 cur[NC];
+  };
+  __device__ __forceinline__ Probe probe(bool valid, int a, int, int pos) const {
+    Probe p;
+    p.v = -1;
+    p.w = 0;
+    p.a = a;
+    if (valid) {
+      p.v = __ldg(csr_dst + pos);
+      p.w = csr_w ? __ldg(csr_w + pos) : 1;
+      const int4 *cur4 = reinterpret_cast<const int4 *>(dist + (size_t)p.v * (4 * NC));
+#pragma unroll
+      for (int c = 0; c < NC; ++c) p.cur[c] = cur4[c];
+    }
+    return p;
+  }
+  __device__ __forceinline__ void commit(const Probe &p) const {
+    if (p.v < 0) return;
+    const int4 *qv4 = reinterpret_cast<const int4 *>(q_vals + (size_t)p.a * (4 * NC));
+    int32_t *row = dist + (size_t)p.v * (4 * NC);
+    uint32_t nb = 0u;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const int4 qv = __ldg(qv4 + c);
+      const int cur[4] = {p.cur[c].x, p.cur[c].y, p.cur[c].z, p.cur[c].w};
+      const int val[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int cand = min(val[k] + p.w, kSsspInf);
+        if (cand < cur[k]) {
+          atomicMin(row + 4 * c + k, cand);
+          nb |= 1u << (4 * c + k);
+        }
+      }
+    }
+    if (nb && (cmask[p.v] & nb) != nb) {
+      const uint32_t old = atomicOr(cmask + p.v, nb);
+      if (old == 0u) atomicOr(tbits + ((uint32_t)p.v >> 5), 1u << (p.v & 31));
+    }
+  }
+};
+
+template <class Pol>
+__global__ void __launch_bounds__(kNT) k_mss_push(Pol pol, gasdev::SlabSource src) {
+  gasdev::slab_loop<Pol, false>(pol, src, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+__global__ void k_mss_init(int32_t *dist, size_t n, uint32_t *lanes_active,
+                           int32_t *lane_rounds) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    dist[k] = kSsspInf;
+  if (blockIdx.x == 0 && threadIdx.x < kMaxLanes) {
+    lane_rounds[threadIdx.x] = 0;
+    if (threadIdx.x == 0) *lanes_active = 0u;
+  }
+}
+
+// Iteration 0: every (graph, lane) source gets distance 0 and is changed.
+__global__ void k_mss_seed(const int32_t *src_global, const BatchParams *prm, int L, int LS,
+                           int32_t *dist, uint32_t *cmask, uint32_t *tbits) {
+  const int n = prm->n_sssp_sources;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int v = src_global[i];
+    if (v < 0) continue;
+    dist[(size_t)v * LS + i % L] = 0;
+    atomicOr(cmask + v, 1u << (i % L));
+    atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
+  }
+}
+
+// Pass 2 of the compaction: the next queue (vertex, changed lanes, snapshot
+// row, inclusive out-edge ends) and the lanes it holds; clears cmask and the
+// touched bitmap.
+__global__ void __launch_bounds__(kNT, 4)
+    k_mss_write(uint32_t *tbits, uint32_t *cmask, const int32_t *csr_off, int nW,
+                const int32_t *part, int LS, const int32_t *dist, int32_t *q_ids,
+                int32_t *q_mask, int32_t *q_vals, int32_t *q_end, int32_t *q_delta,
+                int32_t *chunk_row, uint32_t *lanes_active) {
+  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
+  __shared__ uint32_t s_lanes;
+  if (threadIdx.x == 0) s_lanes = 0u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
+  MsWarp w;
+  ms_load(tbits, cmask, nullptr, csr_off, nW, w0, w);
+  int q, d;
+  ms_totals(w, q, d);
+  if (lane == 0) {
+    s_q[warp] = q;
+    s_d[warp] = d;
+  }
+  __syncthreads();
+  int bq = part[2 * blockIdx.x], bd = part[2 * blockIdx.x + 1];
+  for (int k = 0; k < warp; ++k) {
+    bq += s_q[k];
+    bd += s_d[k];
+  }
+  if (w.myword) tbits[w0 + lane] = 0u;
+  uint32_t lanes = 0u;
+#pragma unroll
+  for (int i = 0; i < kMsWarpWords; ++i) {
+    const int v = (w0 + i) * 32 + lane;
+    const uint32_t word = __shfl_sync(0xffffffffu, w.myword, i);
+    if (!word) continue;  // warp-uniform
+    if ((word >> lane) & 1u) cmask[v] = 0u;
+    const uint32_t nw = w.nw[i];
+    const int deg = nw ? w.deg[i] : 0;
+    const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
+    if (!qb) continue;
+    int incl = deg;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (deg > 0) {
+      const int pos = bq + __popc(qb & ((1u << lane) - 1u));
+      const int end = bd + incl;
+      lanes |= nw;
+      q_ids[pos] = v;
+      q_mask[pos] = (int32_t)nw;
+      q_end[pos] = end;
+      q_delta[pos] = w.off[i] - (end - deg);
+      const int4 *src4 = reinterpret_cast<const int4 *>(dist + (size_t)v * LS);
+      int4 *dst4 = reinterpret_cast<int4 *>(q_vals + (size_t)pos * LS);
+      for (int c = 0; c < (LS >> 2); ++c) dst4[c] = src4[c];
+      for (int c = (end - deg + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk;
+           c * gasdev::kSlabChunk < end; ++c)
+        chunk_row[c] = pos;
+    }
+    bq += __popc(qb);
+    bd += __shfl_sync(0xffffffffu, incl, 31);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lanes |= __shfl_xor_sync(0xffffffffu, lanes, o);
+  if (lane == 0 && lanes) atomicOr(&s_lanes, lanes);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_lanes) atomicOr(lanes_active, s_lanes);
+}
+
+// Loop condition; every lane in the new queue has one more push to run.
+__global__ void k_mss_cond(gas_counters *cnt, unsigned long long *edges,
+                           uint32_t *lanes_active, int32_t *lane_rounds,
+                           cudaGraphConditionalHandle h, int in_graph, int first) {
+  const uint32_t la = *lanes_active;
+  *lanes_active = 0u;
+  for (int l = 0; l < kMaxLanes; ++l)
+    if ((la >> l) & 1u) ++lane_rounds[l];
+  const int it = first ? 0 : ++cnt->iteration;
   set_cond(cnt, cnt->n_scatter_edges > 0, it, h, in_graph);
   if (cnt->cond) *edges += (unsigned long long)cnt->n_scatter_edges;
 }
@@ -558,11 +807,13 @@ __global__ void k_ppr_precond(gas_counters *cnt, cudaGraphConditionalHandle h, i
 struct gas_batch {
   std::vector<int32_t> v_off{0};  // first vertex of every graph; back() = V
   std::vector<int32_t> src, dst;  // union edge list (global ids) until built
+  std::vector<int32_t> w;         // its weights, once a weighted graph came
+  bool weighted = false;
   int64_t n_edges = 0;
   gas_engine *eng = nullptr;      // holds the union graph (CSR + CSC)
   bool built = false;
-  gas_counters *cnt = nullptr;    // [2] device: BFS loop, PPR loop
-  gas_counters *h_cnt = nullptr;  // [2] pinned
+  gas_counters *cnt = nullptr;    // [3] device: BFS loop, PPR loop, SSSP loop
+  gas_counters *h_cnt = nullptr;  // [3] pinned
   BatchParams *prm = nullptr;     // device
   unsigned long long *edges = nullptr;  // BFS edges pushed
   double *resid = nullptr;        // [1 + 32] max and per-lane PPR residual
@@ -571,6 +822,15 @@ struct gas_batch {
   int32_t *depth = nullptr, *q_ids = nullptr, *q_mask = nullptr, *q_end = nullptr,
           *q_delta = nullptr, *part = nullptr, *qpart = nullptr, *srcs = nullptr;
   int32_t depth_lanes = 0, srcs_cap = 0;
+  // SSSP (shares the frontier arrays above; next is the changed-lane mask)
+  int32_t *dist = nullptr, *q_vals = nullptr, *sssp_srcs = nullptr, *lane_rounds = nullptr;
+  uint32_t *lanes_active = nullptr;
+  unsigned long long *sssp_edges = nullptr;
+  int32_t dist_ls = 0, sssp_srcs_cap = 0;
+  // profiling of the SSSP pushes (direct launches, events around each push)
+  bool profiling = false;
+  cudaEvent_t pev[2] = {nullptr, nullptr};
+  gas_kernel_profile prof{};
   // PPR
   int32_t *first_row = nullptr, *fix = nullptr;
   CVal *head = nullptr, *tail = nullptr;
@@ -581,7 +841,7 @@ struct gas_batch {
   int32_t tuned_piece = 0;
   // cached graph
   cudaGraphExec_t graph = nullptr;
-  int32_t g_bfs_lanes = -1, g_ppr_lanes = -1, g_piece = -1;
+  int32_t g_bfs_lanes = -1, g_ppr_lanes = -1, g_piece = -1, g_sssp_lanes = -1;
 };
 
 namespace {
@@ -595,7 +855,7 @@ void bfree(T *&p) {
 void drop_graph(gas_batch *b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
-  b->g_bfs_lanes = b->g_ppr_lanes = b->g_piece = -1;
+  b->g_bfs_lanes = b->g_ppr_lanes = b->g_piece = b->g_sssp_lanes = -1;
 }
 
 void free_state(gas_batch *b) {
@@ -605,6 +865,9 @@ void free_state(gas_batch *b) {
   bfree(b->part); bfree(b->qpart); bfree(b->srcs);
   bfree(b->first_row); bfree(b->fix); bfree(b->head); bfree(b->tail);
   bfree(b->seed_mask); bfree(b->l1);
+  bfree(b->dist); bfree(b->q_vals); bfree(b->sssp_srcs); bfree(b->lane_rounds);
+  bfree(b->lanes_active);
+  b->dist_ls = b->sssp_srcs_cap = 0;
   for (int i = 0; i < 2; ++i) { bfree(b->rank[i]); bfree(b->contrib[i]); }
   b->n_pieces = b->n_fix = b->n_split = b->piece_edges = b->ppr_lanes = b->depth_lanes = 0;
   b->srcs_cap = b->l1_cap = 0;
@@ -621,11 +884,12 @@ int ms_blocks(const gas_batch *b) {
   return std::max(1, (nwords(b) + kMsBlockWords - 1) / kMsBlockWords);
 }
 
-gas_status_t ensure_bfs(gas_batch *b, int lanes, int n_sources) {
+// The frontier arrays the BFS and SSSP loops share (they run one after the
+// other, each prologue resetting them).
+gas_status_t ensure_frontier(gas_batch *b) {
   gas_engine *e = b->eng;
   const size_t nV = std::max(1, e->nV), nW = std::max(1, nwords(b));
-  if (!b->visited) {
-    CUDA_TRY(cudaMalloc(&b->visited, nV * 4));
+  if (!b->next) {
     CUDA_TRY(cudaMalloc(&b->next, nV * 4));
     CUDA_TRY(cudaMalloc(&b->tbits, nW * 4));
     for (int32_t **p : {&b->q_ids, &b->q_mask, &b->q_end, &b->q_delta})
@@ -633,6 +897,40 @@ gas_status_t ensure_bfs(gas_batch *b, int lanes, int n_sources) {
     CUDA_TRY(cudaMalloc(&b->part, ((size_t)e->nE / gasdev::kSlabChunk + 2) * 4));
     CUDA_TRY(cudaMalloc(&b->qpart, 2 * ((size_t)ms_blocks(b) + 1) * 4));
   }
+  return GAS_OK;
+}
+
+gas_status_t ensure_sssp(gas_batch *b, int lanes, int n_sources) {
+  gas_engine *e = b->eng;
+  const size_t nV = std::max(1, e->nV);
+  GAS_TRY(ensure_frontier(b));
+  const int LS = (lanes + 3) & ~3;
+  if (b->dist_ls != LS) {
+    drop_graph(b);
+    bfree(b->dist);
+    bfree(b->q_vals);
+    CUDA_TRY(cudaMalloc(&b->dist, nV * LS * 4));
+    CUDA_TRY(cudaMalloc(&b->q_vals, nV * LS * 4));
+    b->dist_ls = LS;
+  }
+  if (!b->lane_rounds) {
+    CUDA_TRY(cudaMalloc(&b->lane_rounds, kMaxLanes * 4));
+    CUDA_TRY(cudaMalloc(&b->lanes_active, 4));
+  }
+  if (b->sssp_srcs_cap < n_sources) {
+    drop_graph(b);
+    bfree(b->sssp_srcs);
+    CUDA_TRY(cudaMalloc(&b->sssp_srcs, (size_t)std::max(1, n_sources) * 4));
+    b->sssp_srcs_cap = n_sources;
+  }
+  return GAS_OK;
+}
+
+gas_status_t ensure_bfs(gas_batch *b, int lanes, int n_sources) {
+  gas_engine *e = b->eng;
+  const size_t nV = std::max(1, e->nV);
+  GAS_TRY(ensure_frontier(b));
+  if (!b->visited) CUDA_TRY(cudaMalloc(&b->visited, nV * 4));
   if (b->depth_lanes != lanes) {
     drop_graph(b);
     bfree(b->depth);
@@ -716,8 +1014,8 @@ gas_status_t ensure_ppr(gas_batch *b, int lanes, int P, int grid_pieces, int gri
 
 struct RunCtx {
   gas_batch *b;
-  int bfs_lanes, ppr_lanes;
-  int slab_grid, grid_pieces, grid_fix;
+  int bfs_lanes, ppr_lanes, sssp_lanes;
+  int slab_grid, grid_pieces, grid_fix, sssp_grid;
   PprArgs ppr;
 };
 
@@ -786,6 +1084,89 @@ gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, i
                                c->bfs_lanes, b->cnt, 1, b->depth, b->q_ids, b->q_mask,
                                b->q_end, b->q_delta, b->part);
   k_ms_cond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t sssp_compact(RunCtx *c, cudaStream_t s) {
+  gas_batch *b = c->b;
+  gas_engine *e = b->eng;
+  const int nb = ms_blocks(b);
+  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, nullptr, e->csr_off, nwords(b), b->qpart);
+  k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt + 2);
+  k_mss_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, e->csr_off, nwords(b), b->qpart,
+                                 b->dist_ls, b->dist, b->q_ids, b->q_mask, b->q_vals, b->q_end,
+                                 b->q_delta, b->part, b->lanes_active);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t sssp_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
+  gas_batch *b = c->b;
+  gas_engine *e = b->eng;
+  const size_t nV = std::max(1, e->nV), nW = std::max(1, nwords(b));
+  k_b_reset<<<1, 1, 0, s>>>(b->cnt + 2, b->prm, 2, b->sssp_edges);
+  CUDA_TRY(cudaMemsetAsync(b->next, 0, nV * 4, s));
+  CUDA_TRY(cudaMemsetAsync(b->tbits, 0, nW * 4, s));
+  k_mss_init<<<8 * e->num_sms, 256, 0, s>>>(b->dist, nV * b->dist_ls, b->lanes_active,
+                                           b->lane_rounds);
+  k_mss_seed<<<2 * e->num_sms, 256, 0, s>>>(b->sssp_srcs, b->prm, c->sssp_lanes, b->dist_ls,
+                                           b->dist, b->next, b->tbits);
+  GAS_TRY(sssp_compact(c, s));
+  k_mss_cond<<<1, 1, 0, s>>>(b->cnt + 2, b->sssp_edges, b->lanes_active, b->lane_rounds, h, ig,
+                             1);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t sssp_push(RunCtx *c, cudaStream_t s) {
+  gas_batch *b = c->b;
+  gas_engine *e = b->eng;
+  const gasdev::SlabSource q = gasdev::slab_source(
+      b->q_end, b->q_ids, b->q_delta, 0, 0, &b->cnt[2].n_changed, &b->cnt[2].n_scatter_edges,
+      b->part);
+  const int32_t *w = b->weighted ? (const int32_t *)e->csr_ed : nullptr;
+  if (b->dist_ls == 4) {
+    MssPushPolStaged<1> pol{e->csr_dst, w, b->q_vals, b->dist, b->next, b->tbits};
+    k_mss_push<<<c->sssp_grid, kNT, 0, s>>>(pol, q);
+  } else if (b->dist_ls == 8) {
+    MssPushPolStaged<2> pol{e->csr_dst, w, b->q_vals, b->dist, b->next, b->tbits};
+    k_mss_push<<<c->sssp_grid, kNT, 0, s>>>(pol, q);
+  } else {
+    MssPushPol pol{e->csr_dst, w, b->q_mask, b->q_vals, b->dist, b->next, b->tbits,
+                   b->dist_ls};
+    k_mss_push<<<c->sssp_grid, kNT, 0, s>>>(pol, q);
+  }
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+// Algorithmic bytes of one SSSP push: per union edge its index, its weight
+// and the destination row; per queue entry its edge range and snapshot row.
+int64_t sssp_push_bytes(const gas_batch *b, const gas_counters &c) {
+  const int64_t row = 4LL * b->dist_ls;
+  return (int64_t)c.n_scatter_edges * ((b->weighted ? 8 : 4) + row) +
+         (int64_t)c.n_changed * (8 + row);
+}
+
+gas_status_t sssp_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
+  gas_batch *b = c->b;
+  if (b->profiling && !ig) {  // direct launches: the counters were just read
+    CUDA_TRY(cudaEventRecord(b->pev[0], s));
+    GAS_TRY(sssp_push(c, s));
+    CUDA_TRY(cudaEventRecord(b->pev[1], s));
+    CUDA_TRY(cudaEventSynchronize(b->pev[1]));
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, b->pev[0], b->pev[1]));
+    b->prof.push_ms += ms;
+    b->prof.push_bytes += sssp_push_bytes(b, b->h_cnt[2]);
+    b->prof.push_launches += 1;
+  } else {
+    GAS_TRY(sssp_push(c, s));
+  }
+  GAS_TRY(sssp_compact(c, s));
+  k_mss_cond<<<1, 1, 0, s>>>(b->cnt + 2, b->sssp_edges, b->lanes_active, b->lane_rounds, h, ig,
+                             0);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -913,16 +1294,22 @@ void grids(gas_batch *b, RunCtx *c) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ppr_pieces, kNT, 0);
   c->grid_pieces = e->num_sms * (per_sm > 0 ? per_sm : 1);
   c->grid_fix = 8 * e->num_sms;
+  per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mss_push<MssPushPolStaged<2>>, kNT,
+                                                0);
+  c->sssp_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);
 }
 
 gas_status_t check_job(const gas_batch *b, const gas_batch_job *j) {
   if (!j) return fail(GAS_ERR_INVALID, "null job");
   if (j->bfs_lanes < 0 || j->bfs_lanes > kMaxLanes || j->ppr_lanes < 0 ||
-      j->ppr_lanes > kMaxLanes)
+      j->ppr_lanes > kMaxLanes || j->sssp_lanes < 0 || j->sssp_lanes > kMaxLanes)
     return fail(GAS_ERR_INVALID, "lanes must be in [0, %d]", kMaxLanes);
-  if (j->bfs_lanes == 0 && j->ppr_lanes == 0)
-    return fail(GAS_ERR_INVALID, "job has neither BFS nor PPR lanes");
+  if (j->bfs_lanes == 0 && j->ppr_lanes == 0 && j->sssp_lanes == 0)
+    return fail(GAS_ERR_INVALID, "job has no BFS, SSSP or PPR lanes");
   if (j->bfs_lanes > 0 && !j->bfs_sources) return fail(GAS_ERR_INVALID, "null bfs_sources");
+  if (j->sssp_lanes > 0 && !j->sssp_sources)
+    return fail(GAS_ERR_INVALID, "null sssp_sources");
   if (j->ppr_lanes > 0) {
     if (!j->ppr_seeds) return fail(GAS_ERR_INVALID, "null ppr_seeds");
     if (!(j->damping > 0.0 && j->damping < 1.0) || !(j->tol > 0.0))
@@ -931,15 +1318,15 @@ gas_status_t check_job(const gas_batch *b, const gas_batch_job *j) {
   if (j->piece_edges < 0 || j->piece_edges > (1 << 20))
     return fail(GAS_ERR_INVALID, "piece_edges must be in [0, 2^20]");
   const int G = (int)b->v_off.size() - 1;
-  for (int pass = 0; pass < 2; ++pass) {
-    const int L = pass ? j->ppr_lanes : j->bfs_lanes;
-    const int32_t *ids = pass ? j->ppr_seeds : j->bfs_sources;
+  for (int pass = 0; pass < 3; ++pass) {
+    const int L = pass == 0 ? j->bfs_lanes : pass == 1 ? j->ppr_lanes : j->sssp_lanes;
+    const int32_t *ids = pass == 0 ? j->bfs_sources : pass == 1 ? j->ppr_seeds : j->sssp_sources;
     for (int g = 0; g < G; ++g)
       for (int l = 0; l < L; ++l) {
         const int32_t s = ids[(size_t)g * L + l];
         if (s < -1 || s >= b->v_off[g + 1] - b->v_off[g])
           return fail(GAS_ERR_INVALID, "%s %d of graph %d lane %d out of range",
-                      pass ? "seed" : "source", s, g, l);
+                      pass == 1 ? "seed" : "source", s, g, l);
       }
   }
   return GAS_OK;
@@ -968,9 +1355,12 @@ gas_status_t gas_batch_create(gas_batch **out) {
 void gas_batch_destroy(gas_batch *b) {
   if (!b) return;
   free_state(b);
+  for (cudaEvent_t &ev : b->pev)
+    if (ev) cudaEventDestroy(ev);
   bfree(b->cnt);
   bfree(b->prm);
   bfree(b->edges);
+  bfree(b->sssp_edges);
   bfree(b->resid);
   if (b->h_cnt) cudaFreeHost(b->h_cnt);
   gas_engine_destroy(b->eng);
@@ -979,6 +1369,12 @@ void gas_batch_destroy(gas_batch *b) {
 
 gas_status_t gas_batch_add_graph(gas_batch *b, int32_t nV, int64_t nE, const int32_t *srcs,
                                  const int32_t *dsts, int32_t *graph_id) {
+  return gas_batch_add_graph_weighted(b, nV, nE, srcs, dsts, nullptr, graph_id);
+}
+
+gas_status_t gas_batch_add_graph_weighted(gas_batch *b, int32_t nV, int64_t nE,
+                                          const int32_t *srcs, const int32_t *dsts,
+                                          const int32_t *weights, int32_t *graph_id) {
   if (!b || nV < 0 || nE < 0 || (nE > 0 && (!srcs || !dsts)))
     return fail(GAS_ERR_INVALID, "batch_add_graph: bad arguments");
   if (b->built) return fail(GAS_ERR_STATE, "batch already built");
@@ -989,6 +1385,11 @@ gas_status_t gas_batch_add_graph(gas_batch *b, int32_t nV, int64_t nE, const int
     if (srcs[i] < 0 || srcs[i] >= nV || dsts[i] < 0 || dsts[i] >= nV)
       return fail(GAS_ERR_INVALID, "batch_add_graph: edge %lld outside [0, %d)",
                   (long long)i, nV);
+  if (weights)  // the SSSP Program's margin: dist + w never passes INT_MAX
+    for (int64_t i = 0; i < nE; ++i)
+      if (weights[i] < 0 || weights[i] > 100000)
+        return fail(GAS_ERR_INVALID, "batch_add_graph: weight %d of edge %lld outside "
+                    "[0, 100000]", weights[i], (long long)i);
   try {
     const size_t n0 = b->src.size();
     b->src.resize(n0 + nE);
@@ -996,6 +1397,14 @@ gas_status_t gas_batch_add_graph(gas_batch *b, int32_t nV, int64_t nE, const int
     for (int64_t i = 0; i < nE; ++i) {
       b->src[n0 + i] = (int32_t)(srcs[i] + base);
       b->dst[n0 + i] = (int32_t)(dsts[i] + base);
+    }
+    if (weights && !b->weighted) {  // earlier graphs weigh 1 per edge
+      b->w.assign(n0, 1);
+      b->weighted = true;
+    }
+    if (b->weighted) {
+      b->w.resize(n0 + nE, 1);
+      if (weights) std::copy(weights, weights + nE, b->w.begin() + n0);
     }
     b->v_off.push_back((int32_t)(base + nV));
   } catch (...) {
@@ -1011,19 +1420,28 @@ gas_status_t gas_batch_build(gas_batch *b, void *stream) {
   if (b->built) return fail(GAS_ERR_STATE, "batch already built");
   if (b->v_off.size() < 2) return fail(GAS_ERR_STATE, "batch has no graphs");
   const int32_t nV = b->v_off.back();
+  if (b->weighted) {  // an engine whose graph carries int32 edge data
+    gas_engine *we = nullptr;
+    GAS_TRY(gas_engine_create(GAS_PROG_SSSP, &we));
+    gas_engine_destroy(b->eng);
+    b->eng = we;
+  }
   std::vector<int32_t> vd((size_t)std::max(1, nV), -1);
-  GAS_TRY(gas_engine_set_graph(b->eng, nV, vd.data(), (int64_t)b->src.size(), nullptr,
-                               b->src.data(), b->dst.data(), stream));
+  GAS_TRY(gas_engine_set_graph(b->eng, nV, vd.data(), (int64_t)b->src.size(),
+                               b->weighted ? b->w.data() : nullptr, b->src.data(),
+                               b->dst.data(), stream));
   if (!b->cnt) {
-    CUDA_TRY(cudaMalloc(&b->cnt, 2 * sizeof(gas_counters)));
-    CUDA_TRY(cudaMemset(b->cnt, 0, 2 * sizeof(gas_counters)));
-    CUDA_TRY(cudaMallocHost(&b->h_cnt, 2 * sizeof(gas_counters)));
+    CUDA_TRY(cudaMalloc(&b->cnt, 3 * sizeof(gas_counters)));
+    CUDA_TRY(cudaMemset(b->cnt, 0, 3 * sizeof(gas_counters)));
+    CUDA_TRY(cudaMallocHost(&b->h_cnt, 3 * sizeof(gas_counters)));
     CUDA_TRY(cudaMalloc(&b->prm, sizeof(BatchParams)));
     CUDA_TRY(cudaMalloc(&b->edges, sizeof(unsigned long long)));
+    CUDA_TRY(cudaMalloc(&b->sssp_edges, sizeof(unsigned long long)));
     CUDA_TRY(cudaMalloc(&b->resid, (1 + kMaxLanes) * sizeof(double)));
   }
   std::vector<int32_t>().swap(b->src);
   std::vector<int32_t>().swap(b->dst);
+  std::vector<int32_t>().swap(b->w);
   b->built = true;
   return GAS_OK;
 }
@@ -1041,18 +1459,20 @@ int32_t gas_batch_vertex_offset(const gas_batch *b, int32_t g) {
 }
 
 gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *depth_out,
-                           float *rank_out, gas_batch_stats *stats, void *stream) {
+                           int32_t *dist_out, float *rank_out, gas_batch_stats *stats,
+                           void *stream) {
   if (!b || !b->built) return fail(GAS_ERR_STATE, "batch not built");
   GAS_TRY(check_job(b, job));
   gas_engine *e = b->eng;
   cudaStream_t s = S(stream);
   const int G = gas_batch_num_graphs(b), nV = e->nV;
-  const int LB = job->bfs_lanes, LP = job->ppr_lanes;
+  const int LB = job->bfs_lanes, LP = job->ppr_lanes, LS = job->sssp_lanes;
   if (stats) *stats = gas_batch_stats{};
   RunCtx c;
   c.b = b;
   c.bfs_lanes = LB;
   c.ppr_lanes = LP;
+  c.sssp_lanes = LS;
   grids(b, &c);
   const int P = job->piece_edges > 0 ? job->piece_edges : default_piece(b);
   BatchParams prm{};
@@ -1061,7 +1481,9 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
   prm.bfs_max_iter = job->max_bfs_levels > 0 ? job->max_bfs_levels : nV + 2;
   prm.ppr_max_iter = job->max_ppr_iterations > 0 ? job->max_ppr_iterations : 1000;
   prm.n_sources = G * LB;
-  std::vector<int32_t> sg;
+  prm.sssp_max_iter = job->max_sssp_iterations > 0 ? job->max_sssp_iterations : nV + 2;
+  prm.n_sssp_sources = G * LS;
+  std::vector<int32_t> sg, ss;
   if (LB) {
     GAS_TRY(ensure_bfs(b, LB, G * LB));
     sg.resize((size_t)G * LB);
@@ -1069,6 +1491,15 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
       for (int l = 0; l < LB; ++l) {
         const int32_t v = job->bfs_sources[(size_t)g * LB + l];
         sg[(size_t)g * LB + l] = v < 0 ? -1 : v + b->v_off[g];
+      }
+  }
+  if (LS) {
+    GAS_TRY(ensure_sssp(b, LS, G * LS));
+    ss.resize((size_t)G * LS);
+    for (int g = 0; g < G; ++g)
+      for (int l = 0; l < LS; ++l) {
+        const int32_t v = job->sssp_sources[(size_t)g * LS + l];
+        ss[(size_t)g * LS + l] = v < 0 ? -1 : v + b->v_off[g];
       }
   }
   std::vector<uint32_t> mask;
@@ -1082,22 +1513,26 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
       }
     c.ppr = ppr_args(b, LP);
   }
-  Loop loops[2];
-  int which[2];
+  Loop loops[3];
+  int which[3];
   int n = 0;
   if (LB) { loops[n] = Loop{bfs_prologue, bfs_body}; which[n++] = 0; }
+  if (LS) { loops[n] = Loop{sssp_prologue, sssp_body}; which[n++] = 2; }
   if (LP) { loops[n] = Loop{ppr_prologue, ppr_body}; which[n++] = 1; }
-  const bool direct = gas::host_loop_requested();
+  const bool direct = gas::host_loop_requested() || b->profiling;
   if (!direct && (!b->graph || b->g_bfs_lanes != LB || b->g_ppr_lanes != LP ||
-                  b->g_piece != (LP ? P : -1))) {
+                  b->g_sssp_lanes != LS || b->g_piece != (LP ? P : -1))) {
     drop_graph(b);
     GAS_TRY(build_chain(&c, loops, n, &b->graph));
     b->g_bfs_lanes = LB;
     b->g_ppr_lanes = LP;
+    b->g_sssp_lanes = LS;
     b->g_piece = LP ? P : -1;
   }
   CUDA_TRY(cudaMemcpyAsync(b->prm, &prm, sizeof(prm), cudaMemcpyHostToDevice, s));
   if (LB) CUDA_TRY(cudaMemcpyAsync(b->srcs, sg.data(), sg.size() * 4, cudaMemcpyHostToDevice, s));
+  if (LS)
+    CUDA_TRY(cudaMemcpyAsync(b->sssp_srcs, ss.data(), ss.size() * 4, cudaMemcpyHostToDevice, s));
   if (LP)
     CUDA_TRY(cudaMemcpyAsync(b->seed_mask, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice,
                              s));
@@ -1106,15 +1541,23 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
   } else {
     CUDA_TRY(cudaGraphLaunch(b->graph, s));
   }
-  CUDA_TRY(cudaMemcpyAsync(b->h_cnt, b->cnt, 2 * sizeof(gas_counters), cudaMemcpyDeviceToHost, s));
-  unsigned long long edges = 0;
+  CUDA_TRY(cudaMemcpyAsync(b->h_cnt, b->cnt, 3 * sizeof(gas_counters), cudaMemcpyDeviceToHost, s));
+  unsigned long long edges = 0, sedges = 0;
   double resid[1 + kMaxLanes] = {};
+  int32_t rounds[kMaxLanes] = {};
   if (LB) CUDA_TRY(cudaMemcpyAsync(&edges, b->edges, sizeof(edges), cudaMemcpyDeviceToHost, s));
+  if (LS) {
+    CUDA_TRY(cudaMemcpyAsync(&sedges, b->sssp_edges, sizeof(sedges), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(rounds, b->lane_rounds, sizeof(rounds), cudaMemcpyDeviceToHost, s));
+  }
   if (LP) CUDA_TRY(cudaMemcpyAsync(resid, b->resid, sizeof(resid), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
-  const gas_counters cb = b->h_cnt[0], cp = b->h_cnt[1];
+  const gas_counters cb = b->h_cnt[0], cp = b->h_cnt[1], cs = b->h_cnt[2];
   if (depth_out && LB)
     CUDA_TRY(cudaMemcpyAsync(depth_out, b->depth, (size_t)nV * LB * 4, cudaMemcpyDefault, s));
+  if (dist_out && LS && nV > 0)  // rows of LS lanes in the device layout
+    CUDA_TRY(cudaMemcpy2DAsync(dist_out, (size_t)LS * 4, b->dist, (size_t)b->dist_ls * 4,
+                               (size_t)LS * 4, (size_t)nV, cudaMemcpyDefault, s));
   if (rank_out && LP)
     CUDA_TRY(cudaMemcpyAsync(rank_out, b->rank[cp.iteration & 1], (size_t)nV * LP * 4,
                              cudaMemcpyDefault, s));
@@ -1125,10 +1568,20 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
     stats->ppr_iterations = LP ? cp.iteration : 0;
     stats->ppr_residual = resid[0];
     stats->piece_edges = LP ? P : 0;
-    // BFS: prologue 6 kernels, 5 per level; PPR: prologue 3, 3 per iteration
-    stats->kernel_launches = (LB ? 6 + 5 * cb.iteration : 0) + (LP ? 3 + 3 * cp.iteration : 0);
+    stats->sssp_iterations = LS ? cs.iteration : 0;
+    stats->sssp_edges = (int64_t)sedges;
+    for (int l = 0; l < LS; ++l) stats->sssp_lane_iterations[l] = rounds[l];
+    // BFS: prologue 6 kernels, 5 per level; SSSP: prologue 6, 5 per
+    // iteration; PPR: prologue 3, 3 per iteration
+    stats->kernel_launches = (LB ? 6 + 5 * cb.iteration : 0) +
+                             (LS ? 6 + 5 * cs.iteration : 0) + (LP ? 3 + 3 * cp.iteration : 0);
     stats->graph_launches = direct ? 0 : 1;
     for (int l = 0; l < LP; ++l) stats->ppr_lane_residual[l] = resid[1 + l];
+  }
+  if (LS && cs.error) {
+    CUDA_TRY(cudaMemset(&b->cnt[2].error, 0, sizeof(int32_t)));
+    return fail(cs.error == GAS_ERR_ITER_CAP ? GAS_ERR_ITER_CAP : GAS_ERR_DEVICE,
+                "batch sssp: device error %d after %d iterations", cs.error, cs.iteration);
   }
   if (LB && cb.error) {
     CUDA_TRY(cudaMemset(&b->cnt[0].error, 0, sizeof(int32_t)));
@@ -1143,6 +1596,23 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
   return GAS_OK;
 }
 
+gas_status_t gas_batch_set_profiling(gas_batch *b, int32_t on) {
+  if (!b) return fail(GAS_ERR_INVALID, "null batch");
+  if (on && !b->pev[0]) {
+    CUDA_TRY(cudaEventCreate(&b->pev[0]));
+    CUDA_TRY(cudaEventCreate(&b->pev[1]));
+  }
+  b->profiling = on != 0;
+  return GAS_OK;
+}
+
+gas_status_t gas_batch_get_profile(gas_batch *b, gas_kernel_profile *out, int32_t reset) {
+  if (!b || !out) return fail(GAS_ERR_INVALID, "bad arguments");
+  *out = b->prof;
+  if (reset) b->prof = gas_kernel_profile{};
+  return GAS_OK;
+}
+
 gas_status_t gas_batch_tune(gas_batch *b, int32_t ppr_lanes, double damping, int32_t trials,
                             int32_t *piece_edges_out, float *ms_per_iter_out, void *stream) {
   if (!b || !b->built) return fail(GAS_ERR_STATE, "batch not built");
@@ -1154,6 +1624,7 @@ gas_status_t gas_batch_tune(gas_batch *b, int32_t ppr_lanes, double damping, int
   RunCtx c;
   c.b = b;
   c.bfs_lanes = 0;
+  c.sssp_lanes = 0;
   c.ppr_lanes = ppr_lanes;
   grids(b, &c);
   BatchParams prm{};

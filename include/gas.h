@@ -421,6 +421,12 @@ void gas_batch_destroy(gas_batch *b);
 gas_status_t gas_batch_add_graph(gas_batch *b, int32_t nV, int64_t nE,
                                  const int32_t *srcs, const int32_t *dsts,
                                  int32_t *graph_id);
+/* The same with int32 edge weights in [0, 100000] for the SSSP lanes (the
+ * SSSP Program's margin below INT_MAX; weights may be NULL; graphs added
+ * without weights weigh 1 per edge). */
+gas_status_t gas_batch_add_graph_weighted(gas_batch *b, int32_t nV, int64_t nE,
+                                          const int32_t *srcs, const int32_t *dsts,
+                                          const int32_t *weights, int32_t *graph_id);
 /* Uploads the union graph (CSR + CSC); no graphs can be added afterwards. */
 gas_status_t gas_batch_build(gas_batch *b, void *stream);
 int32_t gas_batch_num_graphs(const gas_batch *b);
@@ -440,6 +446,9 @@ typedef struct {
   int32_t max_bfs_levels;      /* <= 0: union V + 2                         */
   int32_t max_ppr_iterations;  /* <= 0: 1000                                */
   int32_t piece_edges;         /* PPR edges per piece; 0: tuned or 256      */
+  int32_t sssp_lanes;          /* 0..32 SSSP sources per graph (0: no SSSP) */
+  const int32_t *sssp_sources; /* [graphs][sssp_lanes] local ids, -1 unused */
+  int32_t max_sssp_iterations; /* <= 0: union V + 2                         */
 } gas_batch_job;
 
 typedef struct {
@@ -450,18 +459,31 @@ typedef struct {
   int32_t piece_edges;         /* piece size the PPR loop used              */
   int32_t kernel_launches;
   int32_t graph_launches;      /* 1, or 0 with GAS_HOST_LOOP=1              */
-  int32_t pad;
+  int32_t sssp_iterations;     /* SSSP pushes run (the largest lane count)  */
   double ppr_lane_residual[GAS_BATCH_MAX_LANES];
+  int64_t sssp_edges;          /* out-edges pushed (lanes of a vertex share) */
+  int32_t sssp_lane_iterations[GAS_BATCH_MAX_LANES]; /* pushes per lane: one */
+                               /* SSSP from that source runs as many        */
 } gas_batch_stats;
 
-/* Runs the job's BFS lanes, then its PPR lanes, as one CUDA-graph launch.
- * depth_out [V][bfs_lanes] int32 (-1 unreached) and rank_out
+/* Runs the job's BFS lanes, its SSSP lanes, then its PPR lanes, as one
+ * CUDA-graph launch.  depth_out [V][bfs_lanes] int32 (-1 unreached),
+ * dist_out [V][sssp_lanes] int32 (INT_MAX - 100000 unreached) and rank_out
  * [V][ppr_lanes] float may be host or device pointers, or NULL.  A lane
  * whose source or seed is -1 stays unreached / all zero.  GAS_ERR_ITER_CAP
  * when a cap ends a loop (results are then those of the last step). */
 gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job,
-                           int32_t *depth_out, float *rank_out,
+                           int32_t *depth_out, int32_t *dist_out, float *rank_out,
                            gas_batch_stats *stats, void *stream);
+
+/* With profiling on, runs use direct launches and bracket every SSSP push
+ * with CUDA events on the run's stream; push_ms / push_bytes (algorithmic:
+ * per union edge its index, weight and destination row, per queue entry its
+ * edge range and snapshot row) / push_launches accumulate until read with
+ * reset != 0. */
+gas_status_t gas_batch_set_profiling(gas_batch *b, int32_t on);
+gas_status_t gas_batch_get_profile(gas_batch *b, gas_kernel_profile *out,
+                                   int32_t reset);
 
 /* Autotuner: times a few PPR iterations for each piece size in
  * {64, 128, ..., 2048} with ppr_lanes lanes and keeps the fastest for runs

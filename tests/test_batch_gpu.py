@@ -225,3 +225,126 @@ def test_device_result_pointers(batch):
     host = b.run(bfs_sources=srcs, ppr_seeds=seeds, tol=PPR_TOL)
     np.testing.assert_array_equal(dd.cpu().numpy(), host.depth)
     np.testing.assert_array_equal(rd.cpu().numpy(), host.rank)
+
+
+# ---------------------------------------------------------------------------
+# multi-source SSSP lanes
+# ---------------------------------------------------------------------------
+SSSP_INF = 2**31 - 1 - 100000
+
+
+def _weighted_graphs():
+    gs = _graphs()
+    out = []
+    for k, el in enumerate(gs):
+        if k == 1:
+            out.append((el, None))  # an unweighted graph among weighted ones: weight 1
+        else:
+            w = el.with_uniform_weights(1, 64, 10 + k).weights if el.nE else np.zeros(0, np.int32)
+            out.append((el, w))
+    return out
+
+
+@pytest.fixture(scope="module")
+def wbatch():
+    gw = _weighted_graphs()
+    b = Batch()
+    for el, w in gw:
+        b.add_graph(el.nV, el.src, el.dst, w)
+    b.build()
+    yield b, gw
+    b.close()
+
+
+def _check_sssp(b, gw, dist, srcs, stats=None):
+    for g, (el, w) in enumerate(gw):
+        d = b.slice(dist, g)
+        ww = w if w is not None else np.ones(el.nE, np.int32)
+        for l in range(srcs.shape[1]):
+            s = int(srcs[g, l])
+            if s < 0:
+                assert np.all(d[:, l] == SSSP_INF)
+                continue
+            ref, rit = oracle.sssp(el.nV, el.src, el.dst, ww, s)
+            np.testing.assert_array_equal(d[:, l], ref, err_msg=f"graph {g} lane {l}")
+
+
+@pytest.mark.parametrize("L", [1, 5, 8, 32])
+def test_multi_source_sssp_bit_exact(wbatch, L):
+    b, gw = wbatch
+    srcs = _lanes([el for el, _ in gw], L, seed=200 + L)
+    res = b.run(sssp_sources=srcs)
+    assert res.depth is None and res.rank is None
+    _check_sssp(b, gw, res.dist, srcs)
+    assert res.stats.sssp_edges > 0 and res.stats.graph_launches == 1
+
+
+def test_sssp_lane_iterations_equal_single_source_runs():
+    """One graph, 8 lanes: every lane runs as many pushes as one SSSP from its
+    source through the engine (and as the oracle's rounds)."""
+    el = EdgeList.rmat(11, 16, seed=2).with_uniform_weights(1, 64, 3)
+    srcs = el.sample_sources(8, 2).astype(np.int32)
+    b = Batch()
+    b.add_graph(el.nV, el.src, el.dst, el.weights)
+    b.build()
+    res = b.run(sssp_sources=srcs[None, :])
+    eng = GASEngineGPU("sssp")
+    eng.setGraph(el.nV, initial_vertex_data("sssp", el.nV, int(srcs[0])), el.nE, el.weights,
+                 el.src, el.dst)
+    for l, s in enumerate(srcs):
+        eng.upload_vertex_data(initial_vertex_data("sssp", el.nV, int(s)))
+        eng.setActive(0, el.nV)
+        st = eng.run_schedule("auto", max_iterations=el.nV + 2)
+        out = np.empty(el.nV, np.int32)
+        eng.download_vertex_data(out)
+        np.testing.assert_array_equal(res.dist[:, l], out)
+        assert res.stats.sssp_lane_iterations[l] == st.iterations, f"lane {l}"
+    assert res.stats.sssp_iterations == max(res.stats.sssp_lane_iterations[l] for l in range(8))
+    eng.close()
+    b.close()
+
+
+def test_all_three_kinds_in_one_launch(wbatch):
+    b, gw = wbatch
+    gs = [el for el, _ in gw]
+    bs, ss, ps = _lanes(gs, 8, 31), _lanes(gs, 8, 32), _lanes(gs, 4, 33)
+    res = b.run(bfs_sources=bs, sssp_sources=ss, ppr_seeds=ps, tol=PPR_TOL)
+    assert res.stats.graph_launches == 1
+    _check_sssp(b, gw, res.dist, ss)
+    _check_ppr(b, gs, res.rank, ps)
+    for g, el in enumerate(gs):
+        d = b.slice(res.depth, g)
+        for l in range(8):
+            s = int(bs[g, l])
+            if s >= 0:
+                ref, _ = oracle.bfs(el.nV, el.src, el.dst, s)
+                np.testing.assert_array_equal(d[:, l], ref)
+
+
+def test_sssp_direct_launch_mode_identical(wbatch):
+    b, gw = wbatch
+    ss = _lanes([el for el, _ in gw], 8, 41)
+    g = b.run(sssp_sources=ss)
+    os.environ["GAS_HOST_LOOP"] = "1"
+    try:
+        d = b.run(sssp_sources=ss)
+    finally:
+        del os.environ["GAS_HOST_LOOP"]
+    assert d.stats.graph_launches == 0
+    np.testing.assert_array_equal(g.dist, d.dist)
+    assert g.stats.sssp_iterations == d.stats.sssp_iterations
+    assert list(g.stats.sssp_lane_iterations) == list(d.stats.sssp_lane_iterations)
+
+
+def test_sssp_cap_and_device_output(wbatch):
+    torch = pytest.importorskip("torch")
+    b, gw = wbatch
+    ss = _lanes([el for el, _ in gw], 8, 51)
+    with pytest.raises(GasError) as ei:
+        b.run(sssp_sources=ss, max_sssp_iterations=1)
+    assert ei.value.status == 4
+    dd = torch.empty((b.num_vertices, 8), dtype=torch.int32, device="cuda")
+    b.run(sssp_sources=ss, dist_out=dd.data_ptr())
+    host = b.run(sssp_sources=ss)
+    np.testing.assert_array_equal(dd.cpu().numpy(), host.dist)
+    _check_sssp(b, gw, host.dist, ss)

@@ -48,6 +48,29 @@ def test_add_graph_rejects_bad_edges_and_run_before_build():
     b.close()
 
 
+def test_weighted_graphs_bookkeeping_and_checks():
+    b = Batch()
+    a = EdgeList.rmat(6, 4, seed=1)
+    assert b.add_graph(a.nV, a.src, a.dst) == 0            # weighs 1 per edge
+    w = np.arange(a.nE, dtype=np.int32) % 7 + 1
+    assert b.add_graph(a.nV, a.src, a.dst, w) == 1
+    assert b.num_edges == 2 * a.nE
+    with pytest.raises(ValueError):
+        b.add_graph(a.nV, a.src, a.dst, w[:-1])
+    for bad in (-1, 100001):
+        wb = w.copy()
+        wb[3] = bad
+        with pytest.raises(GasError) as ei:
+            b.add_graph(a.nV, a.src, a.dst, wb)
+        assert ei.value.status == 1
+    with pytest.raises(GasError) as ei:                     # not built yet
+        b.run(sssp_sources=np.zeros((2, 1), np.int32))
+    assert ei.value.status == 6
+    with pytest.raises(ValueError):
+        b.run(sssp_sources=np.zeros((3, 1), np.int32))      # 2 graphs
+    b.close()
+
+
 def test_ppr_oracle_linearity_and_mass():
     el = EdgeList.erdos_renyi(40, 200, seed=3)
     glob, _, _ = oracle.pagerank_fp64(el.nV, el.src, el.dst, 0.85, 1e-14, 100000)
