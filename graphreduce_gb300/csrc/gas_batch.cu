@@ -216,30 +216,44 @@ __device__ __forceinline__ void ms_totals(const MsWarp &w, int &q, int &d) {
   }
 }
 
-// Pass 1: per block (queue entries, out-edges).
+// Pass 1: per block (queue entries, out-edges); with lanes_active, also
+// the OR of the new lanes of the queue's entries (the SSSP loop).
 __global__ void __launch_bounds__(kNT)
     k_ms_count(const uint32_t *tbits, const uint32_t *next, const uint32_t *visited,
-               const int32_t *csr_off, int nW, int32_t *part) {
+               const int32_t *csr_off, int nW, int32_t *part, uint32_t *lanes_active) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
+  __shared__ uint32_t s_l[kNT / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
   MsWarp w;
   ms_load(tbits, next, visited, csr_off, nW, w0, w);
   int q, d;
   ms_totals(w, q, d);
+  uint32_t lanes = 0u;
+  if (lanes_active) {
+#pragma unroll
+    for (int i = 0; i < kMsWarpWords; ++i)
+      if (w.deg[i] > 0) lanes |= w.nw[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lanes |= __shfl_xor_sync(0xffffffffu, lanes, o);
+  }
   if (lane == 0) {
     s_q[warp] = q;
     s_d[warp] = d;
+    s_l[warp] = lanes;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     int tq = 0, td = 0;
+    uint32_t tl = 0u;
     for (int k = 0; k < kNT / 32; ++k) {
       tq += s_q[k];
       td += s_d[k];
+      tl |= s_l[k];
     }
     part[2 * blockIdx.x] = tq;
     part[2 * blockIdx.x + 1] = td;
+    if (tl) atomicOr(lanes_active, tl);
   }
 }
 
@@ -405,6 +419,22 @@ struct MssPushPol {
   }
 };
 
+// 32-byte row loads (one instruction, one sector): the row must be 32-byte
+// aligned.  row8 is a plain load (the row changes during the push), nc8 a
+// read-only one.
+__device__ __forceinline__ void row8(const int32_t *p, int (&r)[8]) {
+  asm volatile("ld.global.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "l"(p));
+}
+__device__ __forceinline__ void nc8(const int32_t *p, int (&r)[8]) {
+  asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "l"(p));
+}
+
 // Rows of at most 8 lanes (NC = 1 or 2 16-byte chunks): the same push split
 // into probe (the edge's loads and the destination row) and commit, so that
 // both slabs' row reads are in flight before either slab's updates.  Every
@@ -430,7 +460,7 @@ struct MssPushPolStaged {
   __device__ void emit(int, int, Val) const {}
   struct Probe {
     int v, w, a;  // v < 0: no edge
-    int4 cur[NC];
+    int cur[4 * NC];
   };
   __device__ __forceinline__ Probe probe(bool valid, int a, int, int pos) const {
     Probe p;
@@ -440,29 +470,40 @@ struct MssPushPolStaged {
     if (valid) {
       p.v = __ldg(csr_dst + pos);
       p.w = csr_w ? __ldg(csr_w + pos) : 1;
-      const int4 *cur4 = reinterpret_cast<const int4 *>(dist + (size_t)p.v * (4 * NC));
-#pragma unroll
-      for (int c = 0; c < NC; ++c) p.cur[c] = cur4[c];
+      const int32_t *r = dist + (size_t)p.v * (4 * NC);
+      if constexpr (NC == 2) {
+        row8(r, p.cur);
+      } else {
+        const int4 c4 = *reinterpret_cast<const int4 *>(r);
+        p.cur[0] = c4.x;
+        p.cur[1] = c4.y;
+        p.cur[2] = c4.z;
+        p.cur[3] = c4.w;
+      }
     }
     return p;
   }
   __device__ __forceinline__ void commit(const Probe &p) const {
     if (p.v < 0) return;
-    const int4 *qv4 = reinterpret_cast<const int4 *>(q_vals + (size_t)p.a * (4 * NC));
+    const int32_t *q = q_vals + (size_t)p.a * (4 * NC);
+    int val[4 * NC];
+    if constexpr (NC == 2) {
+      nc8(q, val);
+    } else {
+      const int4 q4 = __ldg(reinterpret_cast<const int4 *>(q));
+      val[0] = q4.x;
+      val[1] = q4.y;
+      val[2] = q4.z;
+      val[3] = q4.w;
+    }
     int32_t *row = dist + (size_t)p.v * (4 * NC);
     uint32_t nb = 0u;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const int4 qv = __ldg(qv4 + c);
-      const int cur[4] = {p.cur[c].x, p.cur[c].y, p.cur[c].z, p.cur[c].w};
-      const int val[4] = {qv.x, qv.y, qv.z, qv.w};
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int cand = min(val[k] + p.w, kSsspInf);
-        if (cand < cur[k]) {
-          atomicMin(row + 4 * c + k, cand);
-          nb |= 1u << (4 * c + k);
-        }
+    for (int k = 0; k < 4 * NC; ++k) {
+      const int cand = min(val[k] + p.w, kSsspInf);
+      if (cand < p.cur[k]) {
+        atomicMin(row + k, cand);
+        nb |= 1u << k;
       }
     }
     if (nb && (cmask[p.v] & nb) != nb) {
@@ -502,16 +543,15 @@ __global__ void k_mss_seed(const int32_t *src_global, const BatchParams *prm, in
 }
 
 // Pass 2 of the compaction: the next queue (vertex, changed lanes, snapshot
-// row, inclusive out-edge ends) and the lanes it holds; clears cmask and the
-// touched bitmap.
+// row, inclusive out-edge ends) and the push's chunk partition at the chunk
+// size the spine chose; clears cmask and the touched bitmap.
 __global__ void __launch_bounds__(kNT, 4)
     k_mss_write(uint32_t *tbits, uint32_t *cmask, const int32_t *csr_off, int nW,
                 const int32_t *part, int LS, const int32_t *dist, int32_t *q_ids,
                 int32_t *q_mask, int32_t *q_vals, int32_t *q_end, int32_t *q_delta,
-                int32_t *chunk_row, uint32_t *lanes_active) {
+                int32_t *chunk_row, const gas_counters *cnt) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
-  __shared__ uint32_t s_lanes;
-  if (threadIdx.x == 0) s_lanes = 0u;
+  const int cl = cnt->push_chunk_log2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
   MsWarp w;
@@ -529,7 +569,6 @@ __global__ void __launch_bounds__(kNT, 4)
     bd += s_d[k];
   }
   if (w.myword) tbits[w0 + lane] = 0u;
-  uint32_t lanes = 0u;
 #pragma unroll
   for (int i = 0; i < kMsWarpWords; ++i) {
     const int v = (w0 + i) * 32 + lane;
@@ -549,7 +588,6 @@ __global__ void __launch_bounds__(kNT, 4)
     if (deg > 0) {
       const int pos = bq + __popc(qb & ((1u << lane) - 1u));
       const int end = bd + incl;
-      lanes |= nw;
       q_ids[pos] = v;
       q_mask[pos] = (int32_t)nw;
       q_end[pos] = end;
@@ -557,31 +595,101 @@ __global__ void __launch_bounds__(kNT, 4)
       const int4 *src4 = reinterpret_cast<const int4 *>(dist + (size_t)v * LS);
       int4 *dst4 = reinterpret_cast<int4 *>(q_vals + (size_t)pos * LS);
       for (int c = 0; c < (LS >> 2); ++c) dst4[c] = src4[c];
-      for (int c = (end - deg + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk;
-           c * gasdev::kSlabChunk < end; ++c)
+      for (int c = (end - deg + (1 << cl) - 1) >> cl; (c << cl) < end; ++c)
         chunk_row[c] = pos;
     }
     bq += __popc(qb);
     bd += __shfl_sync(0xffffffffu, incl, 31);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) lanes |= __shfl_xor_sync(0xffffffffu, lanes, o);
-  if (lane == 0 && lanes) atomicOr(&s_lanes, lanes);
-  __syncthreads();
-  if (threadIdx.x == 0 && s_lanes) atomicOr(lanes_active, s_lanes);
 }
 
-// Loop condition; every lane in the new queue has one more push to run.
-__global__ void k_mss_cond(gas_counters *cnt, unsigned long long *edges,
-                           uint32_t *lanes_active, int32_t *lane_rounds,
-                           cudaGraphConditionalHandle h, int in_graph, int first) {
-  const uint32_t la = *lanes_active;
-  *lanes_active = 0u;
-  for (int l = 0; l < kMaxLanes; ++l)
-    if ((la >> l) & 1u) ++lane_rounds[l];
-  const int it = first ? 0 : ++cnt->iteration;
-  set_cond(cnt, cnt->n_scatter_edges > 0, it, h, in_graph);
-  if (cnt->cond) *edges += (unsigned long long)cnt->n_scatter_edges;
+// Exclusive scan of the block pairs in one pass (1024 threads, each holding a
+// run of ceil(nb / 1024) pairs in registers), then the loop control: queue
+// totals, the push's chunk size (512 edges per warp, halved down to 64 while
+// there would be fewer than two chunks per push warp), the lanes of the new
+// queue (each has one more push to run), the WHILE condition.
+constexpr int kMssSpineNT = 1024;
+constexpr int kMssSpineRegs = 8;
+
+__global__ void __launch_bounds__(kMssSpineNT)
+    k_mss_spine(int2 *part, int nb, gas_counters *cnt, int push_warps,
+                unsigned long long *edges, uint32_t *lanes_active, int32_t *lane_rounds,
+                cudaGraphConditionalHandle h, int in_graph, int first) {
+  const int per = (nb + kMssSpineNT - 1) / kMssSpineNT;
+  const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
+  const bool in_regs = per <= kMssSpineRegs;
+  int2 x[kMssSpineRegs];
+  int sq = 0, sd = 0;
+  if (in_regs) {
+#pragma unroll
+    for (int k = 0; k < kMssSpineRegs; ++k) x[k] = b0 + k < b1 ? part[b0 + k] : make_int2(0, 0);
+#pragma unroll
+    for (int k = 0; k < kMssSpineRegs; ++k) {
+      sq += x[k].x;
+      sd += x[k].y;
+    }
+  } else {
+    for (int b = b0; b < b1; ++b) {
+      sq += part[b].x;
+      sd += part[b].y;
+    }
+  }
+  __shared__ int2 s_w[kMssSpineNT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int iq = sq, id = sd;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int oq = __shfl_up_sync(0xffffffffu, iq, d);
+    const int od = __shfl_up_sync(0xffffffffu, id, d);
+    if (lane >= d) {
+      iq += oq;
+      id += od;
+    }
+  }
+  if (lane == 31) s_w[warp] = make_int2(iq, id);
+  __syncthreads();
+  int pq = iq - sq, pd = id - sd, tq = 0, td = 0;
+#pragma unroll 8
+  for (int k = 0; k < kMssSpineNT / 32; ++k) {
+    const int2 t = s_w[k];
+    if (k < warp) {
+      pq += t.x;
+      pd += t.y;
+    }
+    tq += t.x;
+    td += t.y;
+  }
+  if (in_regs) {
+#pragma unroll
+    for (int k = 0; k < kMssSpineRegs; ++k) {
+      if (b0 + k < b1) {
+        part[b0 + k] = make_int2(pq, pd);
+        pq += x[k].x;
+        pd += x[k].y;
+      }
+    }
+  } else {
+    for (int b = b0; b < b1; ++b) {
+      const int2 y = part[b];
+      part[b] = make_int2(pq, pd);
+      pq += y.x;
+      pd += y.y;
+    }
+  }
+  if (threadIdx.x == 0) {
+    cnt->n_changed = tq;
+    cnt->n_scatter_edges = td;
+    int cl = gasdev::kSlabChunkLog2;
+    while (cl > gasdev::kSlabChunkMinLog2 && (td >> cl) < 2 * push_warps) --cl;
+    cnt->push_chunk_log2 = cl;
+    const uint32_t la = *lanes_active;
+    *lanes_active = 0u;
+    for (int l = 0; l < kMaxLanes; ++l)
+      if ((la >> l) & 1u) ++lane_rounds[l];
+    const int it = first ? 0 : ++cnt->iteration;
+    set_cond(cnt, td > 0, it, h, in_graph);
+    if (cnt->cond) *edges += (unsigned long long)td;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -894,7 +1002,8 @@ gas_status_t ensure_frontier(gas_batch *b) {
     CUDA_TRY(cudaMalloc(&b->tbits, nW * 4));
     for (int32_t **p : {&b->q_ids, &b->q_mask, &b->q_end, &b->q_delta})
       CUDA_TRY(cudaMalloc(p, nV * 4));
-    CUDA_TRY(cudaMalloc(&b->part, ((size_t)e->nE / gasdev::kSlabChunk + 2) * 4));
+    // the SSSP push cuts its queue's edges into chunks of 64 to 512 edges
+    CUDA_TRY(cudaMalloc(&b->part, (((size_t)e->nE >> gasdev::kSlabChunkMinLog2) + 2) * 4));
     CUDA_TRY(cudaMalloc(&b->qpart, 2 * ((size_t)ms_blocks(b) + 1) * 4));
   }
   return GAS_OK;
@@ -1059,7 +1168,8 @@ gas_status_t bfs_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle 
   CUDA_TRY(cudaMemsetAsync(b->tbits, 0, nW * 4, s));
   CUDA_TRY(cudaMemsetAsync(b->depth, 0xff, nV * L * 4, s));
   k_ms_seed<<<2 * e->num_sms, 256, 0, s>>>(b->srcs, b->prm, L, b->next, b->tbits);
-  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart);
+  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
+                                nullptr);
   k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
   k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
                                L, b->cnt, 0, b->depth, b->q_ids, b->q_mask, b->q_end,
@@ -1078,7 +1188,8 @@ gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, i
       b->part);
   MsPushPol pol{e->csr_dst, b->q_mask, b->visited, b->next, b->tbits};
   k_ms_push<<<c->slab_grid, kNT, 0, s>>>(pol, q);
-  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart);
+  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
+                                nullptr);
   k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
   k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
                                c->bfs_lanes, b->cnt, 1, b->depth, b->q_ids, b->q_mask,
@@ -1088,15 +1199,21 @@ gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, i
   return GAS_OK;
 }
 
-gas_status_t sssp_compact(RunCtx *c, cudaStream_t s) {
+// The queue of the changed lanes, then the loop control (first: the
+// prologue's queue).
+gas_status_t sssp_compact(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig,
+                          int first) {
   gas_batch *b = c->b;
   gas_engine *e = b->eng;
   const int nb = ms_blocks(b);
-  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, nullptr, e->csr_off, nwords(b), b->qpart);
-  k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt + 2);
+  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, nullptr, e->csr_off, nwords(b), b->qpart,
+                                b->lanes_active);
+  k_mss_spine<<<1, kMssSpineNT, 0, s>>>(reinterpret_cast<int2 *>(b->qpart), nb, b->cnt + 2,
+                                        c->sssp_grid * (kNT / 32), b->sssp_edges,
+                                        b->lanes_active, b->lane_rounds, h, ig, first);
   k_mss_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, e->csr_off, nwords(b), b->qpart,
                                  b->dist_ls, b->dist, b->q_ids, b->q_mask, b->q_vals, b->q_end,
-                                 b->q_delta, b->part, b->lanes_active);
+                                 b->q_delta, b->part, b->cnt + 2);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -1112,11 +1229,7 @@ gas_status_t sssp_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle
                                            b->lane_rounds);
   k_mss_seed<<<2 * e->num_sms, 256, 0, s>>>(b->sssp_srcs, b->prm, c->sssp_lanes, b->dist_ls,
                                            b->dist, b->next, b->tbits);
-  GAS_TRY(sssp_compact(c, s));
-  k_mss_cond<<<1, 1, 0, s>>>(b->cnt + 2, b->sssp_edges, b->lanes_active, b->lane_rounds, h, ig,
-                             1);
-  CUDA_TRY(cudaGetLastError());
-  return GAS_OK;
+  return sssp_compact(c, s, h, ig, 1);
 }
 
 gas_status_t sssp_push(RunCtx *c, cudaStream_t s) {
@@ -1124,7 +1237,7 @@ gas_status_t sssp_push(RunCtx *c, cudaStream_t s) {
   gas_engine *e = b->eng;
   const gasdev::SlabSource q = gasdev::slab_source(
       b->q_end, b->q_ids, b->q_delta, 0, 0, &b->cnt[2].n_changed, &b->cnt[2].n_scatter_edges,
-      b->part);
+      b->part, &b->cnt[2].push_chunk_log2);
   const int32_t *w = b->weighted ? (const int32_t *)e->csr_ed : nullptr;
   if (b->dist_ls == 4) {
     MssPushPolStaged<1> pol{e->csr_dst, w, b->q_vals, b->dist, b->next, b->tbits};
@@ -1164,11 +1277,7 @@ gas_status_t sssp_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, 
   } else {
     GAS_TRY(sssp_push(c, s));
   }
-  GAS_TRY(sssp_compact(c, s));
-  k_mss_cond<<<1, 1, 0, s>>>(b->cnt + 2, b->sssp_edges, b->lanes_active, b->lane_rounds, h, ig,
-                             0);
-  CUDA_TRY(cudaGetLastError());
-  return GAS_OK;
+  return sssp_compact(c, s, h, ig, 0);
 }
 
 gas_status_t ppr_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
@@ -1571,10 +1680,10 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
     stats->sssp_iterations = LS ? cs.iteration : 0;
     stats->sssp_edges = (int64_t)sedges;
     for (int l = 0; l < LS; ++l) stats->sssp_lane_iterations[l] = rounds[l];
-    // BFS: prologue 6 kernels, 5 per level; SSSP: prologue 6, 5 per
-    // iteration; PPR: prologue 3, 3 per iteration
+    // BFS: prologue 6 kernels, 5 per level; SSSP: prologue 6 (reset, init,
+    // seed, 3 compaction), 4 per iteration; PPR: prologue 3, 3 per iteration
     stats->kernel_launches = (LB ? 6 + 5 * cb.iteration : 0) +
-                             (LS ? 6 + 5 * cs.iteration : 0) + (LP ? 3 + 3 * cp.iteration : 0);
+                             (LS ? 6 + 4 * cs.iteration : 0) + (LP ? 3 + 3 * cp.iteration : 0);
     stats->graph_launches = direct ? 0 : 1;
     for (int l = 0; l < LP; ++l) stats->ppr_lane_residual[l] = resid[1 + l];
   }
