@@ -551,8 +551,13 @@ __global__ void __launch_bounds__(kNT, 4)
                 int32_t *q_mask, int32_t *q_vals, int32_t *q_end, int32_t *q_delta,
                 int32_t *chunk_row, const gas_counters *cnt) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
+  // rows spanning many chunks (hubs), written by the whole warp at the end
+  constexpr int kBig = 64;
+  __shared__ int3 s_big[kNT / 32][kBig];
+  __shared__ int s_nbig[kNT / 32];
   const int cl = cnt->push_chunk_log2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) s_nbig[warp] = 0;
   const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
   MsWarp w;
   ms_load(tbits, cmask, nullptr, csr_off, nW, w0, w);
@@ -595,11 +600,22 @@ __global__ void __launch_bounds__(kNT, 4)
       const int4 *src4 = reinterpret_cast<const int4 *>(dist + (size_t)v * LS);
       int4 *dst4 = reinterpret_cast<int4 *>(q_vals + (size_t)pos * LS);
       for (int c = 0; c < (LS >> 2); ++c) dst4[c] = src4[c];
-      for (int c = (end - deg + (1 << cl) - 1) >> cl; (c << cl) < end; ++c)
-        chunk_row[c] = pos;
+      const int c0 = (end - deg + (1 << cl) - 1) >> cl, c1 = (end + (1 << cl) - 1) >> cl;
+      int slot = kBig;
+      if (c1 - c0 > 4) slot = atomicAdd(&s_nbig[warp], 1);
+      if (slot < kBig)
+        s_big[warp][slot] = make_int3(pos, c0, c1);
+      else
+        for (int c = c0; c < c1; ++c) chunk_row[c] = pos;
     }
     bq += __popc(qb);
     bd += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  __syncwarp();
+  const int nbig = min(s_nbig[warp], kBig);
+  for (int k = 0; k < nbig; ++k) {
+    const int3 r = s_big[warp][k];
+    for (int c = r.y + lane; c < r.z; c += 32) chunk_row[c] = r.x;
   }
 }
 
