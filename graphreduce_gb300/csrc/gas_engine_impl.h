@@ -72,6 +72,7 @@ struct gas_engine {
   float *pr_rank[2] = {nullptr, nullptr};
   float *pr_contrib[2] = {nullptr, nullptr};
   int32_t *pr_seed = nullptr;  // personalization seed of the run (-1: none)
+  float *pr_inv_deg = nullptr;  // [V] RN(1 / out-degree) (0: none)
   double *pr_l1 = nullptr;
   int32_t pr_l1_cap = 0;
   double pr_damping = 0.0;

@@ -252,7 +252,7 @@ struct PrPol {
   typedef PrVal Val;
   static constexpr bool kMapNeedsVertex = false;
   const int32_t *csc_src;
-  const int32_t *csr_off;
+  const float *inv_deg;  // RN(1 / out-degree), 0 without out-edges
   const float *contrib;
   const float *rank_old;
   float *rank_new;
@@ -282,10 +282,11 @@ struct PrPol {
     const float sum = __fadd_rn(g.s, g.c);
     const float b = seed < 0 ? base : (v == seed ? base_seed : 0.0f);
     const float r = __fadd_rn(b, __fmul_rn(damping, sum));
-    const int deg = __ldg(csr_off + v + 1) - __ldg(csr_off + v);
     rank_new[v] = r;
-    contrib_new[v] = deg ? __fdiv_rn(r, (float)deg) : 0.0f;
-    l1 += fabs((double)r - (double)rank_old[v]);
+    contrib_new[v] = __fmul_rn(r, __ldg(inv_deg + v));
+    // the step in FP32 (exact while the two ranks are within a factor of
+    // two of each other, Sterbenz), the sum in FP64
+    l1 += (double)fabsf(__fsub_rn(r, rank_old[v]));
   }
 };
 
@@ -375,15 +376,18 @@ __global__ void __launch_bounds__(kNT)
 }
 
 // Initial ranks: 1/N, e_seed (seed >= 0), or the caller's vector already
-// copied into rank.
-__global__ void k_pr_init(float *rank, float *contrib, const int32_t *csr_off,
+// copied into rank; and the reciprocal out-degrees the iterations scale
+// contributions by.
+__global__ void k_pr_init(float *rank, float *contrib, float *inv_deg, const int32_t *csr_off,
                           int n, float r0, int have_init, int seed) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += gridDim.x * blockDim.x) {
     const int deg = csr_off[v + 1] - csr_off[v];
+    const float inv = deg ? __frcp_rn((float)deg) : 0.0f;
     const float r = have_init ? rank[v] : seed < 0 ? r0 : (v == seed ? 1.0f : 0.0f);
     rank[v] = r;
-    contrib[v] = deg ? __fdiv_rn(r, (float)deg) : 0.0f;
+    inv_deg[v] = inv;
+    contrib[v] = __fmul_rn(r, inv);
   }
 }
 
@@ -449,6 +453,7 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
     if (!e->pr_contrib[i]) CUDA_TRY(cudaMalloc(&e->pr_contrib[i], (size_t)nV * 4));
   }
   if (!e->pr_seed) CUDA_TRY(cudaMalloc(&e->pr_seed, sizeof(int32_t)));
+  if (!e->pr_inv_deg) CUDA_TRY(cudaMalloc(&e->pr_inv_deg, (size_t)nV * 4));
   PrCtx c;
   int per_sm = 0;
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pr_slab, kNT, 0));
@@ -466,7 +471,7 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
   }
   c.residual = e->pr_l1 + nparts;
   c.pol.csc_src = e->csc_src;
-  c.pol.csr_off = e->csr_off;
+  c.pol.inv_deg = e->pr_inv_deg;
   c.pol.base = (float)((1.0 - damping) / (double)nV);
   c.pol.base_seed = (float)(1.0 - damping);
   c.pol.damping = (float)damping;
@@ -499,8 +504,8 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
     CUDA_TRY(cudaMemcpyAsync(e->pr_rank[0], init, (size_t)nV * 4, cudaMemcpyDefault,
                              S(stream)));
   k_pr_init<<<gas::engine_grid(nV, kNT, 8 * e->num_sms), kNT, 0, S(stream)>>>(
-      e->pr_rank[0], e->pr_contrib[0], e->csr_off, nV, (float)(1.0 / nV), init ? 1 : 0,
-      seed);
+      e->pr_rank[0], e->pr_contrib[0], e->pr_inv_deg, e->csr_off, nV, (float)(1.0 / nV),
+      init ? 1 : 0, seed);
   k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
   cudaError_t ce = cudaGetLastError();
   if (host_loop) {
