@@ -119,8 +119,16 @@ class ClockSampler:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=self.file, stderr=subprocess.DEVNULL)
+            # nvidia-smi takes a while to start: let its first sample land
+            # before the timed region begins
+            t0 = time.time()
+            while time.time() - t0 < 3.0 and self.proc.poll() is None:
+                self.file.flush()
+                if Path(self.file.name).stat().st_size > 0:
+                    break
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self
