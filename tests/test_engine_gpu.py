@@ -89,6 +89,37 @@ def test_cc_with_grid_islands_against_oracle():
         assert it == rit and it >= 62      # a 32x32 grid needs 62 label hops
 
 
+def test_fast_schedules_at_scale_against_oracle():
+    """Thousands of compaction blocks (R-MAT scale 19 plus 512 grid islands,
+    1M vertices), blocks whose changes come and go between iterations, and
+    the same engine run again: CC and SSSP under the learned and the fixed
+    schedule, bit-exact with the oracle."""
+    from graphreduce_gb300.learn import DATA, MLP
+    model = MLP.load(DATA / "schedule_head.npz")
+    base = EdgeList.rmat(19, 16, seed=7)
+    cases = [("cc", base.with_grid_islands(512, 32), 0)]
+    w = base.with_uniform_weights(1, 64, 8)
+    cases.append(("sssp", w, int(w.sample_sources(1, 9)[0])))
+    for program, el, s in cases:
+        if program == "cc":
+            ref, rit = oracle.cc(el.nV, el.src, el.dst)
+        else:
+            ref, rit = oracle.sssp(el.nV, el.src, el.dst, el.weights, s)
+        eng = GASEngineGPU(program)
+        eng.setGraph(el.nV, initial_vertex_data(program, el.nV, s), el.nE,
+                     el.weights if program == "sssp" else None, el.src, el.dst)
+        eng.set_schedule_model(model)
+        for schedule in ("learned", "auto", "learned"):
+            eng.upload_vertex_data(initial_vertex_data(program, el.nV, s))
+            eng.setActive(0, el.nV)
+            st = eng.run_schedule(schedule, max_iterations=el.nV + 2)
+            out = np.empty(el.nV, np.int32)
+            eng.download_vertex_data(out)
+            np.testing.assert_array_equal(out, ref, err_msg=f"{program}/{schedule}")
+            assert st.iterations == rit, (program, schedule)
+        eng.close()
+
+
 @pytest.mark.parametrize("scale,seed", [(12, 4), (14, 4)])
 def test_pagerank_precision_against_fp64_oracle(scale, seed):
     el = EdgeList.rmat(scale, 16, seed=seed, symmetrize=False)
