@@ -401,11 +401,25 @@ __device__ __forceinline__ void light_loop(const Pol &pol, const int32_t *q_star
   const int lane = threadIdx.x & 31;
   const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  // the next batch's rows are loaded before this batch's edges are walked
+  int nstart = 0, ndeg = 0;
+  {
+    const int i = n0 + gwarp * 32 + lane;
+    if (i < n1) {
+      nstart = __ldg(q_start + i);
+      ndeg = __ldg(q_deg + i);
+    }
+  }
   for (int base = n0 + gwarp * 32; base < n1; base += nwarps * 32) {
     const int i = base + lane;
     const bool ok = i < n1;
-    const int start = ok ? __ldg(q_start + i) : 0;
-    const int deg = ok ? __ldg(q_deg + i) : 0;
+    const int start = nstart;
+    const int deg = ndeg;
+    {
+      const int j = i + nwarps * 32;
+      nstart = j < n1 ? __ldg(q_start + j) : 0;
+      ndeg = j < n1 ? __ldg(q_deg + j) : 0;
+    }
     const int incl = warp_incl_sum_i(deg);
     const int excl = incl - deg;       // the row's first edge in the warp's run
     const int shift = start - excl;    // CSR position - run index, per row
