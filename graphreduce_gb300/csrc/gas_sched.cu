@@ -113,11 +113,12 @@ __global__ void k_seed_finite(const int32_t *vd, int nV, int32_t zero_cap,
 // ---------------------------------------------------------------------------
 // frontier compaction: changed bitmap -> queue of the members with out-edges,
 // in two parts.  Heavy rows [0, q_heavy) (more than kLightDeg out-edges) are
-// pushed by the warp slabs and hold (id, value at the end of the iteration,
-// end of the out-edge range in the heavy rows' edge space, CSR position
-// offset); light rows [q_heavy, n_changed) are pushed one thread per row and
-// hold (id, value, CSR start, out-degree).  Both parts are in vertex order.
-// Also the snapshots of all members for the dense pull.  One lane per vertex:
+// pushed by the warp slabs and hold (value at the end of the iteration, end
+// of the out-edge range in the heavy rows' edge space, CSR position offset);
+// light rows [q_heavy, n_changed) are pushed by warp-cooperative runs and
+// hold (value, CSR start, out-degree).  Both parts are in vertex order.
+// When the next iteration is a dense pull, also the snapshots of all members
+// and the members' ids (by which the snapshots are reset afterwards).  One lane per vertex:
 // each warp takes 8 bitmap words; a word's 32 lanes read their out-degrees
 // coalesced, ballots give queue positions, a warp scan gives edge offsets.
 // ---------------------------------------------------------------------------
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(kNT, 5)
       if (heavy) {
         const int pos = bq + __popc(hb & below);
         const int end = bd + incl;
-        q_ids[pos] = v;
+        if (want_snap) q_ids[pos] = v;  // only a pull's snapshots are reset by id
         q_vals[pos] = val[i];
         q_end[pos] = end;
         q_delta[pos] = w.off[i] - (end - deg);
@@ -286,7 +287,7 @@ __global__ void __launch_bounds__(kNT, 5)
     }
     if (deg > 0 && !heavy) {
       const int pos = lq + __popc(lb & below);
-      q_ids[pos] = v;
+      if (want_snap) q_ids[pos] = v;
       q_vals[pos] = val[i];
       q_end[pos] = deg;
       q_delta[pos] = w.off[i];
