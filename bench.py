@@ -84,6 +84,25 @@ def make_workload(scale):
     return ssp, sources, ccg
 
 
+def max_over_ranks(ms, world, device):
+    """The step time of the slowest rank (replicas: every rank times its own
+    copy of the workload); a barrier after it keeps the ranks in step."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def whole_job_value(units_per_rank, world, ms_per_step):
+    """GTEPS of the whole job: every rank processes units_per_rank edges per
+    step, all within the slowest rank's step time."""
+    return world * units_per_rank / (ms_per_step * 1e-3) / 1e9
+
+
 def edges_visited(el_outdeg, vd, unreached):
     return int(el_outdeg[vd != unreached].sum(dtype=np.int64))
 
@@ -304,11 +323,7 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         ms = start.elapsed_time(end)
-        if world > 1:
-            tt = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            torch.distributed.barrier()
-            ms = float(tt.item())
+        ms = max_over_ranks(ms, world, dev)
         return ms / steps, wall / steps
 
     with ClockSampler(torch.cuda.current_device()) as clk:
@@ -332,8 +347,8 @@ def run_ours(args, rank, world):
              "value": round(world * ev_units / (ms_plain * 1e-3) / 1e9, 4),
              "speedup_of_headline": round(ms_plain / ms_step, 4)}
 
-    value = world * ev_units / (ms_step * 1e-3) / 1e9
-    e2e = world * ev_units / (ms_e2e * 1e-3) / 1e9
+    value = whole_job_value(ev_units, world, ms_step)
+    e2e = whole_job_value(ev_units, world, ms_e2e)
     if batched:  # sources in, the [V][8] distances and the CC labels out
         h2d = len(sources) * 4 + ccg.nV * 4
         d2h = (len(sources) * ssp.nV + ccg.nV) * 4
