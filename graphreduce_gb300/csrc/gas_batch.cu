@@ -506,9 +506,11 @@ struct MssPushPolStaged {
         nb |= 1u << k;
       }
     }
+    // the lanes and the touched bit as fire-and-forget reductions (the
+    // touched bit is idempotent, so no thread waits for an atomic's result)
     if (nb && (cmask[p.v] & nb) != nb) {
-      const uint32_t old = atomicOr(cmask + p.v, nb);
-      if (old == 0u) atomicOr(tbits + ((uint32_t)p.v >> 5), 1u << (p.v & 31));
+      atomicOr(cmask + p.v, nb);
+      atomicOr(tbits + ((uint32_t)p.v >> 5), 1u << (p.v & 31));
     }
   }
 };
