@@ -136,14 +136,14 @@ struct MsPushPol {
   // a: queue position of the pushing vertex, pos: CSR position of the edge.
   // visited does not change during the push; next[v] starts the push at 0
   // and only gains bits, so lanes already seen in it (a plain, possibly
-  // stale load) need no atomic; the first lane to make next[v] non-zero
-  // marks v as touched.
+  // stale load) need no atomic; every thread that adds lanes also marks v
+  // as touched (both reductions, no thread waits for a result).
   __device__ __forceinline__ void visit(int a, int, int pos) const {
     const int v = __ldg(csr_dst + pos);
     const uint32_t m = (uint32_t)__ldg(q_mask + a) & ~visited[v];
     if (m && (next[v] & m) != m) {
-      const uint32_t old = atomicOr(next + v, m);
-      if (old == 0u) atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
+      atomicOr(next + v, m);  // fire-and-forget; the touched bit is idempotent
+      atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
     }
   }
 };
