@@ -413,8 +413,8 @@ struct MssPushPol {
       }
     }
     if (nb && (cmask[v] & nb) != nb) {
-      const uint32_t old = atomicOr(cmask + v, nb);
-      if (old == 0u) atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
+      atomicOr(cmask + v, nb);  // reductions: the touched bit is idempotent
+      atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
     }
   }
 };
