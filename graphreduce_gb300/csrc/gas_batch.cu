@@ -17,10 +17,10 @@
 //     edge): dist[v][l] rows of LS = L rounded up to 4 lanes, cmask[v] the
 //     lanes of v that changed in the current iteration.  One bulk-synchronous
 //     iteration pushes every queued vertex's changed lanes along its
-//     out-edges: the destination's whole row is read once (16-byte loads)
-//     for all lanes, a lane improves with atomicMin when its candidate is
-//     below the value read, and the improved lanes go into cmask (atomicOr,
-//     the first marking the vertex as touched).  The compaction snapshots
+//     out-edges: the destination's whole row is read once (one 32-byte load
+//     for 8 lanes) for all lanes, a lane improves with atomicMin when its
+//     candidate is below the value read, and the improved lanes go into
+//     cmask and the vertex into the touched bitmap (reductions).  The compaction snapshots
 //     each queued vertex's row.  Per lane, distances and iteration counts
 //     equal those of one SSSP per source.
 //   * multi-seed personalized PageRank, r_l = (1-d) e_{s_l} + d A^T D^-1 r_l
