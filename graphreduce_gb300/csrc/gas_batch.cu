@@ -11,7 +11,7 @@
 //     (atomicOr, pre-filtered by visited), marking touched vertices in a
 //     bitmap; a two-pass compaction over that bitmap writes the level into
 //     depth[v][l] for every new lane, folds the lanes into visited and
-//     builds the next queue (vertex, lane mask, inclusive out-edge ends).
+//     builds the next queue (lane mask, inclusive out-edge ends, CSR offset).
 //     Depths equal those of one BFS per source.
 //   * multi-source SSSP (integer weights, unweighted graphs count 1 per
 //     edge): dist[v][l] rows of LS = L rounded up to 4 lanes, cmask[v] the
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kNT)
 __global__ void __launch_bounds__(kNT, 5)
     k_ms_write(uint32_t *tbits, uint32_t *next, uint32_t *visited, const int32_t *csr_off,
                int nW, const int32_t *part, int L, const gas_counters *cnt, int level_add,
-               int32_t *depth, int32_t *q_ids, int32_t *q_mask, int32_t *q_end,
+               int32_t *depth, int32_t *q_mask, int32_t *q_end,
                int32_t *q_delta, int32_t *chunk_row) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   const int level = cnt->iteration + level_add;
@@ -334,7 +334,6 @@ __global__ void __launch_bounds__(kNT, 5)
     if (deg > 0) {
       const int pos = bq + __popc(qb & ((1u << lane) - 1u));
       const int end = bd + incl;
-      q_ids[pos] = v;
       q_mask[pos] = (int32_t)nw;
       q_end[pos] = end;
       q_delta[pos] = w.off[i] - (end - deg);
@@ -544,12 +543,13 @@ __global__ void k_mss_seed(const int32_t *src_global, const BatchParams *prm, in
   }
 }
 
-// Pass 2 of the compaction: the next queue (vertex, changed lanes, snapshot
-// row, inclusive out-edge ends) and the push's chunk partition at the chunk
-// size the spine chose; clears cmask and the touched bitmap.
+// Pass 2 of the compaction: the next queue (snapshot row, inclusive
+// out-edge ends, CSR offset; the changed lanes for rows wider than 8 lanes)
+// and the push's chunk partition at the chunk size the spine chose; clears
+// cmask and the touched bitmap.
 __global__ void __launch_bounds__(kNT, 4)
     k_mss_write(uint32_t *tbits, uint32_t *cmask, const int32_t *csr_off, int nW,
-                const int32_t *part, int LS, const int32_t *dist, int32_t *q_ids,
+                const int32_t *part, int LS, const int32_t *dist,
                 int32_t *q_mask, int32_t *q_vals, int32_t *q_end, int32_t *q_delta,
                 int32_t *chunk_row, const gas_counters *cnt) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
@@ -595,8 +595,7 @@ __global__ void __launch_bounds__(kNT, 4)
     if (deg > 0) {
       const int pos = bq + __popc(qb & ((1u << lane) - 1u));
       const int end = bd + incl;
-      q_ids[pos] = v;
-      q_mask[pos] = (int32_t)nw;
+      if (LS > 8) q_mask[pos] = (int32_t)nw;  // rows of up to 8 lanes try every lane
       q_end[pos] = end;
       q_delta[pos] = w.off[i] - (end - deg);
       const int4 *src4 = reinterpret_cast<const int4 *>(dist + (size_t)v * LS);
@@ -945,7 +944,7 @@ struct gas_batch {
   double *resid = nullptr;        // [1 + 32] max and per-lane PPR residual
   // BFS
   uint32_t *visited = nullptr, *next = nullptr, *tbits = nullptr;
-  int32_t *depth = nullptr, *q_ids = nullptr, *q_mask = nullptr, *q_end = nullptr,
+  int32_t *depth = nullptr, *q_mask = nullptr, *q_end = nullptr,
           *q_delta = nullptr, *part = nullptr, *qpart = nullptr, *srcs = nullptr;
   int32_t depth_lanes = 0, srcs_cap = 0;
   // SSSP (shares the frontier arrays above; next is the changed-lane mask)
@@ -987,7 +986,7 @@ void drop_graph(gas_batch *b) {
 void free_state(gas_batch *b) {
   drop_graph(b);
   bfree(b->visited); bfree(b->next); bfree(b->tbits); bfree(b->depth);
-  bfree(b->q_ids); bfree(b->q_mask); bfree(b->q_end); bfree(b->q_delta);
+  bfree(b->q_mask); bfree(b->q_end); bfree(b->q_delta);
   bfree(b->part); bfree(b->qpart); bfree(b->srcs);
   bfree(b->first_row); bfree(b->fix); bfree(b->head); bfree(b->tail);
   bfree(b->seed_mask); bfree(b->l1);
@@ -1018,7 +1017,7 @@ gas_status_t ensure_frontier(gas_batch *b) {
   if (!b->next) {
     CUDA_TRY(cudaMalloc(&b->next, nV * 4));
     CUDA_TRY(cudaMalloc(&b->tbits, nW * 4));
-    for (int32_t **p : {&b->q_ids, &b->q_mask, &b->q_end, &b->q_delta})
+    for (int32_t **p : {&b->q_mask, &b->q_end, &b->q_delta})
       CUDA_TRY(cudaMalloc(p, nV * 4));
     // the SSSP push cuts its queue's edges into chunks of 64 to 512 edges
     CUDA_TRY(cudaMalloc(&b->part, (((size_t)e->nE >> gasdev::kSlabChunkMinLog2) + 2) * 4));
@@ -1190,7 +1189,7 @@ gas_status_t bfs_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle 
                                 nullptr);
   k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
   k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
-                               L, b->cnt, 0, b->depth, b->q_ids, b->q_mask, b->q_end,
+                               L, b->cnt, 0, b->depth, b->q_mask, b->q_end,
                                b->q_delta, b->part);
   k_ms_precond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
   CUDA_TRY(cudaGetLastError());
@@ -1202,7 +1201,7 @@ gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, i
   gas_engine *e = b->eng;
   const int nb = ms_blocks(b);
   const gasdev::SlabSource q = gasdev::slab_source(
-      b->q_end, b->q_ids, b->q_delta, 0, 0, &b->cnt->n_changed, &b->cnt->n_scatter_edges,
+      b->q_end, nullptr, b->q_delta, 0, 0, &b->cnt->n_changed, &b->cnt->n_scatter_edges,
       b->part);
   MsPushPol pol{e->csr_dst, b->q_mask, b->visited, b->next, b->tbits};
   k_ms_push<<<c->slab_grid, kNT, 0, s>>>(pol, q);
@@ -1210,7 +1209,7 @@ gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, i
                                 nullptr);
   k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
   k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
-                               c->bfs_lanes, b->cnt, 1, b->depth, b->q_ids, b->q_mask,
+                               c->bfs_lanes, b->cnt, 1, b->depth, b->q_mask,
                                b->q_end, b->q_delta, b->part);
   k_ms_cond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
   CUDA_TRY(cudaGetLastError());
@@ -1230,7 +1229,7 @@ gas_status_t sssp_compact(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle 
                                         c->sssp_grid * (kNT / 32), b->sssp_edges,
                                         b->lanes_active, b->lane_rounds, h, ig, first);
   k_mss_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, e->csr_off, nwords(b), b->qpart,
-                                 b->dist_ls, b->dist, b->q_ids, b->q_mask, b->q_vals, b->q_end,
+                                 b->dist_ls, b->dist, b->q_mask, b->q_vals, b->q_end,
                                  b->q_delta, b->part, b->cnt + 2);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
@@ -1254,7 +1253,7 @@ gas_status_t sssp_push(RunCtx *c, cudaStream_t s) {
   gas_batch *b = c->b;
   gas_engine *e = b->eng;
   const gasdev::SlabSource q = gasdev::slab_source(
-      b->q_end, b->q_ids, b->q_delta, 0, 0, &b->cnt[2].n_changed, &b->cnt[2].n_scatter_edges,
+      b->q_end, nullptr, b->q_delta, 0, 0, &b->cnt[2].n_changed, &b->cnt[2].n_scatter_edges,
       b->part, &b->cnt[2].push_chunk_log2);
   const int32_t *w = b->weighted ? (const int32_t *)e->csr_ed : nullptr;
   if (b->dist_ls == 4) {
