@@ -82,23 +82,6 @@ __device__ __forceinline__ int warp_incl(int v) {
   return v;
 }
 
-// Exclusive CTA scan of one int per thread (kNT threads); *total gets the sum.
-__device__ __forceinline__ int cta_excl(int v, int *total) {
-  __shared__ int s_w[kNT / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int incl = warp_incl(v);
-  if (lane == 31) s_w[warp] = incl;
-  __syncthreads();
-  int pre = 0, tot = 0;
-  for (int w = 0; w < kNT / 32; ++w) {
-    if (w < warp) pre += s_w[w];
-    tot += s_w[w];
-  }
-  __syncthreads();
-  *total = tot;
-  return pre + incl - v;
-}
-
 __device__ __forceinline__ void set_cond(gas_counters *cnt, bool more, int it,
                                          cudaGraphConditionalHandle h, int in_graph) {
   if (more && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
@@ -257,43 +240,23 @@ __global__ void __launch_bounds__(kNT)
   }
 }
 
-// Exclusive scan of the block pairs in one pass (thread t folds a run of
-// ceil(nb / kNT) blocks); totals into the counters.
-__global__ void __launch_bounds__(kNT)
-    k_ms_spine(int32_t *part, int nb, gas_counters *cnt) {
-  const int per = (nb + kNT - 1) / kNT;
-  const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
-  int sq = 0, sd = 0;
-  for (int b = b0; b < b1; ++b) {
-    sq += part[2 * b];
-    sd += part[2 * b + 1];
-  }
-  int tq, td;
-  int pq = cta_excl(sq, &tq);
-  int pd = cta_excl(sd, &td);
-  for (int b = b0; b < b1; ++b) {
-    const int q = part[2 * b], d = part[2 * b + 1];
-    part[2 * b] = pq;
-    part[2 * b + 1] = pd;
-    pq += q;
-    pd += d;
-  }
-  if (threadIdx.x == 0) {
-    cnt->n_changed = tq;
-    cnt->n_scatter_edges = td;
-  }
-}
-
-// Pass 2: depths of the new lanes, visited, the next queue; clears next and
-// the touched bitmap.  level = counters.iteration + level_add.
+// Pass 2: depths of the new lanes (level = the iteration the spine just
+// counted), visited, the next queue and the push's chunk partition at the
+// chunk size the spine chose; clears next and the touched bitmap.
 __global__ void __launch_bounds__(kNT, 5)
     k_ms_write(uint32_t *tbits, uint32_t *next, uint32_t *visited, const int32_t *csr_off,
-               int nW, const int32_t *part, int L, const gas_counters *cnt, int level_add,
-               int32_t *depth, int32_t *q_mask, int32_t *q_end,
-               int32_t *q_delta, int32_t *chunk_row) {
+               int nW, const int32_t *part, int L, const gas_counters *cnt,
+               int32_t *depth, int32_t *q_mask, int32_t *q_end, int32_t *q_delta,
+               int32_t *chunk_row) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
-  const int level = cnt->iteration + level_add;
+  // rows spanning many chunks (hubs), written by the whole warp at the end
+  constexpr int kBig = 64;
+  __shared__ int3 s_big[kNT / 32][kBig];
+  __shared__ int s_nbig[kNT / 32];
+  const int level = cnt->iteration;
+  const int cl = cnt->push_chunk_log2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) s_nbig[warp] = 0;
   const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
   MsWarp w;
   ms_load(tbits, next, visited, csr_off, nW, w0, w);
@@ -338,27 +301,23 @@ __global__ void __launch_bounds__(kNT, 5)
       q_end[pos] = end;
       q_delta[pos] = w.off[i] - (end - deg);
       // chunk partition of the next push (chunks starting in this range)
-      for (int c = (end - deg + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk;
-           c * gasdev::kSlabChunk < end; ++c)
-        chunk_row[c] = pos;
+      const int c0 = (end - deg + (1 << cl) - 1) >> cl, c1 = (end + (1 << cl) - 1) >> cl;
+      int slot = kBig;
+      if (c1 - c0 > 4) slot = atomicAdd(&s_nbig[warp], 1);
+      if (slot < kBig)
+        s_big[warp][slot] = make_int3(pos, c0, c1);
+      else
+        for (int c = c0; c < c1; ++c) chunk_row[c] = pos;
     }
     bq += __popc(qb);
     bd += __shfl_sync(0xffffffffu, incl, 31);
   }
-}
-
-// Loop condition after the prologue (level 0 written, no push run yet).
-__global__ void k_ms_precond(gas_counters *cnt, unsigned long long *edges,
-                             cudaGraphConditionalHandle h, int in_graph) {
-  set_cond(cnt, cnt->n_scatter_edges > 0, 0, h, in_graph);
-  if (cnt->cond) *edges += (unsigned long long)cnt->n_scatter_edges;
-}
-
-__global__ void k_ms_cond(gas_counters *cnt, unsigned long long *edges,
-                          cudaGraphConditionalHandle h, int in_graph) {
-  const int it = ++cnt->iteration;
-  set_cond(cnt, cnt->n_scatter_edges > 0, it, h, in_graph);
-  if (cnt->cond) *edges += (unsigned long long)cnt->n_scatter_edges;
+  __syncwarp();
+  const int nbig = min(s_nbig[warp], kBig);
+  for (int k = 0; k < nbig; ++k) {
+    const int3 r = s_big[warp][k];
+    for (int c = r.y + lane; c < r.z; c += 32) chunk_row[c] = r.x;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -621,10 +580,11 @@ __global__ void __launch_bounds__(kNT, 4)
 }
 
 // Exclusive scan of the block pairs in one pass (1024 threads, each holding a
-// run of ceil(nb / 1024) pairs in registers), then the loop control: queue
-// totals, the push's chunk size (512 edges per warp, halved down to 64 while
-// there would be fewer than two chunks per push warp), the lanes of the new
-// queue (each has one more push to run), the WHILE condition.
+// run of ceil(nb / 1024) pairs in registers), then the loop control of the
+// BFS and SSSP loops: queue totals, the push's chunk size (512 edges per
+// warp, halved down to 64 while there would be fewer than two chunks per
+// push warp), the lanes of the new queue (each has one more push to run;
+// SSSP only), the WHILE condition.
 constexpr int kMssSpineNT = 1024;
 constexpr int kMssSpineRegs = 8;
 
@@ -699,10 +659,12 @@ __global__ void __launch_bounds__(kMssSpineNT)
     int cl = gasdev::kSlabChunkLog2;
     while (cl > gasdev::kSlabChunkMinLog2 && (td >> cl) < 2 * push_warps) --cl;
     cnt->push_chunk_log2 = cl;
-    const uint32_t la = *lanes_active;
-    *lanes_active = 0u;
-    for (int l = 0; l < kMaxLanes; ++l)
-      if ((la >> l) & 1u) ++lane_rounds[l];
+    if (lanes_active) {
+      const uint32_t la = *lanes_active;
+      *lanes_active = 0u;
+      for (int l = 0; l < kMaxLanes; ++l)
+        if ((la >> l) & 1u) ++lane_rounds[l];
+    }
     const int it = first ? 0 : ++cnt->iteration;
     set_cond(cnt, td > 0, it, h, in_graph);
     if (cnt->cond) *edges += (unsigned long long)td;
@@ -1174,46 +1136,49 @@ PprArgs ppr_args(gas_batch *b, int lanes) {
 
 typedef gas_status_t (*StepFn)(RunCtx *, cudaStream_t, cudaGraphConditionalHandle, int);
 
+// The next frontier of new lanes, then the loop control (first: the
+// prologue's sources, level 0).
+gas_status_t bfs_compact(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig,
+                         int first) {
+  gas_batch *b = c->b;
+  gas_engine *e = b->eng;
+  const int nb = ms_blocks(b);
+  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
+                                nullptr);
+  k_mss_spine<<<1, kMssSpineNT, 0, s>>>(reinterpret_cast<int2 *>(b->qpart), nb, b->cnt,
+                                        c->slab_grid * (kNT / 32), b->edges, nullptr, nullptr,
+                                        h, ig, first);
+  k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
+                               c->bfs_lanes, b->cnt, b->depth, b->q_mask, b->q_end, b->q_delta,
+                               b->part);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
 gas_status_t bfs_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
   gas_batch *b = c->b;
   gas_engine *e = b->eng;
   const size_t nV = std::max(1, e->nV), nW = std::max(1, nwords(b));
-  const int L = c->bfs_lanes, nb = ms_blocks(b);
+  const int L = c->bfs_lanes;
   k_b_reset<<<1, 1, 0, s>>>(b->cnt, b->prm, 0, b->edges);
   CUDA_TRY(cudaMemsetAsync(b->visited, 0, nV * 4, s));
   CUDA_TRY(cudaMemsetAsync(b->next, 0, nV * 4, s));
   CUDA_TRY(cudaMemsetAsync(b->tbits, 0, nW * 4, s));
   CUDA_TRY(cudaMemsetAsync(b->depth, 0xff, nV * L * 4, s));
   k_ms_seed<<<2 * e->num_sms, 256, 0, s>>>(b->srcs, b->prm, L, b->next, b->tbits);
-  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
-                                nullptr);
-  k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
-  k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
-                               L, b->cnt, 0, b->depth, b->q_mask, b->q_end,
-                               b->q_delta, b->part);
-  k_ms_precond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
-  CUDA_TRY(cudaGetLastError());
-  return GAS_OK;
+  return bfs_compact(c, s, h, ig, 1);
 }
 
 gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
   gas_batch *b = c->b;
   gas_engine *e = b->eng;
-  const int nb = ms_blocks(b);
   const gasdev::SlabSource q = gasdev::slab_source(
       b->q_end, nullptr, b->q_delta, 0, 0, &b->cnt->n_changed, &b->cnt->n_scatter_edges,
-      b->part);
+      b->part, &b->cnt->push_chunk_log2);
   MsPushPol pol{e->csr_dst, b->q_mask, b->visited, b->next, b->tbits};
   k_ms_push<<<c->slab_grid, kNT, 0, s>>>(pol, q);
-  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
-                                nullptr);
-  k_ms_spine<<<1, kNT, 0, s>>>(b->qpart, nb, b->cnt);
-  k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
-                               c->bfs_lanes, b->cnt, 1, b->depth, b->q_mask,
-                               b->q_end, b->q_delta, b->part);
-  k_ms_cond<<<1, 1, 0, s>>>(b->cnt, b->edges, h, ig);
   CUDA_TRY(cudaGetLastError());
-  return GAS_OK;
+  return bfs_compact(c, s, h, ig, 0);
 }
 
 // The queue of the changed lanes, then the loop control (first: the
@@ -1697,9 +1662,10 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job, int32_t *dept
     stats->sssp_iterations = LS ? cs.iteration : 0;
     stats->sssp_edges = (int64_t)sedges;
     for (int l = 0; l < LS; ++l) stats->sssp_lane_iterations[l] = rounds[l];
-    // BFS: prologue 6 kernels, 5 per level; SSSP: prologue 6 (reset, init,
-    // seed, 3 compaction), 4 per iteration; PPR: prologue 3, 3 per iteration
-    stats->kernel_launches = (LB ? 6 + 5 * cb.iteration : 0) +
+    // BFS: prologue 5 kernels (reset, seed, 3 compaction), 4 per level;
+    // SSSP: prologue 6 (reset, init, seed, 3 compaction), 4 per iteration;
+    // PPR: prologue 3, 3 per iteration
+    stats->kernel_launches = (LB ? 5 + 4 * cb.iteration : 0) +
                              (LS ? 6 + 4 * cs.iteration : 0) + (LP ? 3 + 3 * cp.iteration : 0);
     stats->graph_launches = direct ? 0 : 1;
     for (int l = 0; l < LP; ++l) stats->ppr_lane_residual[l] = resid[1 + l];
