@@ -72,16 +72,6 @@ struct BatchParams {
   int32_t pad;
 };
 
-__device__ __forceinline__ int warp_incl(int v) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int o = __shfl_up_sync(0xffffffffu, v, d);
-    if (lane >= d) v += o;
-  }
-  return v;
-}
-
 __device__ __forceinline__ void set_cond(gas_counters *cnt, bool more, int it,
                                          cudaGraphConditionalHandle h, int in_graph) {
   if (more && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
