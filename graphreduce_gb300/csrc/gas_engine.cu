@@ -424,12 +424,6 @@ __global__ void k_bfs_apply(const int32_t *act, const gas_counters *cnt,
   }
 }
 
-__global__ void k_fill_i32(int32_t *p, int32_t v, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = v;
-}
-
 }  // namespace
 
 namespace {

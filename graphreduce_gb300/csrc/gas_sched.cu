@@ -49,31 +49,7 @@ namespace {
 
 inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
 
-constexpr int kWordsPerThread = 4;
-constexpr int kCompactBlock = kNT * kWordsPerThread;  // bitmap words per block
-
 enum { kModePush = 0, kModePull = 1 };
-
-__device__ __forceinline__ int cta_excl_sum(int v, int *total) {
-  __shared__ int s_w[kNT / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int incl = v;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int o = __shfl_up_sync(0xffffffffu, incl, d);
-    if (lane >= d) incl += o;
-  }
-  if (lane == 31) s_w[warp] = incl;
-  __syncthreads();
-  int pre = 0, tot = 0;
-  for (int w = 0; w < kNT / 32; ++w) {
-    if (w < warp) pre += s_w[w];
-    tot += s_w[w];
-  }
-  __syncthreads();
-  *total = tot;
-  return pre + incl - v;
-}
 
 // ---------------------------------------------------------------------------
 // iteration 0 -> the changed set
