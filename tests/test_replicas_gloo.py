@@ -32,7 +32,7 @@ def _rank(rank, world, port, times, out):
 def test_two_replicas_report_the_slowest_rank():
     world, port = 2, _free_port()
     times = [12.5, 14.0]   # ms per step on each rank
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:   # no fork of a threaded process
         out = m.dict()
         mp.spawn(_rank, args=(world, port, times, out), nprocs=world, join=True)
         res = dict(out)
