@@ -509,6 +509,160 @@ def kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev, s
 
 
 # ---------------------------------------------------------------------------
+# batched lanes on one scale-24 graph: 16 BFS sources, 16 PPR seeds
+# ---------------------------------------------------------------------------
+LANES24 = 16
+
+
+def run_lanes24(args):
+    """The batched engine on single R-MAT scale-24 graphs: multi-source BFS
+    (16 sources, the symmetrised graph of the headline at scale 24, seed 2)
+    and multi-seed personalized PageRank (16 seeds, the directed graph of the
+    PageRank workload, seed 4), each against the same instances run one by
+    one on the single-graph engine.  Roofline: BFS from the profiled pushes
+    (per union edge index + visited + next words, per queue entry 12 B); PPR
+    from the autotuner's per-iteration time (per edge index + 16 lanes of the
+    source's contribution, per vertex offsets, seed mask, old and new rank and
+    new contribution)."""
+    import torch
+
+    import graphreduce_gb300 as gg
+    from graphreduce_gb300.engine import initial_vertex_data
+    from graphreduce_gb300.graph import EdgeList
+    from graphreduce_gb300.learn import DATA, MLP
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    scale, L = args.pr_scale, LANES24
+    peak, peak_kind = measured_peaks()
+    model = MLP.load(DATA / "schedule_head.npz")
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        z = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        z.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(z) / steps
+
+    out = {"metric": f"GTEPS (batched lanes on one R-MAT scale-{scale} graph: "
+                     f"{L} BFS sources, {L} PPR seeds)", "unit": "GTEPS", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+           "dtype": "int32 (BFS), f32 two-sum + f64 residual (PPR)", "data": "synthetic"}
+
+    # --- BFS ---------------------------------------------------------------
+    el = EdgeList.rmat(scale, EDGE_FACTOR, *RMAT_ABC, seed=GRAPH_SEED, symmetrize=True)
+    srcs = el.sample_sources(L, SOURCE_SEED).astype(np.int32)
+    b = gg.Batch()
+    b.add_graph(el.nV, el.src, el.dst)
+    b.build(sp)
+    depth_d = torch.empty((el.nV, L), dtype=torch.int32, device=dev)
+    run_b = lambda: b.run(bfs_sources=srcs[None, :], depth_out=depth_d.data_ptr(), stream=sp)
+    run_b()
+    depth = depth_d.cpu().numpy()
+    od = el.out_degree().astype(np.int64)
+    bfs_units = int(((depth >= 0) * od[:, None]).sum())
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms_b = timed(run_b, args.steps, args.warmup)
+    b.set_profiling(True)
+    b.profile(reset=True)
+    run_b()
+    torch.cuda.synchronize()
+    pb = b.profile()
+    b.set_profiling(False)
+    e = gg.GASEngineGPU("bfs")
+    e.setGraph(el.nV, initial_vertex_data("bfs", el.nV), el.nE, None, el.src, el.dst, sp)
+    e.set_schedule_model(model)
+    init = torch.from_numpy(initial_vertex_data("bfs", el.nV)).to(dev)
+    one = torch.empty(el.nV, dtype=torch.int32)
+
+    def plain_bfs():
+        for s in srcs:
+            e.upload_vertex_data_ptr(init.data_ptr(), sp)
+            e.setActive(int(s), int(s) + 1, sp)
+            e.run_schedule("learned", max_iterations=el.nV + 2, stream=sp)
+
+    e.upload_vertex_data_ptr(init.data_ptr(), sp)
+    e.setActive(int(srcs[0]), int(srcs[0]) + 1, sp)
+    e.run_schedule("learned", max_iterations=el.nV + 2, stream=sp)
+    e.download_vertex_data(one.numpy(), sp)
+    same = bool(np.array_equal(one.numpy(), depth[:, 0]))
+    ms_plain_b = timed(plain_bfs, 1, 1)
+    e.close()
+    b.close()
+    ach = pb.push_bytes / (pb.push_ms * 1e-3) / 1e9 if pb.push_ms > 0 else 0.0
+    out["bfs"] = {"graph": f"rmat-s{scale}-ef{EDGE_FACTOR}-sym seed {GRAPH_SEED}",
+                  "V": el.nV, "E": el.nE, "lanes": L, "ms": round(ms_b, 3),
+                  "gteps": round(bfs_units / (ms_b * 1e-3) / 1e9, 4),
+                  "plain_one_by_one_ms": round(ms_plain_b, 3),
+                  "speedup_vs_plain": round(ms_plain_b / ms_b, 3),
+                  "lane0_equals_single_source_run": same,
+                  "roofline": {"kernel": "k_ms_push (16-lane BFS push)", "bound": "hbm",
+                               "achieved": round(ach, 1), "unit": "GB/s", "peak": peak,
+                               "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                               "launches": pb.push_launches,
+                               "push_share_of_run": round(pb.push_ms / ms_b, 3)}}
+    del el, depth, depth_d
+    clocks_b = clk.summary()
+
+    # --- PPR ---------------------------------------------------------------
+    d = EdgeList.rmat(scale, EDGE_FACTOR, *RMAT_ABC, seed=PR_SEED, symmetrize=False)
+    seeds = d.sample_sources(L, 7).astype(np.int32)
+    b = gg.Batch()
+    b.add_graph(d.nV, d.src, d.dst)
+    b.build(sp)
+    piece, ms_iter = b.tune(L, PPR_DAMPING, 5, sp)
+    rank_d = torch.empty((d.nV, L), dtype=torch.float32, device=dev)
+    run_p = lambda: b.run(ppr_seeds=seeds[None, :], damping=PPR_DAMPING, tol=PPR_TOL,
+                          rank_out=rank_d.data_ptr(), stream=sp)
+    st = run_p().stats
+    ms_p = timed(run_p, args.steps, args.warmup)
+    p = gg.GASEngineGPU("pagerank")
+    p.setGraph(d.nV, initial_vertex_data("pagerank", d.nV, 0, d.out_degree()), d.nE, None,
+               d.src, d.dst, sp)
+    outp = torch.empty(d.nV, dtype=torch.float32, device=dev)
+    plain_iters = [0]
+
+    def plain_ppr():
+        plain_iters[0] = 0
+        for s in seeds:
+            _, pst = p.ppr_precision(int(s), PPR_DAMPING, PPR_TOL, out=outp.data_ptr(),
+                                     stream=sp)
+            plain_iters[0] += pst.iterations
+
+    ms_plain_p = timed(plain_ppr, 1, 0)
+    p.close()
+    b.close()
+    ppr_units = d.nE * L * st.ppr_iterations
+    ppr_bytes = d.nE * (4 + 4 * L) + d.nV * (12 + 12 * L)
+    ach = ppr_bytes / (ms_iter * 1e-3) / 1e9
+    out["ppr"] = {"graph": f"rmat-s{scale}-ef{EDGE_FACTOR} directed seed {PR_SEED}",
+                  "V": d.nV, "E": d.nE, "lanes": L, "iterations": st.ppr_iterations,
+                  "ms": round(ms_p, 3), "gteps": round(ppr_units / (ms_p * 1e-3) / 1e9, 4),
+                  "plain_one_by_one_ms": round(ms_plain_p, 3),
+                  "plain_iterations": plain_iters[0],
+                  "speedup_vs_plain": round(ms_plain_p / ms_p, 3),
+                  "residual": st.ppr_residual,
+                  "roofline": {"kernel": "PPR iteration (k_ppr_pieces + k_ppr_fix + k_ppr_finish)",
+                               "bound": "hbm", "achieved": round(ach, 1), "unit": "GB/s",
+                               "peak": peak, "frac": round(ach / peak, 4),
+                               "peak_source": peak_kind, "piece_edges": piece,
+                               "ms_per_iteration": round(ms_iter, 4),
+                               "algorithmic_bytes_per_iteration": int(ppr_bytes)}}
+    total_units = bfs_units + ppr_units
+    out["value"] = round(total_units / ((ms_b + ms_p) * 1e-3) / 1e9, 4)
+    out["ms_per_step"] = round(ms_b + ms_p, 3)
+    out["clocks"] = clocks_b
+    return out
+
+
+# ---------------------------------------------------------------------------
 # batched workload: 64 graphs x (16 BFS sources + 16 PPR seeds)
 # ---------------------------------------------------------------------------
 BATCH_GRAPHS, BATCH_LANES, BATCH_SEED = 64, 16, 6
@@ -884,7 +1038,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--edges", default="device", choices=["device", "host"],
                     help="edge arrays in HBM or in pinned host memory (NVLink-C2C)")
-    ap.add_argument("--workload", default="sssp-cc", choices=["sssp-cc", "batched", "pagerank"])
+    ap.add_argument("--workload", default="sssp-cc",
+                    choices=["sssp-cc", "batched", "pagerank", "lanes24"])
     ap.add_argument("--pr-scale", type=int, default=PR_SCALE)
     ap.add_argument("--pr-check", action="store_true",
                     help="compare with the FP64 oracle (single-threaded C, slow)")
@@ -911,6 +1066,10 @@ def main():
     if args.workload == "pagerank":
         if rank == 0:
             print(json.dumps(run_pagerank(args)), flush=True)
+        return
+    if args.workload == "lanes24":
+        if rank == 0:
+            print(json.dumps(run_lanes24(args)), flush=True)
         return
 
     if world > 1:

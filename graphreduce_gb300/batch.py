@@ -87,8 +87,8 @@ class Batch:
         return L.load().gas_batch_vertex_offset(self._h, g)
 
     def set_profiling(self, on: bool) -> None:
-        """Kernel-level timing of the SSSP pushes of later runs (direct
-        launches, CUDA events)."""
+        """Kernel-level timing of the BFS and SSSP pushes of later runs
+        (direct launches, CUDA events)."""
         L.call("gas_batch_set_profiling", self._h, int(on))
 
     def profile(self, reset: bool = True) -> L.KernelProfile:

@@ -1159,7 +1159,7 @@ gas_status_t bfs_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle 
   return bfs_compact(c, s, h, ig, 1);
 }
 
-gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
+gas_status_t bfs_push(RunCtx *c, cudaStream_t s) {
   gas_batch *b = c->b;
   gas_engine *e = b->eng;
   const gasdev::SlabSource q = gasdev::slab_source(
@@ -1168,6 +1168,27 @@ gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, i
   MsPushPol pol{e->csr_dst, b->q_mask, b->visited, b->next, b->tbits};
   k_ms_push<<<c->slab_grid, kNT, 0, s>>>(pol, q);
   CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+gas_status_t bfs_body(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h, int ig) {
+  gas_batch *b = c->b;
+  if (b->profiling && !ig) {  // direct launches: the counters were just read
+    // algorithmic bytes: per union edge its index and the destination's
+    // visited and next words; per queue entry its edge range and lane mask
+    const gas_counters &k = b->h_cnt[0];
+    CUDA_TRY(cudaEventRecord(b->pev[0], s));
+    GAS_TRY(bfs_push(c, s));
+    CUDA_TRY(cudaEventRecord(b->pev[1], s));
+    CUDA_TRY(cudaEventSynchronize(b->pev[1]));
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, b->pev[0], b->pev[1]));
+    b->prof.push_ms += ms;
+    b->prof.push_bytes += (int64_t)k.n_scatter_edges * 12 + (int64_t)k.n_changed * 12;
+    b->prof.push_launches += 1;
+  } else {
+    GAS_TRY(bfs_push(c, s));
+  }
   return bfs_compact(c, s, h, ig, 0);
 }
 

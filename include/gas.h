@@ -476,11 +476,13 @@ gas_status_t gas_batch_run(gas_batch *b, const gas_batch_job *job,
                            int32_t *depth_out, int32_t *dist_out, float *rank_out,
                            gas_batch_stats *stats, void *stream);
 
-/* With profiling on, runs use direct launches and bracket every SSSP push
- * with CUDA events on the run's stream; push_ms / push_bytes (algorithmic:
- * per union edge its index, weight and destination row, per queue entry its
- * edge range and snapshot row) / push_launches accumulate until read with
- * reset != 0. */
+/* With profiling on, runs use direct launches and bracket every BFS and
+ * SSSP push with CUDA events on the run's stream; push_ms / push_bytes /
+ * push_launches accumulate until read with reset != 0.  Algorithmic bytes:
+ * BFS, per union edge its index and the destination's visited and next
+ * words, per queue entry its edge range and lane mask; SSSP, per union edge
+ * its index, weight and destination row, per queue entry its edge range and
+ * snapshot row. */
 gas_status_t gas_batch_set_profiling(gas_batch *b, int32_t on);
 gas_status_t gas_batch_get_profile(gas_batch *b, gas_kernel_profile *out,
                                    int32_t reset);

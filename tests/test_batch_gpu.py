@@ -348,3 +348,25 @@ def test_sssp_cap_and_device_output(wbatch):
     host = b.run(sssp_sources=ss)
     np.testing.assert_array_equal(dd.cpu().numpy(), host.dist)
     _check_sssp(b, gw, host.dist, ss)
+
+
+def test_profiled_pushes_same_results(wbatch):
+    b, gw = wbatch
+    gs = [el for el, _ in gw]
+    bs, ss = _lanes(gs, 8, 61), _lanes(gs, 8, 62)
+    ref = b.run(bfs_sources=bs, sssp_sources=ss)
+    b.set_profiling(True)
+    try:
+        b.profile(reset=True)
+        got = b.run(bfs_sources=bs, sssp_sources=ss)
+        p = b.profile()
+    finally:
+        b.set_profiling(False)
+    np.testing.assert_array_equal(got.depth, ref.depth)
+    np.testing.assert_array_equal(got.dist, ref.dist)
+    # at most one push per BFS level and per SSSP iteration, none when off
+    it = got.stats.bfs_iterations + got.stats.sssp_iterations
+    assert 0 < p.push_launches <= it + 2
+    assert p.push_ms > 0 and p.push_bytes > 0
+    b.run(bfs_sources=bs)
+    assert b.profile().push_launches == 0
