@@ -954,7 +954,7 @@ def run_pagerank(args):
                        "speedup": round(ms / ms_warm, 4),
                        "l1_between_results": float(np.abs(r_uni.astype(np.float64) -
                                                           r_warm).sum())},
-        "roofline": {"kernel": "k_pr_slab + k_pr_fixup (one PageRank iteration's slab pass)",
+        "roofline": {"kernel": "k_pr_merge + k_pr_merge_fix (one PageRank iteration's gather)",
                      "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                      "peak_source": peak_kind,

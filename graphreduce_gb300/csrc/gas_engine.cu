@@ -491,6 +491,8 @@ void free_graph(gas_engine *e) {
   dfree(e->ppart); dfree(e->cpart); dfree(e->cnt);
   for (int i = 0; i < 2; ++i) { dfree(e->pr_rank[i]); dfree(e->pr_contrib[i]); }
   dfree(e->pr_seed); dfree(e->pr_inv_deg); dfree(e->pr_l1); dfree(e->csr_to_csc);
+  dfree(e->pr_tile_row); dfree(e->pr_head); dfree(e->pr_tail);
+  e->pr_tile_cap = 0;
   e->h_csr_perm.clear();
   e->h_csr_to_csc.clear();
   e->host_ed = nullptr;

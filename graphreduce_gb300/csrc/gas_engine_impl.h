@@ -75,6 +75,11 @@ struct gas_engine {
   float *pr_inv_deg = nullptr;  // [V] RN(1 / out-degree) (0: none)
   double *pr_l1 = nullptr;
   int32_t pr_l1_cap = 0;
+  // merge-path tiles of the CSC: start rows [tiles + 1], head and tail
+  // carry records [tiles]
+  int32_t *pr_tile_row = nullptr;
+  void *pr_head = nullptr, *pr_tail = nullptr;
+  int32_t pr_tile_cap = 0;
   double pr_damping = 0.0;
 
   // fast-schedule state (lazily allocated): frontier queue of C_k with the

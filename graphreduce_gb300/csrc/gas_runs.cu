@@ -248,9 +248,11 @@ __device__ __forceinline__ PrVal two_sum_add(const PrVal &a, const PrVal &b) {
   return PrVal{s, __fadd_rn(__fadd_rn(a.c, b.c), err)};
 }
 
+// The row epilogue of the precision PageRank: the gathered sum (value +
+// compensation) of a destination row becomes its new rank and contribution;
+// the L1 step accumulates per thread.
 struct PrPol {
   typedef PrVal Val;
-  static constexpr bool kMapNeedsVertex = false;
   const int32_t *csc_src;
   const float *inv_deg;  // RN(1 / out-degree), 0 without out-edges
   const float *contrib;
@@ -263,30 +265,19 @@ struct PrPol {
   const int32_t *seed_p;
   int32_t seed;
   double l1;
-  __device__ Val zero() const { return PrVal{0.0f, 0.0f}; }
-  __device__ __forceinline__ Val reduce(const Val &a, const Val &b) const {
-    return two_sum_add(a, b);
-  }
-  // Inside a 32-edge slab the contributions are summed as plain floats by
-  // the log-depth segmented scan (relative error <= 5 u of the slab's sum,
-  // the terms being non-negative); the slab sums of a row are combined with
-  // two-sum.
-  typedef float Scan;
-  __device__ __forceinline__ Scan to_scan(const Val &v) const { return v.s; }
-  __device__ __forceinline__ Val from_scan(Scan x) const { return PrVal{x, 0.0f}; }
-  __device__ __forceinline__ Scan scan_add(Scan a, Scan b) const { return __fadd_rn(a, b); }
-  __device__ __forceinline__ Val map(int, int, int pos) const {
-    return PrVal{__ldg(contrib + __ldg(csc_src + pos)), 0.0f};
-  }
-  __device__ __forceinline__ void emit(int, int v, const Val &g) {
+  // inv and old: the row's reciprocal out-degree and previous rank
+  __device__ __forceinline__ void emit(int v, const Val &g, float inv, float old) {
     const float sum = __fadd_rn(g.s, g.c);
     const float b = seed < 0 ? base : (v == seed ? base_seed : 0.0f);
     const float r = __fadd_rn(b, __fmul_rn(damping, sum));
     rank_new[v] = r;
-    contrib_new[v] = __fmul_rn(r, __ldg(inv_deg + v));
+    contrib_new[v] = __fmul_rn(r, inv);
     // the step in FP32 (exact while the two ranks are within a factor of
     // two of each other, Sterbenz), the sum in FP64
-    l1 += (double)fabsf(__fsub_rn(r, rank_old[v]));
+    l1 += (double)fabsf(__fsub_rn(r, old));
+  }
+  __device__ __forceinline__ void emit(int v, const Val &g) {
+    emit(v, g, __ldg(inv_deg + v), rank_old[v]);
   }
 };
 
@@ -318,32 +309,287 @@ __device__ __forceinline__ void block_sum_store(double v, double *out) {
   }
 }
 
-__global__ void __launch_bounds__(kNT)
-    k_pr_slab(PrPol pol, PrBufs bufs, gasdev::SlabSource src, PrVal *cf, PrVal *cc,
-              int32_t *ca0, int32_t *fix, int32_t *fix_n, const gas_counters *cnt,
-              double *l1_part) {
-  pr_bind(pol, bufs, cnt);
-  gasdev::slab_loop<PrPol, true>(pol, src, cf, cc, ca0, fix, fix_n);
-  block_sum_store(pol.l1, l1_part + blockIdx.x);
+// ---- merge-path gather (Merrill & Garland, "Merge-based parallel sparse
+// matrix-vector multiplication", SC'16) ----
+// The CSC is walked as one merge path of nV row ends and nE in-edges (an
+// edge is taken while its index is below the current row's end offset).  A
+// warp owns a tile of kPrW consecutive path items, a lane kPrK of them; the
+// warps of a CTA never wait for one another.  A tile stages its row end
+// offsets and the gathered contributions of its edges in the warp's shared
+// memory (coalesced index loads, kPrK independent gathers per lane), each
+// lane sums its items sequentially, a segmented warp scan of the lanes'
+// open-row partials joins rows that span lanes, and the rows that start and
+// end inside the tile are finished there with coalesced writes.  A row that
+// spans tiles leaves its first part as the tile's tail record and the
+// following parts as head records; k_pr_merge_fix joins them.
+constexpr int kPrK = 8;
+constexpr int kPrW = 32 * kPrK;
+constexpr int kPrWarps = kNT / 32;
+// s_val is padded by one word per kPrK: a lane reads about kPrK words past
+// its neighbour, which without the pad puts 32 / kPrK lanes on one bank
+__device__ __forceinline__ int pr_pad(int j) { return j + j / kPrK; }
+constexpr int kPrValWords = kPrW + kPrW / kPrK;
+
+struct PrCarry {
+  int32_t row;   // -1: no record
+  int32_t done;  // head: the row ends in this tile
+  float s, c;
+};
+
+// Merge-path coordinate (rows ended) of each tile start, once per run.
+__global__ void k_pr_tiles(const int32_t *csc_off, int nV, int nE, int n_tiles,
+                           int32_t *tile_row) {
+  const long long path = (long long)nV + nE;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t <= n_tiles;
+       t += gridDim.x * blockDim.x) {
+    const long long d = min((long long)t * kPrW, path);
+    long long lo = max(d - nE, 0LL), hi = min(d, (long long)nV);
+    while (lo < hi) {
+      const long long p = (lo + hi) >> 1;
+      if (csc_off[p + 1] <= d - p - 1)
+        lo = p + 1;
+      else
+        hi = p;
+    }
+    tile_row[t] = (int32_t)lo;
+  }
 }
 
-__global__ void __launch_bounds__(kNT)
-    k_pr_fixup(PrPol pol, PrBufs bufs, gasdev::SlabSource src, const PrVal *cf,
-               const PrVal *cc, const int32_t *ca0, const int32_t *fix,
-               const int32_t *fix_n, const gas_counters *cnt, double *l1_part) {
-  pr_bind(pol, bufs, cnt);
-  gasdev::slab_fixup_loop<PrPol>(pol, src, cf, cc, ca0, fix, fix_n);
-  block_sum_store(pol.l1, l1_part + blockIdx.x);
+__device__ __forceinline__ int32_t pr_ld_stream(const int32_t *p) {
+  int32_t v;
+  asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
 }
 
-// Vertices without in-edges: rank = (1-d)/N.
-__global__ void __launch_bounds__(kNT)
-    k_pr_empty(PrPol pol, PrBufs bufs, const int32_t *zero_vid, int n_zero,
+__global__ void __launch_bounds__(kNT, 3)
+    k_pr_merge(PrPol pol, PrBufs bufs, const int32_t *csc_off, int nV, int nE,
+               const int32_t *tile_row, int n_tiles, PrCarry *head, PrCarry *tail,
                const gas_counters *cnt, double *l1_part) {
+  __shared__ int32_t s_end_all[kPrWarps][kPrW + 1];
+  __shared__ float s_val_all[kPrWarps][kPrValWords];
+  __shared__ float2 s_sum_all[kPrWarps][kPrW];
   pr_bind(pol, bufs, cnt);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_zero;
-       i += gridDim.x * blockDim.x)
-    pol.emit(0, zero_vid[i], pol.zero());
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t *s_end = s_end_all[warp];
+  float *s_val = s_val_all[warp];
+  float2 *s_sum = s_sum_all[warp];
+  const long long path = (long long)nV + nE;
+  const int nwarps = gridDim.x * kPrWarps;
+  // software pipeline: the next tile's coordinates and edge indices load
+  // while this tile's gathers and sums run
+  int tile = blockIdx.x * kPrWarps + warp;
+  int r0 = 0, r1 = 0;
+  int idx[kPrK];
+  if (tile < n_tiles) {
+    r0 = tile_row[tile];
+    r1 = tile_row[tile + 1];
+    const int e0 = (int)((long long)tile * kPrW - r0);
+    const int ne = (int)(min((long long)tile * kPrW + kPrW, path) - r1) - e0;
+#pragma unroll
+    for (int k = 0; k < kPrK; ++k) {
+      const int j = lane + 32 * k;
+      idx[k] = j < ne ? pr_ld_stream(pol.csc_src + e0 + j) : 0;
+    }
+  }
+  for (; tile < n_tiles; tile += nwarps) {
+    const long long D0 = (long long)tile * kPrW;
+    const long long D1 = min(D0 + kPrW, path);
+    const int e0 = (int)(D0 - r0), e1 = (int)(D1 - r1);
+    const int nrows = r1 - r0, ne = e1 - e0;
+    float val[kPrK];
+#pragma unroll
+    for (int k = 0; k < kPrK; ++k) {
+      const int j = lane + 32 * k;
+      val[k] = j < ne ? __ldg(pol.contrib + idx[k]) : 0.0f;
+    }
+    const int off0 = csc_off[r0];
+#pragma unroll
+    for (int k = 0; k < kPrK; ++k) {
+      const int j = lane + 32 * k;
+      if (j < nrows) s_end[j] = csc_off[r0 + 1 + j];
+    }
+    if (lane == 0) s_end[nrows] = INT_MAX;
+    const int next = tile + nwarps;
+    int nr0 = 0, nr1 = 0;
+    if (next < n_tiles) {
+      nr0 = tile_row[next];
+      nr1 = tile_row[next + 1];
+      const int ne0 = (int)((long long)next * kPrW - nr0);
+      const int nne = (int)(min((long long)next * kPrW + kPrW, path) - nr1) - ne0;
+#pragma unroll
+      for (int k = 0; k < kPrK; ++k) {
+        const int j = lane + 32 * k;
+        idx[k] = j < nne ? pr_ld_stream(pol.csc_src + ne0 + j) : 0;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kPrK; ++k) {
+      const int j = lane + 32 * k;
+      if (j < ne) s_val[pr_pad(j)] = val[k];
+    }
+    // the epilogue's inputs for the tile's first 32 rows
+    float inv0 = 0.0f, old0 = 0.0f;
+    if (lane < nrows) {
+      inv0 = __ldg(pol.inv_deg + r0 + lane);
+      old0 = pol.rank_old[r0 + lane];
+    }
+    __syncwarp();
+    // this lane's kPrK items: find its start on the tile's path
+    const int tlen = nrows + ne;
+    const int dt = min(lane * kPrK, tlen), dend = min(dt + kPrK, tlen);
+    int lo = max(dt - ne, 0), hi = min(dt, nrows);
+    while (lo < hi) {
+      const int p = (lo + hi) >> 1;
+      if (s_end[p] <= e0 + dt - p - 1)
+        lo = p + 1;
+      else
+        hi = p;
+    }
+    int r = lo, e = e0 + dt - lo;
+    int end_r = s_end[r];
+    float acc = 0.0f, first = 0.0f;
+    int first_r = 0;
+    bool ended = false;
+#pragma unroll
+    for (int k = 0; k < kPrK; ++k) {
+      if (dt + k < dend) {
+        if (e < end_r) {
+          acc = __fadd_rn(acc, s_val[pr_pad(e - e0)]);
+          ++e;
+        } else {
+          if (!ended) {
+            first = acc;
+            first_r = r;
+          } else {
+            s_sum[r] = make_float2(acc, 0.0f);
+          }
+          ended = true;
+          acc = 0.0f;
+          ++r;
+          end_r = s_end[r];
+        }
+      }
+    }
+    // segmented inclusive scan of the open-row partials (a lane that ended
+    // a row starts a segment)
+    PrVal v{acc, 0.0f};
+    int f = ended;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const PrVal u{__shfl_up_sync(0xffffffffu, v.s, o), __shfl_up_sync(0xffffffffu, v.c, o)};
+      const int g = __shfl_up_sync(0xffffffffu, f, o);
+      if (lane >= o) {
+        if (!f) v = two_sum_add(u, v);
+        f |= g;
+      }
+    }
+    PrVal cin{__shfl_up_sync(0xffffffffu, v.s, 1), __shfl_up_sync(0xffffffffu, v.c, 1)};
+    if (lane == 0) cin = PrVal{0.0f, 0.0f};
+    if (ended) {
+      const PrVal t = two_sum_add(cin, PrVal{first, 0.0f});
+      s_sum[first_r] = make_float2(t.s, t.c);
+    }
+    const PrVal tot{__shfl_sync(0xffffffffu, v.s, 31), __shfl_sync(0xffffffffu, v.c, 31)};
+    __syncwarp();
+    // rows that start and end in this tile; row r0 started in an earlier
+    // tile when e0 is past its first edge
+    const bool split = e0 > off0;
+    if (lane < nrows && !(lane == 0 && split)) {
+      const float2 t = s_sum[lane];
+      pol.emit(r0 + lane, PrVal{t.x, t.y}, inv0, old0);
+    }
+    for (int i = lane + 32; i < nrows; i += 32) {
+      const float2 t = s_sum[i];
+      pol.emit(r0 + i, PrVal{t.x, t.y});
+    }
+    if (lane == 0) {
+      PrCarry h{-1, 0, 0.0f, 0.0f}, tl{-1, 0, 0.0f, 0.0f};
+      if (split) {
+        if (nrows > 0)
+          h = PrCarry{r0, 1, s_sum[0].x, s_sum[0].y};
+        else
+          h = PrCarry{r0, 0, tot.s, tot.c};
+      }
+      if (r1 < nV && !(split && nrows == 0)) {
+        const int off_r1 = nrows > 0 ? s_end[nrows - 1] : off0;
+        if (e1 > max(off_r1, e0)) tl = PrCarry{r1, 0, tot.s, tot.c};
+      }
+      head[tile] = h;
+      tail[tile] = tl;
+    }
+    __syncwarp();
+    r0 = nr0;
+    r1 = nr1;
+  }
+  block_sum_store(pol.l1, l1_part + blockIdx.x);
+}
+
+// Rows that span tiles.  A thread per tile with a tail record: when the
+// next tile's head ends the row (a row of fewer than about kPrW in-edges),
+// the two parts are the row.  Longer rows are walked by the whole warp, 32
+// head records at a time, up to the tile the row ends in.  A broken chain
+// sets the device error word instead of a rank.
+__global__ void __launch_bounds__(kNT)
+    k_pr_merge_fix(PrPol pol, PrBufs bufs, const PrCarry *head, const PrCarry *tail,
+                   int n_tiles, gas_counters *cnt, double *l1_part) {
+  pr_bind(pol, bufs, cnt);
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * kNT;
+  bool bad = false;
+  for (int t0 = blockIdx.x * kNT + (threadIdx.x & ~31); t0 < n_tiles; t0 += stride) {
+    const int t = t0 + lane;
+    PrCarry tl{-1, 0, 0.0f, 0.0f};
+    if (t < n_tiles) tl = tail[t];
+    bool walk = false;
+    if (tl.row >= 0) {
+      if (t + 1 < n_tiles) {
+        const PrCarry h = head[t + 1];
+        bad |= h.row != tl.row;
+        if (h.done)
+          pol.emit(tl.row, two_sum_add(PrVal{tl.s, tl.c}, PrVal{h.s, h.c}));
+        else
+          walk = true;
+      } else {
+        bad = true;
+      }
+    }
+    unsigned m = __ballot_sync(0xffffffffu, walk);
+    while (m) {
+      const int src_lane = __ffs(m) - 1;
+      m &= m - 1;
+      const int wt = __shfl_sync(0xffffffffu, t, src_lane);
+      const int row = __shfl_sync(0xffffffffu, tl.row, src_lane);
+      PrVal sum{__shfl_sync(0xffffffffu, tl.s, src_lane),
+                __shfl_sync(0xffffffffu, tl.c, src_lane)};
+      if (lane != 0) sum = PrVal{0.0f, 0.0f};
+      bool done = false;
+      for (int c = wt + 1; c < n_tiles && !done; c += 32) {
+        const int i = c + lane;
+        PrCarry h{-1, 0, 0.0f, 0.0f};
+        if (i < n_tiles) h = head[i];
+        const unsigned dm = __ballot_sync(0xffffffffu, i < n_tiles && h.done);
+        const int stop = dm ? __ffs(dm) - 1 : 31;
+        if (lane <= stop && i < n_tiles) {
+          bad |= h.row != row;
+          sum = two_sum_add(sum, PrVal{h.s, h.c});
+        }
+        done = dm != 0u;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const PrVal u{__shfl_down_sync(0xffffffffu, sum.s, o),
+                      __shfl_down_sync(0xffffffffu, sum.c, o)};
+        sum = two_sum_add(sum, u);
+      }
+      if (lane == 0) {
+        if (done)
+          pol.emit(row, sum);
+        else
+          bad = true;
+      }
+    }
+  }
+  if (bad) atomicExch(&cnt->error, (int32_t)GAS_ERR_DEVICE);
   block_sum_store(pol.l1, l1_part + blockIdx.x);
 }
 
@@ -364,7 +610,7 @@ __global__ void __launch_bounds__(kNT)
   if (threadIdx.x == 0) {
     const double l1 = s[0];
     const double tol = *tol_p;
-    *fix_n = 0;  // the fixup of this iteration has run
+    if (fix_n) *fix_n = 0;  // the fixup of this iteration has run
     const int max_iter = cnt->max_iter;
     *residual = l1;
     const int it = ++cnt->iteration;
@@ -394,10 +640,11 @@ __global__ void k_pr_init(float *rank, float *contrib, float *inv_deg, const int
 struct PrCtx {
   PrPol pol;
   PrBufs bufs;
-  gasdev::SlabSource src;
-  int tiles_grid;
+  int32_t *tile_row;
+  PrCarry *head, *tail;
+  int n_tiles;
+  int merge_grid;
   int fix_grid;
-  int empty_grid;
   double *residual;
 };
 
@@ -408,20 +655,14 @@ gas_status_t pr_body(gas_engine *e, cudaStream_t cs,
   // source's contribution; per vertex offsets, old and new rank, new
   // contribution
   gas::prof_begin(e, cs, gas::kProfPagerank, 8LL * e->nE + 16LL * e->nV);
-  k_pr_slab<<<c->tiles_grid, kNT, 0, cs>>>(
-      c->pol, c->bufs, c->src, (PrVal *)e->slab_first, (PrVal *)e->slab_carry,
-      e->slab_a0, e->slab_fix, e->slab_fix_n, e->cnt, e->pr_l1);
-  k_pr_fixup<<<c->fix_grid, kNT, 0, cs>>>(
-      c->pol, c->bufs, c->src, (const PrVal *)e->slab_first,
-      (const PrVal *)e->slab_carry, e->slab_a0, e->slab_fix, e->slab_fix_n, e->cnt,
-      e->pr_l1 + c->tiles_grid);
+  k_pr_merge<<<c->merge_grid, kNT, 0, cs>>>(c->pol, c->bufs, e->csc_off, e->nV, e->nE,
+                                            c->tile_row, c->n_tiles, c->head, c->tail,
+                                            e->cnt, e->pr_l1);
+  k_pr_merge_fix<<<c->fix_grid, kNT, 0, cs>>>(c->pol, c->bufs, c->head, c->tail, c->n_tiles,
+                                              e->cnt, e->pr_l1 + c->merge_grid);
   gas::prof_end(e, cs);
-  k_pr_empty<<<c->empty_grid, kNT, 0, cs>>>(c->pol, c->bufs, e->zero_vid, e->n_zero,
-                                            e->cnt,
-                                            e->pr_l1 + c->tiles_grid + c->fix_grid);
-  k_pr_finish<<<1, kNT, 0, cs>>>(e->pr_l1, c->tiles_grid + c->fix_grid + c->empty_grid,
-                                 c->residual + 1, e->cnt, c->residual, e->slab_fix_n, h,
-                                 e->in_graph ? 1 : 0);
+  k_pr_finish<<<1, kNT, 0, cs>>>(e->pr_l1, c->merge_grid + c->fix_grid, c->residual + 1,
+                                 e->cnt, c->residual, nullptr, h, e->in_graph ? 1 : 0);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
@@ -455,12 +696,30 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
   if (!e->pr_seed) CUDA_TRY(cudaMalloc(&e->pr_seed, sizeof(int32_t)));
   if (!e->pr_inv_deg) CUDA_TRY(cudaMalloc(&e->pr_inv_deg, (size_t)nV * 4));
   PrCtx c;
+  const long long path = (long long)nV + e->nE;
+  c.n_tiles = (int)((path + kPrW - 1) / kPrW);
+  if (!e->pr_tile_row || e->pr_tile_cap < c.n_tiles) {
+    if (e->pr_tile_row) cudaFree(e->pr_tile_row);
+    if (e->pr_head) cudaFree(e->pr_head);
+    if (e->pr_tail) cudaFree(e->pr_tail);
+    e->pr_tile_row = nullptr;
+    e->pr_head = e->pr_tail = nullptr;
+    e->pr_tile_cap = 0;
+    if (e->graphs[kGraphPagerank]) cudaGraphExecDestroy(e->graphs[kGraphPagerank]);
+    e->graphs[kGraphPagerank] = nullptr;
+    CUDA_TRY(cudaMalloc(&e->pr_tile_row, ((size_t)c.n_tiles + 1) * 4));
+    CUDA_TRY(cudaMalloc(&e->pr_head, (size_t)c.n_tiles * sizeof(PrCarry)));
+    CUDA_TRY(cudaMalloc(&e->pr_tail, (size_t)c.n_tiles * sizeof(PrCarry)));
+    e->pr_tile_cap = c.n_tiles;
+  }
+  c.tile_row = e->pr_tile_row;
+  c.head = static_cast<PrCarry *>(e->pr_head);
+  c.tail = static_cast<PrCarry *>(e->pr_tail);
   int per_sm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pr_slab, kNT, 0));
-  c.tiles_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);  // resident CTAs only
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pr_merge, kNT, 0));
+  c.merge_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);  // resident CTAs only
   c.fix_grid = 2 * e->num_sms;
-  c.empty_grid = 2 * e->num_sms;
-  const int nparts = c.tiles_grid + c.fix_grid + c.empty_grid;
+  const int nparts = c.merge_grid + c.fix_grid;
   if (!e->pr_l1 || e->pr_l1_cap < nparts + 2) {
     if (e->pr_l1) cudaFree(e->pr_l1);
     e->pr_l1 = nullptr;
@@ -482,8 +741,6 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
   c.bufs.rank[1] = e->pr_rank[1];
   c.bufs.contrib[0] = e->pr_contrib[0];
   c.bufs.contrib[1] = e->pr_contrib[1];
-  c.src = gasdev::slab_source(e->ne_end, e->ne_vid, nullptr, e->n_ne, e->nE, nullptr,
-                              nullptr, e->slab_dpart);
 
   // damping is baked into the captured policy: rebuild when it changes
   if (e->graphs[kGraphPagerank] && e->pr_damping != damping) {
@@ -499,7 +756,8 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
                            cudaMemcpyHostToDevice, S(stream)));
   CUDA_TRY(cudaMemcpyAsync(e->pr_seed, &seed, sizeof(int32_t), cudaMemcpyHostToDevice,
                            S(stream)));
-  gasdev::k_slab_partition<><<<2 * e->num_sms, 256, 0, S(stream)>>>(c.src, e->slab_dpart);
+  k_pr_tiles<<<gas::engine_grid(c.n_tiles + 1, kNT, 2 * e->num_sms), kNT, 0, S(stream)>>>(
+      e->csc_off, nV, e->nE, c.n_tiles, e->pr_tile_row);
   if (init)
     CUDA_TRY(cudaMemcpyAsync(e->pr_rank[0], init, (size_t)nV * 4, cudaMemcpyDefault,
                              S(stream)));
@@ -531,7 +789,7 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
   if (stats) {
     stats->iterations = cnt.iteration;
     stats->pull_iters = cnt.iteration;
-    stats->kernel_launches = 4 * cnt.iteration + 3;
+    stats->kernel_launches = 3 * cnt.iteration + 3;
     stats->edges_processed = (int64_t)cnt.iteration * e->nE;
     stats->residual = resid;
   }

@@ -135,6 +135,41 @@ def test_pagerank_precision_against_fp64_oracle(scale, seed):
     assert st.residual <= 1e-6
 
 
+def _tile_spanning_graphs():
+    """Rows that span many merge-path tiles (2,048 path items each): a hub
+    with 200,000 in-edges (about 100 tiles, several 32-record fix-up rounds),
+    one more at the last vertex (the path's last tile), a scattered ring,
+    and thousands of rows without in-edges; a graph with no edges; one
+    vertex with a self-loop."""
+    nV = 300_000
+    a = np.arange(1, 200_001, dtype=np.int32)
+    b = np.arange(200_001, 270_001, dtype=np.int32)
+    v = np.arange(0, nV, 3, dtype=np.int64)
+    src = np.concatenate([a, b, v.astype(np.int32)])
+    dst = np.concatenate([np.zeros_like(a), np.full_like(b, nV - 1),
+                          ((v * 7 + 3) % nV).astype(np.int32)])
+    return [EdgeList(nV, src, dst),
+            EdgeList(1000, np.zeros(0, np.int32), np.zeros(0, np.int32)),
+            EdgeList(1, np.zeros(1, np.int32), np.zeros(1, np.int32))]
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_pagerank_precision_rows_spanning_tiles(k):
+    el = _tile_spanning_graphs()[k]
+    ref, rit, rl1 = oracle.pagerank_fp64(el.nV, el.src, el.dst, 0.85, 1e-6)
+    eng = GASEngineGPU("pagerank")
+    vd = initial_vertex_data("pagerank", el.nV, 0, el.out_degree())
+    eng.setGraph(el.nV, vd, el.nE, None, el.src, el.dst)
+    for _ in range(2):   # the second run reuses the captured loop
+        ranks, st = eng.pagerank_precision(0.85, 1e-6)
+        err = np.abs(ranks.astype(np.float64) - ref)
+        assert err.sum() <= 1e-6, err.sum()
+        assert err.max() <= 1e-7
+        assert abs(st.iterations - rit) <= 1
+        assert st.residual <= 1e-6
+    eng.close()
+
+
 def test_gather_without_apply_then_scatter():
     """gather() followed by scatterActivate() without apply(): the reference
     runs the gather and keeps the previous apply flags."""
