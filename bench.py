@@ -867,6 +867,11 @@ def run_batched(args):
 # precision-form PageRank: R-MAT scale 24, directed
 # ---------------------------------------------------------------------------
 PR_SCALE, PR_SEED = 24, 4
+# DRAM bytes (read + write) of one iteration's gather at scale 24 (k_pr_merge
+# 1.477 + 0.154 GB, k_pr_merge_fix 0.016 GB), from one full ncu capture:
+#   GAS_HOST_LOOP=1 ncu --set full --clock-control none -k regex:k_pr_merge -s 6 -c 2 \
+#     python bench.py --workload pagerank --launch-list
+PR_TRAFFIC = {24: 1.647e9}
 PR_METRIC = "GTEPS (precision PageRank, R-MAT scale 24 directed, E x iterations / time)"
 
 
@@ -956,7 +961,8 @@ def run_pagerank(args):
                                                           r_warm).sum())},
         "roofline": {"kernel": "k_pr_merge + k_pr_merge_fix (one PageRank iteration's gather)",
                      "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": PR_TRAFFIC.get(scale),
                      "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": int(prof.pagerank_bytes /
                                                          max(1, prof.pagerank_launches)),
