@@ -6,7 +6,8 @@
 //
 //   * multi-source BFS: lane l of a vertex belongs to source l of the
 //     vertex's own graph (graphs are disjoint, so lanes of different graphs
-//     never meet).  visited[v] and next[v] are 32-bit lane masks.  One level
+//     never meet).  vn[v] = {visited, next}, two 32-bit lane masks in one
+//     8-byte record, so a push reads both with one access.  One level
 //     pushes every queued vertex's new-lane mask to its out-neighbours
 //     (atomicOr, pre-filtered by visited), marking touched vertices in a
 //     bitmap; a two-pass compaction over that bitmap writes the level into
@@ -99,8 +100,7 @@ struct MsPushPol {
   static constexpr bool kMapNeedsVertex = false;
   const int32_t *csr_dst;
   const int32_t *q_mask;
-  const uint32_t *visited;
-  uint32_t *next;
+  uint32_t *vn;  // [V][2]: visited, next
   uint32_t *tbits;
   __device__ Val zero() const { return 0; }
   __device__ Val reduce(Val a, Val) const { return a; }
@@ -113,9 +113,10 @@ struct MsPushPol {
   // as touched (both reductions, no thread waits for a result).
   __device__ __forceinline__ void visit(int a, int, int pos) const {
     const int v = __ldg(csr_dst + pos);
-    const uint32_t m = (uint32_t)__ldg(q_mask + a) & ~visited[v];
-    if (m && (next[v] & m) != m) {
-      atomicOr(next + v, m);  // fire-and-forget; the touched bit is idempotent
+    const uint2 p = reinterpret_cast<const uint2 *>(vn)[v];
+    const uint32_t m = (uint32_t)__ldg(q_mask + a) & ~p.x;
+    if (m && (p.y & m) != m) {
+      atomicOr(vn + 2 * (size_t)v + 1, m);  // fire-and-forget; the touched bit is idempotent
       atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
     }
   }
@@ -128,12 +129,12 @@ __global__ void __launch_bounds__(kNT)
 
 // Level 0: every (graph, lane) source.
 __global__ void k_ms_seed(const int32_t *src_global, const BatchParams *prm, int L,
-                          uint32_t *next, uint32_t *tbits) {
+                          uint32_t *vn, uint32_t *tbits) {
   const int n = prm->n_sources;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int v = src_global[i];
     if (v < 0) continue;
-    atomicOr(next + v, 1u << (i % L));
+    atomicOr(vn + 2 * (size_t)v + 1, 1u << (i % L));
     atomicOr(tbits + ((uint32_t)v >> 5), 1u << (v & 31));
   }
 }
@@ -152,8 +153,10 @@ struct MsWarp {
   int deg[kMsWarpWords];
 };
 
+// next: the SSSP's changed-lane words; vn (BFS, next unused): the
+// {visited, next} pairs, new lanes = next & ~visited
 __device__ __forceinline__ void ms_load(const uint32_t *tbits, const uint32_t *next,
-                                        const uint32_t *visited, const int32_t *csr_off,
+                                        const uint32_t *vn, const int32_t *csr_off,
                                         int nW, int w0, MsWarp &w) {
   const int lane = threadIdx.x & 31;
   w.myword = (lane < kMsWarpWords && w0 + lane < nW) ? tbits[w0 + lane] : 0u;
@@ -165,7 +168,12 @@ __device__ __forceinline__ void ms_load(const uint32_t *tbits, const uint32_t *n
     w.deg[i] = 0;
     if ((word >> lane) & 1u) {
       const int v = (w0 + i) * 32 + lane;
-      w.nw[i] = visited ? next[v] & ~visited[v] : next[v];
+      if (vn) {
+        const uint2 p = reinterpret_cast<const uint2 *>(vn)[v];
+        w.nw[i] = p.y & ~p.x;
+      } else {
+        w.nw[i] = next[v];
+      }
       w.off[i] = csr_off[v];
       w.deg[i] = csr_off[v + 1] - w.off[i];
     }
@@ -192,14 +200,14 @@ __device__ __forceinline__ void ms_totals(const MsWarp &w, int &q, int &d) {
 // Pass 1: per block (queue entries, out-edges); with lanes_active, also
 // the OR of the new lanes of the queue's entries (the SSSP loop).
 __global__ void __launch_bounds__(kNT)
-    k_ms_count(const uint32_t *tbits, const uint32_t *next, const uint32_t *visited,
+    k_ms_count(const uint32_t *tbits, const uint32_t *next, const uint32_t *vn,
                const int32_t *csr_off, int nW, int32_t *part, uint32_t *lanes_active) {
   __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   __shared__ uint32_t s_l[kNT / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
   MsWarp w;
-  ms_load(tbits, next, visited, csr_off, nW, w0, w);
+  ms_load(tbits, next, vn, csr_off, nW, w0, w);
   int q, d;
   ms_totals(w, q, d);
   uint32_t lanes = 0u;
@@ -234,7 +242,7 @@ __global__ void __launch_bounds__(kNT)
 // counted), visited, the next queue and the push's chunk partition at the
 // chunk size the spine chose; clears next and the touched bitmap.
 __global__ void __launch_bounds__(kNT, 5)
-    k_ms_write(uint32_t *tbits, uint32_t *next, uint32_t *visited, const int32_t *csr_off,
+    k_ms_write(uint32_t *tbits, uint32_t *vn, const int32_t *csr_off,
                int nW, const int32_t *part, int L, const gas_counters *cnt,
                int32_t *depth, int32_t *q_mask, int32_t *q_end, int32_t *q_delta,
                int32_t *chunk_row) {
@@ -249,7 +257,7 @@ __global__ void __launch_bounds__(kNT, 5)
   if (lane == 0) s_nbig[warp] = 0;
   const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
   MsWarp w;
-  ms_load(tbits, next, visited, csr_off, nW, w0, w);
+  ms_load(tbits, nullptr, vn, csr_off, nW, w0, w);
   int q, d;
   ms_totals(w, q, d);
   if (lane == 0) {
@@ -270,9 +278,9 @@ __global__ void __launch_bounds__(kNT, 5)
     if (!word) continue;  // warp-uniform
     const bool touched = (word >> lane) & 1u;
     const uint32_t nw = w.nw[i];
-    if (touched) next[v] = 0u;
+    if (touched) vn[2 * (size_t)v + 1] = 0u;
     if (nw) {
-      visited[v] |= nw;
+      vn[2 * (size_t)v] |= nw;
       for (uint32_t m = nw; m; m &= m - 1) depth[(size_t)v * L + (__ffs(m) - 1)] = level;
     }
     const int deg = nw ? w.deg[i] : 0;
@@ -895,7 +903,7 @@ struct gas_batch {
   unsigned long long *edges = nullptr;  // BFS edges pushed
   double *resid = nullptr;        // [1 + 32] max and per-lane PPR residual
   // BFS
-  uint32_t *visited = nullptr, *next = nullptr, *tbits = nullptr;
+  uint32_t *vn = nullptr, *next = nullptr, *tbits = nullptr;  // vn: [V][2] BFS pairs
   int32_t *depth = nullptr, *q_mask = nullptr, *q_end = nullptr,
           *q_delta = nullptr, *part = nullptr, *qpart = nullptr, *srcs = nullptr;
   int32_t depth_lanes = 0, srcs_cap = 0;
@@ -937,7 +945,7 @@ void drop_graph(gas_batch *b) {
 
 void free_state(gas_batch *b) {
   drop_graph(b);
-  bfree(b->visited); bfree(b->next); bfree(b->tbits); bfree(b->depth);
+  bfree(b->vn); bfree(b->next); bfree(b->tbits); bfree(b->depth);
   bfree(b->q_mask); bfree(b->q_end); bfree(b->q_delta);
   bfree(b->part); bfree(b->qpart); bfree(b->srcs);
   bfree(b->first_row); bfree(b->fix); bfree(b->head); bfree(b->tail);
@@ -1008,7 +1016,7 @@ gas_status_t ensure_bfs(gas_batch *b, int lanes, int n_sources) {
   gas_engine *e = b->eng;
   const size_t nV = std::max(1, e->nV);
   GAS_TRY(ensure_frontier(b));
-  if (!b->visited) CUDA_TRY(cudaMalloc(&b->visited, nV * 4));
+  if (!b->vn) CUDA_TRY(cudaMalloc(&b->vn, nV * 8));
   if (b->depth_lanes != lanes) {
     drop_graph(b);
     bfree(b->depth);
@@ -1133,12 +1141,12 @@ gas_status_t bfs_compact(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h
   gas_batch *b = c->b;
   gas_engine *e = b->eng;
   const int nb = ms_blocks(b);
-  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
+  k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, nullptr, b->vn, e->csr_off, nwords(b), b->qpart,
                                 nullptr);
   k_mss_spine<<<1, kMssSpineNT, 0, s>>>(reinterpret_cast<int2 *>(b->qpart), nb, b->cnt,
                                         c->slab_grid * (kNT / 32), b->edges, nullptr, nullptr,
                                         h, ig, first);
-  k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, b->visited, e->csr_off, nwords(b), b->qpart,
+  k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->vn, e->csr_off, nwords(b), b->qpart,
                                c->bfs_lanes, b->cnt, b->depth, b->q_mask, b->q_end, b->q_delta,
                                b->part);
   CUDA_TRY(cudaGetLastError());
@@ -1151,11 +1159,10 @@ gas_status_t bfs_prologue(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle 
   const size_t nV = std::max(1, e->nV), nW = std::max(1, nwords(b));
   const int L = c->bfs_lanes;
   k_b_reset<<<1, 1, 0, s>>>(b->cnt, b->prm, 0, b->edges);
-  CUDA_TRY(cudaMemsetAsync(b->visited, 0, nV * 4, s));
-  CUDA_TRY(cudaMemsetAsync(b->next, 0, nV * 4, s));
+  CUDA_TRY(cudaMemsetAsync(b->vn, 0, nV * 8, s));
   CUDA_TRY(cudaMemsetAsync(b->tbits, 0, nW * 4, s));
   CUDA_TRY(cudaMemsetAsync(b->depth, 0xff, nV * L * 4, s));
-  k_ms_seed<<<2 * e->num_sms, 256, 0, s>>>(b->srcs, b->prm, L, b->next, b->tbits);
+  k_ms_seed<<<2 * e->num_sms, 256, 0, s>>>(b->srcs, b->prm, L, b->vn, b->tbits);
   return bfs_compact(c, s, h, ig, 1);
 }
 
@@ -1165,7 +1172,7 @@ gas_status_t bfs_push(RunCtx *c, cudaStream_t s) {
   const gasdev::SlabSource q = gasdev::slab_source(
       b->q_end, nullptr, b->q_delta, 0, 0, &b->cnt->n_changed, &b->cnt->n_scatter_edges,
       b->part, &b->cnt->push_chunk_log2);
-  MsPushPol pol{e->csr_dst, b->q_mask, b->visited, b->next, b->tbits};
+  MsPushPol pol{e->csr_dst, b->q_mask, b->vn, b->tbits};
   k_ms_push<<<c->slab_grid, kNT, 0, s>>>(pol, q);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
