@@ -592,6 +592,11 @@ def run_lanes24(args):
     b.build(sp)
     depth_d = torch.empty((el.nV, L), dtype=torch.int32, device=dev)
     run_b = lambda: b.run(bfs_sources=srcs[None, :], depth_out=depth_d.data_ptr(), stream=sp)
+    if args.launch_list:
+        # one batched BFS run and nothing else (for an ncu launch list / capture)
+        r = run_b()
+        torch.cuda.synchronize()
+        return {"launch_list": True, "bfs_levels": r.stats.bfs_iterations}
     run_b()
     depth = depth_d.cpu().numpy()
     od = el.out_degree().astype(np.int64)
@@ -622,8 +627,16 @@ def run_lanes24(args):
     e.download_vertex_data(one.numpy(), sp)
     same = bool(np.array_equal(one.numpy(), depth[:, 0]))
     ms_plain_b = timed(plain_bfs, 1, 1)
+    # the single-source engine's push roofline over the same 16 runs
+    e.set_profiling(True)
+    e.profile(reset=True)
+    plain_bfs()
+    torch.cuda.synchronize()
+    pe = e.profile()
+    e.set_profiling(False)
     e.close()
     b.close()
+    ach1 = pe.push_bytes / (pe.push_ms * 1e-3) / 1e9 if pe.push_ms > 0 else 0.0
     ach = pb.push_bytes / (pb.push_ms * 1e-3) / 1e9 if pb.push_ms > 0 else 0.0
     out["bfs"] = {"graph": f"rmat-s{scale}-ef{EDGE_FACTOR}-sym seed {GRAPH_SEED}",
                   "V": el.nV, "E": el.nE, "lanes": L, "ms": round(ms_b, 3),
@@ -631,6 +644,11 @@ def run_lanes24(args):
                   "plain_one_by_one_ms": round(ms_plain_b, 3),
                   "speedup_vs_plain": round(ms_plain_b / ms_b, 3),
                   "lane0_equals_single_source_run": same,
+                  "plain_push_roofline": {"kernel": "k_push (single-source BFS, learned)",
+                                          "achieved": round(ach1, 1), "unit": "GB/s",
+                                          "frac": round(ach1 / peak, 4),
+                                          "launches": pe.push_launches,
+                                          "pull_launches": pe.pull_launches},
                   "roofline": {"kernel": "k_ms_push (16-lane BFS push)", "bound": "hbm",
                                "achieved": round(ach, 1), "unit": "GB/s", "peak": peak,
                                "frac": round(ach / peak, 4), "peak_source": peak_kind,
