@@ -95,7 +95,7 @@ def test_multi_source_bfs_bit_exact(batch, L):
     assert res.stats.bfs_edges > 0
 
 
-@pytest.mark.parametrize("L", [1, 5, 16, 32])
+@pytest.mark.parametrize("L", [1, 4, 5, 8, 12, 16, 20, 32])
 def test_multi_seed_ppr_within_tolerance(batch, L):
     b, gs = batch
     seeds = _lanes(gs, L, seed=100 + L)
