@@ -8,6 +8,7 @@
 //     convergence on the device.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -718,7 +719,10 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
   int per_sm = 0;
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pr_merge, kNT, 0));
   c.merge_grid = e->num_sms * (per_sm > 0 ? per_sm : 1);  // resident CTAs only
-  c.fix_grid = 2 * e->num_sms;
+  // a thread per tile record, at most 16 CTAs per SM: the records' loads
+  // are dependent chains, so they want many threads in flight
+  c.fix_grid = (int)std::min<long long>(16LL * e->num_sms,
+                                        std::max(1, (c.n_tiles + kNT - 1) / kNT));
   const int nparts = c.merge_grid + c.fix_grid;
   if (!e->pr_l1 || e->pr_l1_cap < nparts + 2) {
     if (e->pr_l1) cudaFree(e->pr_l1);
