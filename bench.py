@@ -53,7 +53,7 @@ RMAT_ABC = (0.57, 0.19, 0.19)
 GRAPH_SEED, WEIGHT_SEED, SOURCE_SEED = 2, 3, 2
 N_SOURCES = 8
 N_ISLANDS, ISLAND_SIDE = 4096, 32
-METRIC = "GTEPS (SSSP x8 + CC, R-MAT scale 22)"
+METRIC = "GTEPS (SSSP x8 + CC, R-MAT scale {scale})"
 MAX_ITERS = 20000  # far above any run of this workload; bounds a device loop
 # Per-launch DRAM bytes (read + write) of the dominant kernel, by (kernel,
 # scale, edge placement, schedule): one-pass ncu metrics over every launch of
@@ -397,7 +397,8 @@ def run_ours(args, rank, world):
     roof["peak_source"] = peak_kind
 
     result = {
-        "metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": world,
+        "metric": METRIC.format(scale=args.scale), "value": round(value, 4), "unit": "GTEPS",
+        "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded R-MAT + grid islands; reference datasets unavailable)",
@@ -918,7 +919,7 @@ PR_SCALE, PR_SEED = 24, 4
 #   GAS_HOST_LOOP=1 ncu --set full --clock-control none -k regex:k_pr_merge -s 6 -c 2 \
 #     python bench.py --workload pagerank --launch-list
 PR_TRAFFIC = {24: 1.647e9}
-PR_METRIC = "GTEPS (precision PageRank, R-MAT scale 24 directed, E x iterations / time)"
+PR_METRIC = "GTEPS (precision PageRank, R-MAT scale {scale} directed, E x iterations / time)"
 
 
 def run_pagerank(args):
@@ -991,7 +992,7 @@ def run_pagerank(args):
     achieved = prof.pagerank_bytes / (prof.pagerank_ms * 1e-3) / 1e9 if prof.pagerank_ms else 0
     units = el.nE * st_u.iterations
     res = {
-        "metric": PR_METRIC, "value": round(units / (ms * 1e-3) / 1e9, 4), "unit": "GTEPS",
+        "metric": PR_METRIC.format(scale=scale), "value": round(units / (ms * 1e-3) / 1e9, 4), "unit": "GTEPS",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (two-sum compensated gather) + f64 residual",
@@ -1066,7 +1067,7 @@ def run_reference(args):
     value = statistics.median(vals)
     sample = (f"SSSP from {n} of the {N_SOURCES} sources, one thread each, on the scale-"
               f"{args.scale} graph (CC part of the step not sampled)")
-    return {"metric": METRIC, "value": round(value, 5), "unit": "GTEPS", "n_gpus": args.gpus,
+    return {"metric": METRIC.format(scale=args.scale), "value": round(value, 5), "unit": "GTEPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * statistics.median(walls), 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
