@@ -499,11 +499,11 @@ void free_graph(gas_engine *e) {
   e->edges_dirty = false;
   dfree(e->q_ids); dfree(e->q_vals); dfree(e->q_end); dfree(e->q_delta); dfree(e->snap);
   dfree(e->qpart); dfree(e->cbits);
-  dfree(e->ne_vid); dfree(e->ne_end); dfree(e->zero_vid);
+  dfree(e->ne_vid); dfree(e->ne_end);
   dfree(e->slab_dpart); dfree(e->slab_qpart); dfree(e->slab_a0);
   dfree(e->slab_first); dfree(e->slab_carry); dfree(e->slab_fix); dfree(e->slab_fix_n);
   dfree(e->trace); dfree(e->hist);
-  e->n_ne = e->n_zero = e->slab_cap = 0;
+  e->n_ne = e->slab_cap = 0;
   for (int i = 0; i < kGraphSlots; ++i) {
     if (e->graphs[i]) cudaGraphExecDestroy(e->graphs[i]);
     e->graphs[i] = nullptr;
@@ -873,8 +873,8 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
     e->host_ed = const_cast<void *>(edge_data);
   }
 
-  // rows of the CSC with / without in-edges, for the dense slab passes
-  std::vector<int32_t> ne_vid, ne_end, zero_vid;
+  // rows of the CSC with in-edges, for the dense slab passes
+  std::vector<int32_t> ne_vid, ne_end;
   try {
     ne_vid.reserve(V);
     ne_end.reserve(V);
@@ -882,18 +882,14 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
       if (e->h_csc_off[v + 1] > e->h_csc_off[v]) {
         ne_vid.push_back(v);
         ne_end.push_back(e->h_csc_off[v + 1]);
-      } else {
-        zero_vid.push_back(v);
       }
     }
   } catch (...) {
     return gas::fail(GAS_ERR_NOMEM, "set_graph: row lists");
   }
   e->n_ne = (int32_t)ne_vid.size();
-  e->n_zero = (int32_t)zero_vid.size();
   GAS_TRY(dalloc(&e->ne_vid, ne_vid.size()));
   GAS_TRY(dalloc(&e->ne_end, ne_end.size()));
-  GAS_TRY(dalloc(&e->zero_vid, zero_vid.size()));
   e->slab_cap = (int32_t)((E + gasdev::kSlabChunk - 1) / gasdev::kSlabChunk + 1);
   GAS_TRY(dalloc(&e->slab_dpart, (size_t)e->slab_cap));
   // the push may cut its queue's edges into chunks as small as 64 edges
@@ -912,9 +908,6 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
     CUDA_TRY(cudaMemcpyAsync(e->ne_vid, ne_vid.data(), ne_vid.size() * 4, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(e->ne_end, ne_end.data(), ne_end.size() * 4, cudaMemcpyHostToDevice, st));
   }
-  if (!zero_vid.empty())
-    CUDA_TRY(cudaMemcpyAsync(e->zero_vid, zero_vid.data(), zero_vid.size() * 4,
-                             cudaMemcpyHostToDevice, st));
   if (!dev_build) {
     CUDA_TRY(cudaMemcpyAsync(e->csc_off, e->h_csc_off.data(), (V + 1) * 4,
                              cudaMemcpyHostToDevice, st));

@@ -90,9 +90,9 @@ struct gas_engine {
   uint32_t *cbits = nullptr;
   int32_t pull_div = 4;
 
-  // non-empty in-edge rows of the CSC (dense slab passes) and the rest
-  int32_t *ne_vid = nullptr, *ne_end = nullptr, *zero_vid = nullptr;
-  int32_t n_ne = 0, n_zero = 0;
+  // non-empty in-edge rows of the CSC (dense slab passes)
+  int32_t *ne_vid = nullptr, *ne_end = nullptr;
+  int32_t n_ne = 0;
   // warp-slab chunk state: partitions of the dense CSC and of the push
   // queue, per-chunk carries (8-byte values) and fixup rows
   int32_t *slab_dpart = nullptr, *slab_qpart = nullptr, *slab_a0 = nullptr;
