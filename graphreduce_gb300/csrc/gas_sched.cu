@@ -21,7 +21,9 @@
 // apply() return true.  Iteration k+1 exists iff C_k has an out-edge.
 //
 // BFS (bfs.cu:58-71): C_k = vertices first reached at level k; push marks
-// unvisited out-neighbours with atomicCAS.
+// unvisited out-neighbours (plain store of the level, reduction of the
+// changed bit); the bottom-up pull lets every unvisited vertex look for an
+// in-neighbour in C_k and stop at the first -- the same level k+1 set.
 //
 // The whole run is one CUDA graph: the iteration-0 kernels, a kernel that
 // sets the loop condition, then a WHILE node whose body runs push or pull
@@ -207,7 +209,8 @@ __global__ void __launch_bounds__(kNT)
   }
 }
 
-constexpr int kSpineNT = 1024;  // k_q_spine (with the loop control, below)
+constexpr int kSpineNT = 1024;
+constexpr int kBfsPullDiv = 16;  // BFS: bottom-up while out-edges(C_k) * 16 > E  // k_q_spine (with the loop control, below)
 constexpr int kSpineRegs = 4;
 
 // (at most 48 registers: 5 CTAs per SM, so a sparse iteration's mostly
@@ -443,6 +446,34 @@ __global__ void __launch_bounds__(kNT)
   gasdev::slab_loop<BfsPushPol, false>(pol, src, nullptr, nullptr, nullptr, nullptr,
                                        nullptr);
   light_loop(pol, src.delta, src.ends, cnt);
+}
+
+// Bottom-up BFS level: a thread per vertex; an unvisited vertex reads its
+// in-edges four at a time (indices, then the sources' depths) and stops at
+// the first source reached at the previous level.  A source claimed in this
+// same pass reads as -1 or as the new level, never as the previous one, so
+// the level set is exactly the push's.
+__global__ void __launch_bounds__(kNT)
+    k_bfs_pull(const int32_t *csc_off, const int32_t *csc_src, int32_t *depth,
+               uint32_t *cbits, int nV, const gas_counters *cnt) {
+  if (cnt->mode != kModePull) return;
+  const int level = cnt->iteration, prev = level - 1;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    if (depth[v] != -1) continue;
+    const int b = __ldg(csc_off + v), end = __ldg(csc_off + v + 1);
+    bool found = false;
+    for (int i = b; i < end && !found; i += 4) {
+      int u[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) u[j] = i + j < end ? ld_stream(csc_src + i + j) : -1;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) found |= u[j] >= 0 && depth[u[j]] == prev;
+    }
+    if (found) {
+      __stcg(depth + v, level);
+      atomicOr(cbits + ((uint32_t)v >> 5), 1u << (v & 31));
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -846,7 +877,11 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   const bool prof_pull = e->profiling && !e->in_graph && e->h_cnt->mode == kModePull;
   const int64_t wbytes = e->prog == GAS_PROG_SSSP ? 4 : 0;
   if (e->profiling && !e->in_graph) {
-    if (prof_pull)  // per edge index (+ weight) + state or bitmap; per row 16 B
+    if (prof_pull && e->prog == GAS_PROG_BFS)  // bottom-up: the dense depth and
+      // offset reads only (the in-edges inspected before each early exit are
+      // not counted, so this is a lower bound)
+      gas::prof_begin(e, cs, gas::kProfPull, 12LL * e->nV);
+    else if (prof_pull)  // per edge index (+ weight) + state or bitmap; per row 16 B
       gas::prof_begin(e, cs, gas::kProfPull, (8 + wbytes) * e->nE + 16LL * e->n_ne);
     else  // per pushed edge dst (+ weight) + state; per queue entry 16 B
       gas::prof_begin(e, cs, gas::kProfPush,
@@ -856,6 +891,8 @@ gas_status_t body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
   if (e->prog == GAS_PROG_BFS) {
     BfsPushPol pol{e->csr_dst, (int32_t *)e->vd, e->cbits, 0};
     k_bfs_push<<<pgrid, kNT, 0, cs>>>(pol, qsrc, e->cnt);
+    k_bfs_pull<<<grid, kNT, 0, cs>>>(e->csc_off, e->csc_src, (int32_t *)e->vd, e->cbits,
+                                     e->nV, e->cnt);
   } else if (e->prog == GAS_PROG_SSSP) {
     PushPol<true> pol{e->csr_dst, (const int32_t *)e->csr_ed, e->q_vals,
                       (int32_t *)e->vd, e->cbits, zero_cap};
@@ -978,8 +1015,10 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
                       void *stream) {
   if (e->prog == GAS_PROG_PAGERANK)  // not monotone: the generic kernels
     return gas_engine_run_schedule(e, GAS_SCHED_GENERIC, max_iterations, stats, stream);
-  // BFS has the top-down push only: every schedule pushes
-  if (e->prog == GAS_PROG_BFS) schedule = GAS_SCHED_PUSH;
+  // BFS: push or the bottom-up pull per level; AUTO and LEARNED both take
+  // the direction rule below (the schedule head's features do not tell BFS
+  // from CC, whose pull costs far more)
+  if (e->prog == GAS_PROG_BFS && schedule == GAS_SCHED_LEARNED) schedule = GAS_SCHED_AUTO;
   if (schedule == GAS_SCHED_LEARNED && !e->sched_model)
     return fail(GAS_ERR_STATE, "LEARNED schedule without a schedule model");
   GAS_TRY(ensure_fast_buffers(e));
@@ -1014,7 +1053,9 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
   if (!host_loop && !e->graphs[slot]) GAS_TRY(build_fast_graph(e, &ctx, &e->graphs[slot]));
   const int forced = schedule == GAS_SCHED_PUSH ? 1 : schedule == GAS_SCHED_PULL ? 2
                      : schedule == GAS_SCHED_LEARNED ? 3 : 0;
-  k_fast_reset<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations, forced, e->pull_div);
+  // BFS pulls while the frontier's out-edges exceed 1/16 of the edges
+  const int pull_div = e->prog == GAS_PROG_BFS ? kBfsPullDiv : e->pull_div;
+  k_fast_reset<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations, forced, pull_div);
   cudaError_t ce = cudaGetLastError();
   if (host_loop) {
     if (ce == cudaSuccess) {
@@ -1044,9 +1085,10 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     // prologue (snapshot fill; gather/apply, fixup, commit | bfs apply;
     // seed; partition of the dense pull; 3 compaction, the last two also
     // the loop control and the next push's partition) + per iteration
-    // (push, pull, pull fixup | bfs push; 3 compaction) + reset + finish
+    // (push, pull, pull fixup | bfs push, bfs pull; 3 compaction) + reset
+    // + finish
     const int pro = e->prog == GAS_PROG_BFS ? 6 : (ctx.seeded ? 6 : 10);
-    const int per = e->prog == GAS_PROG_BFS ? 4 : 6;
+    const int per = e->prog == GAS_PROG_BFS ? 5 : 6;
     const int loop_iters = ctx.seeded ? c.iteration : (c.iteration > 0 ? c.iteration - 1 : 0);
     stats->kernel_launches = pro + per * loop_iters + 2;
   }

@@ -120,6 +120,32 @@ def test_fast_schedules_at_scale_against_oracle():
         eng.close()
 
 
+def test_bfs_bottom_up_levels_at_scale():
+    """BFS from a source in the R-MAT part of a 1M-vertex graph (scale 19 +
+    512 grid islands the source cannot reach): top-down only, bottom-up
+    only, and the direction rule (AUTO, and LEARNED, which takes the same
+    rule for BFS) give the oracle's depths and level count; the rule
+    switches to bottom-up for the heavy levels and back."""
+    el = EdgeList.rmat(19, 16, seed=7).with_grid_islands(512, 32)
+    s = int(EdgeList.rmat(19, 16, seed=7).sample_sources(1, 9)[0])
+    ref, rit = oracle.bfs(el.nV, el.src, el.dst, s)
+    from graphreduce_gb300.learn import DATA, MLP
+    eng = GASEngineGPU("bfs")
+    eng.setGraph(el.nV, initial_vertex_data("bfs", el.nV), el.nE, None, el.src, el.dst)
+    eng.set_schedule_model(MLP.load(DATA / "schedule_head.npz"))
+    for schedule in ("push", "pull", "auto", "learned"):
+        eng.upload_vertex_data(initial_vertex_data("bfs", el.nV))
+        eng.setActive(s, s + 1)
+        st = eng.run_schedule(schedule, max_iterations=el.nV + 2)
+        out = np.empty(el.nV, np.int32)
+        eng.download_vertex_data(out)
+        np.testing.assert_array_equal(out, ref, err_msg=schedule)
+        assert st.iterations == rit, schedule
+        if schedule in ("auto", "learned"):
+            assert st.pull_iters > 0 and st.push_iters > 0, (st.push_iters, st.pull_iters)
+    eng.close()
+
+
 @pytest.mark.parametrize("scale,seed", [(12, 4), (14, 4)])
 def test_pagerank_precision_against_fp64_oracle(scale, seed):
     el = EdgeList.rmat(scale, 16, seed=seed, symmetrize=False)
