@@ -172,12 +172,13 @@ __device__ __forceinline__ int4 q_warp_totals(const QWarp &w) {
 // features).  The snapshots are written only for a queue that a dense pull
 // reads: after a pull iteration (mode still says so here) the previous
 // queue's snapshots (its length is still in the counters) go back to
-// Program::gatherZero first.
+// Program::gatherZero first.  BFS's bottom-up pass reads depths, never
+// snapshots (bfs != 0: none are written or reset).
 __global__ void __launch_bounds__(kNT)
     k_q_count(const uint32_t *cbits, const int32_t *csr_off, int nW,
               int4 *part, const int32_t *q_ids, int32_t *snap, int32_t zero,
-              int32_t *hist, const gas_counters *cnt) {
-  if (cnt->mode == kModePull) {
+              int32_t *hist, const gas_counters *cnt, int bfs) {
+  if (!bfs && cnt->mode == kModePull) {
     const int n_old = cnt->n_changed;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old;
          i += gridDim.x * blockDim.x)
@@ -209,8 +210,8 @@ __global__ void __launch_bounds__(kNT)
   }
 }
 
-constexpr int kSpineNT = 1024;
-constexpr int kBfsPullDiv = 16;  // BFS: bottom-up while out-edges(C_k) * 16 > E  // k_q_spine (with the loop control, below)
+constexpr int kSpineNT = 1024;  // k_q_spine (with the loop control, below)
+constexpr int kBfsPullDiv = 16;  // BFS: bottom-up while out-edges(C_k) * 16 > E
 constexpr int kSpineRegs = 4;
 
 // (at most 48 registers: 5 CTAs per SM, so a sparse iteration's mostly
@@ -219,10 +220,15 @@ __global__ void __launch_bounds__(kNT, 5)
     k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int4 *part,
               const int32_t *vd, int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
               int32_t *q_delta, int32_t *snap, int32_t *chunk_row,
-              const gas_counters *cnt) {
+              const gas_counters *cnt, int bfs) {
   __shared__ int4 s_t[kNT / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
+  if (bfs && cnt->mode == kModePull) {  // grid-uniform: the next BFS level is
+    // bottom-up and reads depths, so only the changed bitmap is cleared
+    if (lane < kQWordsPerWarp && w0 + lane < nW && cbits[w0 + lane]) cbits[w0 + lane] = 0u;
+    return;
+  }
   QWarp w;
   q_warp_load(cbits, csr_off, nW, w0, w);
   int val[kQWordsPerWarp];
@@ -236,7 +242,7 @@ __global__ void __launch_bounds__(kNT, 5)
   for (int k = 0; k < warp; ++k) base = add4(base, s_t[k]);
   int bq = base.x, bd = base.y, lq = cnt->q_heavy + base.z;
   const int cl = cnt->push_chunk_log2;
-  const bool want_snap = cnt->mode == kModePull;  // the next iteration's mode
+  const bool want_snap = !bfs && cnt->mode == kModePull;  // the next iteration's mode
   if (w.myword) cbits[w0 + lane] = 0u;
   const unsigned below = (1u << lane) - 1u;
 #pragma unroll
@@ -811,14 +817,15 @@ gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c,
                         cudaGraphConditionalHandle h, int phase) {
   int4 *part = reinterpret_cast<int4 *>(e->qpart);
   int32_t *hist = (e->trace_on || e->sched_model) ? e->hist : nullptr;
+  const int bfs = e->prog == GAS_PROG_BFS ? 1 : 0;
   k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, part, e->q_ids,
-                                         e->snap, snap_zero(e), hist, e->cnt);
+                                         e->snap, snap_zero(e), hist, e->cnt, bfs);
   k_q_spine<<<1, kSpineNT, 0, cs>>>(part, c.n_qblocks, e->cnt, c.push_grid * (kNT / 32),
                                     loop_ctl(e, h), phase, c.seeded ? 1 : 0);
   k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, part,
                                          (const int32_t *)e->vd, e->q_ids, e->q_vals,
                                          e->q_end, e->q_delta, e->snap, e->slab_qpart,
-                                         e->cnt);
+                                         e->cnt, bfs);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
 }
