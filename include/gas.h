@@ -223,7 +223,10 @@ gas_status_t gas_engine_upload_vertex_data(gas_engine *e, const void *host,
 gas_status_t gas_engine_download_vertex_data(gas_engine *e, void *host,
                                              void *stream);
 
-/* Schedule of the built-in fast runs. */
+/* Schedule of the built-in fast runs.  For BFS the pull is the bottom-up
+ * level (each unvisited vertex stops at its first in-neighbour of the
+ * previous level), and AUTO and LEARNED both take the direction rule
+ * "bottom-up while the frontier's out-edges exceed E/16". */
 typedef enum {
   GAS_SCHED_AUTO = 0,      /* fixed heuristic per iteration                */
   GAS_SCHED_GENERIC = 1,   /* the step-API kernels (pull over active set)  */
