@@ -594,10 +594,24 @@ def run_lanes24(args):
     depth_d = torch.empty((el.nV, L), dtype=torch.int32, device=dev)
     run_b = lambda: b.run(bfs_sources=srcs[None, :], depth_out=depth_d.data_ptr(), stream=sp)
     if args.launch_list:
-        # one batched BFS run and nothing else (for an ncu launch list / capture)
+        # one batched BFS run, then the first two sources one by one on the
+        # single-graph engine (learned: the direction rule), and nothing else
+        # (for an ncu launch list / capture)
         r = run_b()
+        e = gg.GASEngineGPU("bfs")
+        e.setGraph(el.nV, initial_vertex_data("bfs", el.nV), el.nE, None, el.src, el.dst, sp)
+        e.set_schedule_model(model)
+        init = torch.from_numpy(initial_vertex_data("bfs", el.nV)).to(dev)
+        levels = []
+        for src in srcs[:2]:
+            e.upload_vertex_data_ptr(init.data_ptr(), sp)
+            e.setActive(int(src), int(src) + 1, sp)
+            st = e.run_schedule("learned", max_iterations=el.nV + 2, stream=sp)
+            levels.append([st.iterations, st.push_iters, st.pull_iters])
         torch.cuda.synchronize()
-        return {"launch_list": True, "bfs_levels": r.stats.bfs_iterations}
+        e.close()
+        return {"launch_list": True, "bfs_levels": r.stats.bfs_iterations,
+                "single_source": levels}
     run_b()
     depth = depth_d.cpu().numpy()
     od = el.out_degree().astype(np.int64)
