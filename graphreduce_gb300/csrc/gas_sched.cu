@@ -455,8 +455,8 @@ __global__ void __launch_bounds__(kNT)
 }
 
 // Bottom-up BFS level: a thread per vertex; an unvisited vertex reads its
-// in-edges four at a time (indices, then the sources' depths) and stops at
-// the first source reached at the previous level.  A source claimed in this
+// first in-edge, then the rest four at a time (indices, then the sources'
+// depths), and stops at the first source reached at the previous level.  A source claimed in this
 // same pass reads as -1 or as the new level, never as the previous one, so
 // the level set is exactly the push's.
 __global__ void __launch_bounds__(kNT)
@@ -467,8 +467,10 @@ __global__ void __launch_bounds__(kNT)
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
     if (depth[v] != -1) continue;
     const int b = __ldg(csc_off + v), end = __ldg(csc_off + v + 1);
-    bool found = false;
-    for (int i = b; i < end && !found; i += 4) {
+    // the first in-edge alone first: sources are in id order and low ids
+    // are the hubs, so the first is the likeliest parent
+    bool found = b < end && depth[ld_stream(csc_src + b)] == prev;
+    for (int i = b + 1; i < end && !found; i += 4) {
       int u[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) u[j] = i + j < end ? ld_stream(csc_src + i + j) : -1;
