@@ -1,10 +1,12 @@
 """THE ORACLE -- test infrastructure only.
 
 ctypes access to oracle/_build/liboracle.so (gas_oracle.c, the C restatement
-of the reference's CPU engine refgas.h and its four programs) and, when it was
-built from the reference sources, oracle/_ref/libref.so (the reference's own
-refgas.h / graphio.cpp).  Only tests/, __graft_entry__.smoke() and bench.py's
-CPU-baseline leg import this package; the engine never does.
+of the reference's CPU engine refgas.h and its four programs, and
+gas_oracle_gen.c, the seeded input generators the CPU baseline builds its
+workload with) and, when it was built from the reference sources,
+oracle/_ref/libref.so (the reference's own refgas.h / graphio.cpp).  Only
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+package; the engine never does.  Loading it never loads the product library.
 """
 from __future__ import annotations
 
@@ -48,8 +50,83 @@ def _oracle():
             for f in ("orc_bfs", "orc_sssp", "orc_cc", "orc_pagerank", "orc_pagerank_fp64",
                       "orc_ppr_fp64"):
                 getattr(lib, f).restype = c_i64
+            lib.orc_set_threads.argtypes = [c_i32]
+            lib.orc_set_threads.restype = None
+            lib.orc_get_threads.restype = c_i32
+            lib.orc_free.argtypes = [c_vp]
+            lib.orc_free.restype = None
+            lib.orc_rmat.argtypes = [c_i32, c_i32, c_dbl, c_dbl, c_dbl, C.c_uint64, c_i32,
+                                     C.POINTER(C.POINTER(c_i32)), C.POINTER(C.POINTER(c_i32))]
+            lib.orc_rmat.restype = c_i64
+            lib.orc_grid_islands.argtypes = [c_i32, c_i32, c_i32, c_vp, c_vp]
+            lib.orc_grid_islands.restype = c_i64
+            lib.orc_uniform_weights.argtypes = [c_i64, c_vp, c_vp, c_i32, c_i32, C.c_uint64,
+                                                c_vp]
+            lib.orc_uniform_weights.restype = C.c_int
+            lib.orc_sample_sources.argtypes = [c_i32, c_i64, c_vp, c_vp, c_i32, C.c_uint64,
+                                               c_vp]
+            lib.orc_sample_sources.restype = C.c_int
             _orc = lib
     return _orc
+
+
+def set_threads(n: int) -> None:
+    """OpenMP threads of the oracle's loops (results do not depend on it)."""
+    _oracle().orc_set_threads(int(n))
+
+
+def threads() -> int:
+    return int(_oracle().orc_get_threads())
+
+
+# ---------------------------------------------------------------------------
+# Seeded inputs (gas_oracle_gen.c): the workload graphs without the product
+# library.
+# ---------------------------------------------------------------------------
+
+def rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, symmetrize=True):
+    """R-MAT edge list sorted by (src, dst) -> (nV, src int32, dst int32)."""
+    ps, pd = C.POINTER(c_i32)(), C.POINTER(c_i32)()
+    lib = _oracle()
+    n = lib.orc_rmat(scale, edge_factor, a, b, c, seed, int(bool(symmetrize)), C.byref(ps),
+                     C.byref(pd))
+    if n < 0:
+        raise RuntimeError(f"oracle rmat failed with code {n}")
+    try:
+        src = np.ctypeslib.as_array(ps, shape=(max(1, n),))[:n].copy()
+        dst = np.ctypeslib.as_array(pd, shape=(max(1, n),))[:n].copy()
+    finally:
+        lib.orc_free(C.cast(ps, c_vp))
+        lib.orc_free(C.cast(pd, c_vp))
+    return 1 << scale, src, dst
+
+
+def with_grid_islands(nV, src, dst, n_islands, side):
+    """Appends the grid islands after vertex nV -> (nV', src', dst')."""
+    m = n_islands * 4 * side * (side - 1)
+    s2, d2 = np.empty(m, np.int32), np.empty(m, np.int32)
+    n = _oracle().orc_grid_islands(nV, n_islands, side, s2.ctypes.data, d2.ctypes.data)
+    if n != m:
+        raise RuntimeError("oracle grid islands: bad arguments")
+    return nV + n_islands * side * side, np.concatenate([src, s2]), np.concatenate([dst, d2])
+
+
+def uniform_weights(src, dst, lo, hi, seed):
+    s, d = _i32(src), _i32(dst)
+    w = np.empty(s.shape[0], np.int32)
+    if _oracle().orc_uniform_weights(s.shape[0], s.ctypes.data, d.ctypes.data, lo, hi, seed,
+                                     w.ctypes.data):
+        raise ValueError("uniform_weights: bad range")
+    return w
+
+
+def sample_sources(nV, src, dst, k, seed):
+    s, d = _i32(src), _i32(dst)
+    out = np.zeros(k, np.int32)
+    if _oracle().orc_sample_sources(nV, s.shape[0], s.ctypes.data, d.ctypes.data, k, seed,
+                                    out.ctypes.data):
+        raise ValueError("sample_sources: bad arguments or component too small")
+    return out
 
 
 def _i32(a) -> np.ndarray:

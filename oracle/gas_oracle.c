@@ -24,6 +24,18 @@
  * their edge-list order.  Integer programs (min / level) do not depend on that
  * order; PageRank sums can differ in the last ulp, which the tests allow for.
  *
+ * Threads: the engine's per-vertex loops and the FP64 PageRank loops run on
+ * OpenMP threads (orc_set_threads); results do not depend on the thread
+ * count (per-vertex folds stay sequential in CSC order, residuals are summed
+ * per fixed chunk of ORC_CHUNK vertices and then in chunk order).
+ *
+ * Synthetic inputs: orc_rmat, orc_append_grid_islands, orc_set_uniform_weights
+ * and orc_sample_sources restate the seeded generators of the product library
+ * (graphreduce_gb300/csrc/gas_host_graph.cpp; they have no reference
+ * counterpart) so that the CPU baseline can build its workload without
+ * loading the product library; tests/test_oracle.py checks that they give
+ * the same edge lists, weights and sources.
+ *
  * Build: oracle/Makefile (gcc -O2 -ffp-contract=off, so x86 and Arm agree).
  */
 #include <stdint.h>
@@ -32,14 +44,31 @@
 #include <math.h>
 #include <limits.h>
 
+#include <omp.h>
+
 #define ORC_EXPORT __attribute__((visibility("default")))
+/* Vertices per chunk of the parallel loops whose partial results are joined
+ * in a fixed order (next active list, residual sums). */
+#define ORC_CHUNK 65536
+
+ORC_EXPORT void orc_set_threads(int32_t n) { if (n > 0) omp_set_num_threads(n); }
+ORC_EXPORT int32_t orc_get_threads(void) { return (int32_t)omp_get_max_threads(); }
 
 /* ------------------------------------------------------------------------ */
 /* CSR / CSC construction: util.cuh:80-121 (edgeListToCSR / edgeListToCSC).  */
 /* ------------------------------------------------------------------------ */
 
+static int cmp_eid(const void *a, const void *b)
+{
+  const int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
+  return (x > y) - (x < y);
+}
+
 /* offsets[nV+1]; out[nE] = vals[perm[i]]; perm[nE] = original edge index.
- * Keys outside [0,nV) are a caller error and return -1. */
+ * Keys outside [0,nV) are a caller error and return -1.  The result is that
+ * of a stable counting sort by key (edges of one key keep their edge-list
+ * order); it is computed in parallel by placing edge ids with atomic
+ * cursors and then sorting each row's ids. */
 ORC_EXPORT int orc_edge_list_to_csr(int32_t nV, int64_t nE,
                                     const int32_t *keys, const int32_t *vals,
                                     int64_t *offsets, int32_t *out,
@@ -48,21 +77,47 @@ ORC_EXPORT int orc_edge_list_to_csr(int32_t nV, int64_t nE,
   int64_t i;
   int32_t v;
   int64_t *cursor;
+  int32_t *ids = perm;
+  int bad = 0;
   for (v = 0; v <= nV; ++v) offsets[v] = 0;
+#pragma omp parallel for schedule(static) reduction(|:bad)
   for (i = 0; i < nE; ++i) {
-    if (keys[i] < 0 || keys[i] >= nV) return -1;
-    offsets[keys[i] + 1]++;
+    if (keys[i] < 0 || keys[i] >= nV) { bad = 1; continue; }
+    __atomic_fetch_add(&offsets[keys[i] + 1], 1, __ATOMIC_RELAXED);
   }
+  if (bad) return -1;
   for (v = 0; v < nV; ++v) offsets[v + 1] += offsets[v];
   cursor = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nV > 0 ? nV : 1));
-  if (!cursor) return -2;
-  for (v = 0; v < nV; ++v) cursor[v] = offsets[v];
-  for (i = 0; i < nE; ++i) {
-    int64_t pos = cursor[keys[i]]++;
-    if (out) out[pos] = vals[i];
-    if (perm) perm[pos] = (int32_t)i;
+  if (!ids) ids = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nE > 0 ? nE : 1));
+  if (!cursor || !ids) {
+    free(cursor);
+    if (ids != perm) free(ids);
+    return -2;
+  }
+  memcpy(cursor, offsets, sizeof(int64_t) * (size_t)nV);
+#pragma omp parallel for schedule(static)
+  for (i = 0; i < nE; ++i)
+    ids[__atomic_fetch_add(&cursor[keys[i]], 1, __ATOMIC_RELAXED)] = (int32_t)i;
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (v = 0; v < nV; ++v) {
+    int32_t *row = ids + offsets[v];
+    int64_t n = offsets[v + 1] - offsets[v], a, b;
+    if (n > 32) {
+      qsort(row, (size_t)n, sizeof(int32_t), cmp_eid);
+    } else {
+      for (a = 1; a < n; ++a) {
+        int32_t x = row[a];
+        for (b = a; b > 0 && row[b - 1] > x; --b) row[b] = row[b - 1];
+        row[b] = x;
+      }
+    }
+  }
+  if (out) {
+#pragma omp parallel for schedule(static)
+    for (i = 0; i < nE; ++i) out[i] = vals[ids[i]];
   }
   free(cursor);
+  if (ids != perm) free(ids);
   return 0;
 }
 
@@ -293,6 +348,47 @@ ORC_EXPORT int64_t orc_pagerank(int32_t nV, int64_t nE, const int32_t *srcs,
   return it;
 }
 
+/* One FP64 power-iteration step shared by the PageRank oracles:
+ * contrib[u] = r[u] / outdeg(u) (0 without out-edges), then
+ * rn[v] = teleport(v) + d * sum_{u->v} contrib[u] folded in CSC order, with
+ * teleport(v) = (1-d)/N for global PageRank (seed < 0) and (1-d)[v == seed]
+ * for personalized PageRank.  Returns sum_v |rn[v] - r[v]|, summed per chunk
+ * of ORC_CHUNK vertices and then over chunks in order (independent of the
+ * thread count), or -1 if the chunk table cannot be allocated. */
+static double fp64_step(const orc_graph *g, double damping, int32_t seed,
+                        const double *r, double *rn, double *contrib)
+{
+  const int64_t nV = g->nV;
+  const int64_t nchunk = (nV + ORC_CHUNK - 1) / ORC_CHUNK;
+  double *part = (double *)malloc(sizeof(double) * (size_t)(nchunk > 0 ? nchunk : 1));
+  double l1 = 0.0;
+  int64_t c;
+  if (!part) return -1.0;
+#pragma omp parallel for schedule(static)
+  for (c = 0; c < nV; ++c) {
+    int64_t od = g->csr_off[c + 1] - g->csr_off[c];
+    contrib[c] = od ? r[c] / (double)od : 0.0;
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (c = 0; c < nchunk; ++c) {
+    int64_t v, hi = (c + 1) * ORC_CHUNK < nV ? (c + 1) * ORC_CHUNK : nV;
+    double acc = 0.0;
+    for (v = c * ORC_CHUNK; v < hi; ++v) {
+      double s = 0.0;
+      int64_t ie;
+      for (ie = g->csc_off[v]; ie < g->csc_off[v + 1]; ++ie)
+        s += contrib[g->csc_src[ie]];
+      rn[v] = (seed < 0 ? (1.0 - damping) / (double)nV
+                        : (v == seed ? 1.0 - damping : 0.0)) + damping * s;
+      acc += fabs(rn[v] - r[v]);
+    }
+    part[c] = acc;
+  }
+  for (c = 0; c < nchunk; ++c) l1 += part[c];
+  free(part);
+  return l1;
+}
+
 /* Precision-form PageRank in FP64: r0 = 1/N; every vertex active every
  * iteration; r'_v = (1-d)/N + d * sum_{u->v} r_u / outdeg(u) (no dangling
  * redistribution); stop after the first iteration whose L1 residual
@@ -320,19 +416,8 @@ ORC_EXPORT int64_t orc_pagerank_fp64(int32_t nV, int64_t nE,
   for (v = 0; v < nV; ++v) r[v] = 1.0 / (double)nV;
   for (;;) {
     if (it >= max_iter) { it = -3; break; }
-    for (v = 0; v < nV; ++v) {
-      int64_t od = g.csr_off[v + 1] - g.csr_off[v];
-      contrib[v] = od ? r[v] / (double)od : 0.0;
-    }
-    l1 = 0.0;
-    for (v = 0; v < nV; ++v) {
-      double s = 0.0;
-      int64_t ie;
-      for (ie = g.csc_off[v]; ie < g.csc_off[v + 1]; ++ie)
-        s += contrib[g.csc_src[ie]];
-      rn[v] = (1.0 - damping) / (double)nV + damping * s;
-      l1 += fabs(rn[v] - r[v]);
-    }
+    l1 = fp64_step(&g, damping, -1, r, rn, contrib);
+    if (l1 < 0) { it = -2; break; }
     { double *t = r; r = rn; rn = t; }
     ++it;
     if (l1 <= tol) break;
@@ -370,19 +455,8 @@ ORC_EXPORT int64_t orc_ppr_fp64(int32_t nV, int64_t nE, const int32_t *srcs,
   for (v = 0; v < nV; ++v) r[v] = v == seed ? 1.0 : 0.0;
   for (;;) {
     if (it >= max_iter) { it = -3; break; }
-    for (v = 0; v < nV; ++v) {
-      int64_t od = g.csr_off[v + 1] - g.csr_off[v];
-      contrib[v] = od ? r[v] / (double)od : 0.0;
-    }
-    l1 = 0.0;
-    for (v = 0; v < nV; ++v) {
-      double s = 0.0;
-      int64_t ie;
-      for (ie = g.csc_off[v]; ie < g.csc_off[v + 1]; ++ie)
-        s += contrib[g.csc_src[ie]];
-      rn[v] = (v == seed ? 1.0 - damping : 0.0) + damping * s;
-      l1 += fabs(rn[v] - r[v]);
-    }
+    l1 = fp64_step(&g, damping, seed, r, rn, contrib);
+    if (l1 < 0) { it = -2; break; }
     { double *t = r; r = rn; rn = t; }
     ++it;
     if (l1 <= tol) break;

@@ -130,3 +130,47 @@ def test_oracle_against_live_reference(scale, seed):
     b, ib = oracle.ref_bfs(el.nV, el.src, el.dst, s)
     assert ia == ib
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("scale,ef,sym,seed", [(9, 16, True, 2), (11, 8, False, 4),
+                                               (12, 16, True, 1)])
+def test_oracle_generators_match_library(scale, ef, sym, seed):
+    """The oracle's own input generators (what the CPU baseline builds its
+    workload with, never loading the product library) give the product
+    library's graphs, islands, weights and sources exactly."""
+    from graphreduce_gb300.graph import EdgeList
+    el = EdgeList.rmat(scale, ef, seed=seed, symmetrize=sym)
+    nV, s, d = oracle.rmat(scale, ef, seed=seed, symmetrize=sym)
+    assert nV == el.nV
+    np.testing.assert_array_equal(s, el.src)
+    np.testing.assert_array_equal(d, el.dst)
+    isl = el.with_grid_islands(12, 5)
+    nV2, s2, d2 = oracle.with_grid_islands(nV, s, d, 12, 5)
+    assert nV2 == isl.nV
+    np.testing.assert_array_equal(s2, isl.src)
+    np.testing.assert_array_equal(d2, isl.dst)
+    np.testing.assert_array_equal(oracle.uniform_weights(s, d, 1, 64, 3),
+                                  el.with_uniform_weights(1, 64, 3).weights)
+    np.testing.assert_array_equal(oracle.sample_sources(nV, s, d, 8, seed),
+                                  el.sample_sources(8, seed))
+
+
+def test_oracle_results_do_not_depend_on_thread_count():
+    nV, s, d = oracle.rmat(12, 16, seed=5, symmetrize=True)
+    w = oracle.uniform_weights(s, d, 1, 64, 3)
+    src = int(oracle.sample_sources(nV, s, d, 1, 5)[0])
+    nd, sd, dd = oracle.rmat(12, 16, seed=6, symmetrize=False)
+    runs = []
+    before = oracle.threads()
+    try:
+        for th in (1, 3, 8):
+            oracle.set_threads(th)
+            runs.append((oracle.sssp(nV, s, d, w, src), oracle.cc(nV, s, d),
+                         oracle.bfs(nV, s, d, src), oracle.pagerank(nd, sd, dd),
+                         oracle.pagerank_fp64(nd, sd, dd), oracle.edge_list_to_csr(nV, d, s)))
+    finally:
+        oracle.set_threads(before)
+    for other in runs[1:]:
+        for a, b in zip(runs[0], other):
+            for x, y in zip(a, b):
+                np.testing.assert_array_equal(x, y)
