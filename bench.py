@@ -1,23 +1,22 @@
-"""Benchmark of the GAS hot path on the scale-22 workload.
+"""Benchmark of the GAS hot path: every configuration of the workload table.
 
-Workload (one "step"): SSSP from 8 sources and CC on an R-MAT graph of scale
-22 (4,194,304 vertices, edge factor 16, (a,b,c,d) = (0.57,0.19,0.19,0.05),
-seed 2, symmetrised, self loops and duplicates removed); SSSP weights
-uniform in [1,64] (seed 3, both directions equal); sources drawn uniformly
-from the largest component (seed 2); CC on the same graph plus 4,096
-disjoint 32x32 4-neighbour grid islands.  Synthetic data: the reference's
-real-world datasets are not available.
+Headline ("value", one "step"): SSSP from 8 sources and CC on an R-MAT graph
+of scale 22 (4,194,304 vertices, edge factor 16, (a,b,c,d) =
+(0.57,0.19,0.19,0.05), seed 2, symmetrised, self loops and duplicates
+removed); SSSP weights uniform in [1,64] (seed 3, both directions equal);
+sources drawn uniformly from the largest component (seed 2); CC on the same
+graph plus 4,096 disjoint 32x32 4-neighbour grid islands.  Synthetic data:
+the reference's real-world datasets are not available.
 
 Metric: GTEPS with the reference's definition (sssp.cu:202-211): for every
 run, the sum of out-degrees of the vertices it reached, divided by time
 (for CC every vertex is reached, so a run counts all its edges).
 
 The engine under test is the learned-schedule, batched one: the 8 SSSP
-sources run as the 8 lanes of one multi-source SSSP launch (per lane
-bit-exact with, and as many iterations as, one run per source; checked
-every time the bench starts), CC runs through the engine with the learned
-schedule.  The same step with one SSSP run per source ("comparisons") and
-the plain fixed-heuristic form ("plain") are timed beside it.
+sources run as the 8 lanes of one multi-source SSSP launch, CC runs through
+the engine with the learned schedule.  The plain fixed-heuristic form (one
+SSSP run per source and CC, schedule AUTO) is timed beside it, device
+resident and end to end.
 
   value  -- device-resident: graph and initial vertex states already in HBM,
             timed with CUDA events on the engine's stream.
@@ -27,7 +26,26 @@ the plain fixed-heuristic form ("plain") are timed beside it.
             comes down (the [V][8] distances, the CC labels) inside the
             timed region.
 
+At one GPU the same line also carries "configs", one entry per workload
+configuration, each with its GTEPS, the dominant kernel's roofline on
+algorithmic bytes (and on DRAM bytes where an ncu capture of that kernel is
+recorded), and a parity flag from the oracle:
+  c1_bfs        BFS, R-MAT scale 16, seed 1, source = first vertex of
+                maximum out-degree (bfs.cu:175-195); depths and levels
+                bit-exact against the oracle
+  c2_sssp_cc    the headline step: all 8 SSSP lanes and the CC labels
+                bit-exact against the oracle (iterations included)
+  c3_pagerank   precision PageRank, R-MAT scale 24 directed, seed 4; L1 and
+                max-abs error against the FP64 oracle
+  c4_learned    the schedule head and the PageRank warm start on held-out
+                graphs (R-MAT scale 24 seed 5; Erdos-Renyi, 2^24 vertices,
+                average degree 16, seed 5) against every fixed schedule
+  c5_batched    64 R-MAT graphs x (16 BFS + 16 PPR) in one graph launch
+                against the same instances one by one; a per-lane parity
+                sample against the oracle
+
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                [--configs c1,c2,c3,c4,c5 | --no-configs]
 """
 from __future__ import annotations
 
@@ -38,7 +56,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 from pathlib import Path
 
@@ -53,16 +70,28 @@ RMAT_ABC = (0.57, 0.19, 0.19)
 GRAPH_SEED, WEIGHT_SEED, SOURCE_SEED = 2, 3, 2
 N_SOURCES = 8
 N_ISLANDS, ISLAND_SIDE = 4096, 32
+SSSP_UNREACHED = 2**31 - 1 - 100000  # sssp.cu:32-33 gatherZero
 METRIC = "GTEPS (SSSP x8 + CC, R-MAT scale {scale})"
 MAX_ITERS = 20000  # far above any run of this workload; bounds a device loop
-# Per-launch DRAM bytes (read + write) of the dominant kernel, by (kernel,
-# scale, edge placement, schedule): one-pass ncu metrics over every launch of
-# that kernel in one step, captured with
-#   GAS_HOST_LOOP=1 ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,\
-#     dram__bytes_write.sum --clock-control none --csv --log-file launches.csv \
-#     python bench.py --launch-list --no-cpu-baseline
-# (k_mss_push: 11 launches, 8.95 GB in all).
-PUSH_TRAFFIC = {("mss_push", 22, "device", "learned"): 814.0e6}
+ALL_CONFIGS = ("c1", "c2", "c3", "c4", "c5")
+
+# DRAM bytes (read + write) per launch of a dominant kernel, from ncu
+# captures recorded under profiles/ (each names its command).  Keys:
+# (kernel, workload).  Where only a smaller case was captured, the bytes are
+# scaled to the bench's launch by the edges processed (the profile says so).
+DRAM_PER_LAUNCH = {
+    # one-pass counters over the 11 batched-SSSP push launches of a scale-22
+    # step (profiles/launches_sssp8-cc_rmat-s22_batched.md)
+    ("mss_push", "rmat-s22"): 814.0e6,
+    # CC push, mean over the 63 launches of the same step (same profile)
+    ("push", "rmat-s22-cc"): 103.2e6,
+    # k_pr_merge + k_pr_merge_fix, one iteration at scale 24
+    # (profiles/k_pr_merge_pagerank_rmat-s24.md)
+    ("pr_gather", "rmat-s24"): 1.647e9,
+    # k_ppr_pieces + k_ppr_fix, one PPR iteration of the 64-graph batch
+    # (profiles/k_ppr_pieces_batched-8graphs.md)
+    ("ppr_iteration", "batched-64"): 10.30e9,
+}
 
 
 def log(*a):
@@ -70,7 +99,7 @@ def log(*a):
 
 
 # ---------------------------------------------------------------------------
-# workload
+# shared helpers
 # ---------------------------------------------------------------------------
 def make_workload(scale):
     from graphreduce_gb300.graph import EdgeList
@@ -103,8 +132,12 @@ def whole_job_value(units_per_rank, world, ms_per_step):
     return world * units_per_rank / (ms_per_step * 1e-3) / 1e9
 
 
-def edges_visited(el_outdeg, vd, unreached):
-    return int(el_outdeg[vd != unreached].sum(dtype=np.int64))
+def edges_visited(outdeg, vd, unreached):
+    return int(outdeg[vd != unreached].sum(dtype=np.int64))
+
+
+def gteps(units, ms):
+    return round(units / (ms * 1e-3) / 1e9, 4) if ms > 0 else 0.0
 
 
 def config_dict(scale, extra=None):
@@ -118,6 +151,70 @@ def config_dict(scale, extra=None):
     if extra:
         d.update(extra)
     return d
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def roofline(kernel, key, total_bytes, total_ms, launches, workload, extra=None):
+    """The dominant kernel's roofline: algorithmic bytes over its measured
+    time (CUDA events around its launches), and where an ncu capture of the
+    kernel on this workload is recorded, its DRAM bytes over the same time."""
+    peak, kind = measured_peaks()
+    launches = max(1, int(launches))
+    ms_l = total_ms / launches
+    alg_l = total_bytes / launches
+    ach = alg_l / (ms_l * 1e-3) / 1e9 if ms_l > 0 else 0.0
+    dram = DRAM_PER_LAUNCH.get((key, workload))
+    r = {"kernel": kernel, "bound": "hbm", "achieved": round(ach, 1), "unit": "GB/s",
+         "peak": peak, "peak_source": kind, "frac": round(ach / peak, 4),
+         "algorithmic_bytes_per_launch": int(alg_l), "avg_launch_ms": round(ms_l, 4),
+         "launches": launches, "traffic": dram,
+         "dram_achieved": round(dram / (ms_l * 1e-3) / 1e9, 1) if dram and ms_l > 0 else None,
+         "dram_frac": round(dram / (ms_l * 1e-3) / 1e9 / peak, 4) if dram and ms_l > 0 else None}
+    if extra:
+        r.update(extra)
+    return r
+
+
+def cuda_timed(stream, fn, steps, warmup):
+    """Mean ms of fn() over `steps` calls after `warmup`, CUDA events on the
+    stream the work is launched on, synchronised on both sides."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    z = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    z.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(z) / max(1, steps)
+
+
+def free_gpu():
+    import gc
+
+    import torch
+    gc.collect()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+
+def oracle_threads():
+    """Every host thread for the oracle's loops (its results do not depend
+    on the count)."""
+    import oracle
+    n = os.cpu_count() or 1
+    oracle.set_threads(n)
+    return n
 
 
 # ---------------------------------------------------------------------------
@@ -180,22 +277,14 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def measured_peaks():
-    p = ROOT / "MEASURED_PEAKS.json"
-    if p.exists():
-        d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
-
-
 # ---------------------------------------------------------------------------
-# our arm
+# C2, the headline: SSSP x8 + CC at scale 22
 # ---------------------------------------------------------------------------
 def run_ours(args, rank, world):
     import torch
 
     import graphreduce_gb300 as gg
-    from graphreduce_gb300.engine import SSSP_GATHER_ZERO, initial_vertex_data
+    from graphreduce_gb300.engine import initial_vertex_data
 
     torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -312,24 +401,16 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         return {"launch_list": True, "gpu_launches": launches[0]}, None
 
-    # correctness of this exact workload + units per step
+    # outputs of this exact workload (checked against the oracle at the end)
     one_step(e2e=True)
     torch.cuda.synchronize()
-    if batched:
-        for k in range(len(sources)):
-            res_s[k].copy_(dist_pin[:, k])
-    ev_units = 0
-    for k in range(len(sources)):
-        ev_units += edges_visited(out_sssp, res_s[k].numpy(), SSSP_GATHER_ZERO)
-    ev_units += edges_visited(out_cc, res_c.numpy(), -12345)  # every CC vertex is reached
-    first_sssp = res_s[0].numpy().copy()
-    if batched:
-        # the lanes equal one SSSP per source through the engine (bit-exact)
-        one_step(e2e=True, use_batch=False)
-        torch.cuda.synchronize()
-        for k in range(len(sources)):
-            if not np.array_equal(res_s[k].numpy(), dist_pin[:, k].numpy()):
-                raise SystemExit(f"batched SSSP lane {k} differs from the single-source run")
+    lanes = np.array(dist_pin.numpy()) if batched else np.stack(
+        [r.numpy() for r in res_s], axis=1)
+    cc_labels = res_c.numpy().copy()
+    out_iters = {"sssp": list(iters["sssp"]), "cc": iters["cc"]}
+    ev_units = sum(edges_visited(out_sssp, lanes[:, k], SSSP_UNREACHED)
+                   for k in range(len(sources)))
+    ev_units += edges_visited(out_cc, cc_labels, -12345)  # every CC vertex is reached
 
     def timed(e2e, steps, warmup, schedule=args.schedule, use_batch=batched):
         for _ in range(warmup):
@@ -340,37 +421,41 @@ def run_ours(args, rank, world):
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
         start.record(stream)
         for _ in range(steps):
             one_step(e2e, schedule, use_batch)
         end.record(stream)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
         ms = start.elapsed_time(end)
-        ms = max_over_ranks(ms, world, dev)
-        return ms / steps, wall / steps
+        return max_over_ranks(ms, world, dev) / steps
 
     with ClockSampler(torch.cuda.current_device()) as clk:
-        ms_step, _ = timed(False, args.steps, args.warmup)
+        ms_step = timed(False, args.steps, args.warmup)
     clocks = clk.summary()
     launches_per_step = launches[0]
     iters_step = {"sssp": list(iters["sssp"]), "cc": iters["cc"]}
-    ms_e2e, _ = timed(True, max(1, args.steps), 1)
+    ms_e2e = timed(True, max(1, args.steps), 1)
     comparisons = {}
     # the same step with one SSSP run per source (learned schedule), and the
-    # plain form: one run per source under the fixed heuristic (AUTO)
+    # plain form: one run per source under the fixed heuristic (AUTO), both
+    # device resident and end to end
     if batched:
-        ms_seq, _ = timed(False, args.steps, args.warmup, args.schedule, False)
+        ms_seq = timed(False, args.steps, args.warmup, args.schedule, False)
         comparisons["sequential_sources"] = {
             "schedule": args.schedule, "ms_per_step": round(ms_seq, 3),
             "value": round(world * ev_units / (ms_seq * 1e-3) / 1e9, 4),
             "speedup_of_headline": round(ms_seq / ms_step, 4)}
-    ms_plain, _ = timed(False, args.steps, args.warmup, "auto", False)
+    ms_plain = timed(False, args.steps, args.warmup, "auto", False)
+    ms_plain_e2e = timed(True, max(1, args.steps), 1, "auto", False)
     plain = {"schedule": "auto (fixed heuristic), one SSSP run per source",
              "ms_per_step": round(ms_plain, 3),
              "value": round(world * ev_units / (ms_plain * 1e-3) / 1e9, 4),
-             "speedup_of_headline": round(ms_plain / ms_step, 4)}
+             "speedup_of_headline": round(ms_plain / ms_step, 4),
+             "e2e": {"ms_per_step": round(ms_plain_e2e, 3),
+                     "value": round(world * ev_units / (ms_plain_e2e * 1e-3) / 1e9, 4),
+                     "h2d_bytes_per_step": (len(sources) * ssp.nV + ccg.nV) * 4,
+                     "d2h_bytes_per_step": (len(sources) * ssp.nV + ccg.nV) * 4,
+                     "speedup_of_headline_e2e": round(ms_plain_e2e / ms_e2e, 4)}}
 
     value = whole_job_value(ev_units, world, ms_step)
     e2e = whole_job_value(ev_units, world, ms_e2e)
@@ -384,17 +469,8 @@ def run_ours(args, rank, world):
     # per-algorithm split and the dominant kernel's roofline (untimed pass)
     split = per_algo_split(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, out_sssp, sources,
                            lane_src, dist_dev, args.schedule, sp, stream)
-    roof = kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev,
-                           args.schedule, sp)
-    traffic = PUSH_TRAFFIC.get((roof["kernel_key"], args.scale, args.edges, args.schedule))
-    if traffic:
-        roof["traffic"] = traffic
-        roof["traffic_source"] = "ncu dram bytes per launch of this kernel, same workload"
-    del roof["kernel_key"]
-    peak, peak_kind = measured_peaks()
-    roof["peak"] = peak
-    roof["frac"] = roof["achieved"] / peak
-    roof["peak_source"] = peak_kind
+    roof, by_kernel = kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src,
+                                      dist_dev, args.schedule, sp, args.scale, args.edges)
 
     result = {
         "metric": METRIC.format(scale=args.scale), "value": round(value, 4), "unit": "GTEPS",
@@ -415,12 +491,19 @@ def run_ours(args, rank, world):
                            "pinned host buffers, on the compute stream")},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roof,
+        "by_kernel": by_kernel,
         "algos": split,
         "plain": plain,
         "comparisons": comparisons,
         "clocks": clocks,
     }
-    return result, (ssp, sources, out_sssp, first_sssp)
+    for e in (e_s, e_c):
+        e.close()
+    if bat is not None:
+        bat.close()
+    outputs = {"ssp": ssp, "ccg": ccg, "sources": sources, "lanes": lanes,
+               "cc_labels": cc_labels, "iters": out_iters, "ev_units": ev_units}
+    return result, outputs
 
 
 def per_algo_split(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, out_sssp, sources, lane_src,
@@ -436,7 +519,7 @@ def per_algo_split(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, out_sssp, sources, lan
         e_s.setActive(0, ssp.nV, sp)
         e_s.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
         e_s.download_vertex_data(host, sp)
-        ev += edges_visited(out_sssp, host, 2**31 - 1 - 100000)
+        ev += edges_visited(out_sssp, host, SSSP_UNREACHED)
     torch.cuda.synchronize()
     a.record(stream)
     its = []
@@ -448,7 +531,7 @@ def per_algo_split(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, out_sssp, sources, lan
     torch.cuda.synchronize()
     ms = a.elapsed_time(b)
     out["sssp_sequential"] = {"ms_per_source": round(ms / len(sources), 3),
-                              "gteps": round(ev / (ms * 1e-3) / 1e9, 4), "iterations": its}
+                              "gteps": gteps(ev, ms), "iterations": its}
     if bat is not None:
         a.record(stream)
         r = bat.run(sssp_sources=lane_src, max_sssp_iterations=MAX_ITERS,
@@ -456,8 +539,7 @@ def per_algo_split(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, out_sssp, sources, lan
         b.record(stream)
         torch.cuda.synchronize()
         ms = a.elapsed_time(b)
-        out["sssp_batched"] = {"ms_8_sources": round(ms, 3),
-                               "gteps": round(ev / (ms * 1e-3) / 1e9, 4),
+        out["sssp_batched"] = {"ms_8_sources": round(ms, 3), "gteps": gteps(ev, ms),
                                "iterations": r.stats.sssp_iterations,
                                "union_edges_pushed": int(r.stats.sssp_edges)}
     a.record(stream)
@@ -467,29 +549,27 @@ def per_algo_split(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, out_sssp, sources, lan
     b.record(stream)
     torch.cuda.synchronize()
     ms = a.elapsed_time(b)
-    out["cc"] = {"ms": round(ms, 3), "gteps": round(ccg.nE / (ms * 1e-3) / 1e9, 4),
-                 "iterations": it}
+    out["cc"] = {"ms": round(ms, 3), "gteps": gteps(ccg.nE, ms), "iterations": it}
     return out
 
 
-def kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev, schedule, sp):
+def kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev, schedule, sp,
+                    scale, edges):
     """One extra pass of the step's runs with kernel profiling on: the
     engines bracket every push / dense-pull launch (and the batch every
     multi-source SSSP push) with CUDA events on the run's stream and
     accumulate its algorithmic bytes (per edge: index, weight for SSSP, and
     the state, row or membership word it reads; per frontier entry or row:
     its offsets and state).  The dominant kernel is the one with the largest
-    total time."""
+    total time; every kernel's roofline is returned beside it."""
     import torch
     kinds = {}
 
     def add(key, p, name):
-        ms, by, n = (getattr(p, f"{name}_ms"), getattr(p, f"{name}_bytes"),
-                     getattr(p, f"{name}_launches"))
         k = kinds.setdefault(key, {"ms": 0.0, "bytes": 0, "launches": 0})
-        k["ms"] += ms
-        k["bytes"] += by
-        k["launches"] += n
+        k["ms"] += getattr(p, f"{name}_ms")
+        k["bytes"] += getattr(p, f"{name}_bytes")
+        k["launches"] += getattr(p, f"{name}_launches")
 
     if bat is None:  # one SSSP run per source through the engine
         e_s.set_profiling(True)
@@ -501,8 +581,8 @@ def kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev, s
         torch.cuda.synchronize()
         ps = e_s.profile()
         e_s.set_profiling(False)
-        add("push", ps, "push")
-        add("pull", ps, "pull")
+        add("sssp_push", ps, "push")
+        add("sssp_pull", ps, "pull")
     e_c.set_profiling(True)
     e_c.profile(reset=True)
     e_c.upload_vertex_data_ptr(dev_c.data_ptr(), sp)
@@ -521,20 +601,565 @@ def kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev, s
         torch.cuda.synchronize()
         add("mss_push", bat.profile(), "push")
         bat.set_profiling(False)
-    for k in kinds.values():
-        k["achieved_gbs"] = (k["bytes"] / (k["ms"] * 1e-3) / 1e9) if k["ms"] > 0 else 0.0
-    dom = max(kinds, key=lambda k: kinds[k]["ms"])
-    d = kinds[dom]
-    return {"kernel": {"pull": "k_pull (CC dense pull, warp-slab)",
-                       "push": "k_push (frontier push, warp-slab)",
-                       "mss_push": "k_mss_push (8-lane multi-source SSSP push, warp-slab)"}[dom],
-            "kernel_key": dom,
-            "bound": "hbm", "achieved": round(d["achieved_gbs"], 1), "unit": "GB/s",
-            "traffic": None, "launches": d["launches"],
-            "algorithmic_bytes_per_launch": int(d["bytes"] / max(1, d["launches"])),
-            "avg_launch_ms": round(d["ms"] / max(1, d["launches"]), 4),
-            "by_kernel": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv)
-                              for kk, vv in v.items()} for k, v in kinds.items()}}
+    names = {"pull": "k_pull (CC dense pull, warp-slab)",
+             "push": "k_push (CC frontier push, warp-slab)",
+             "sssp_push": "k_push (SSSP frontier push, warp-slab)",
+             "sssp_pull": "k_pull (SSSP dense pull, warp-slab)",
+             "mss_push": "k_mss_push (8-lane multi-source SSSP push, warp-slab)"}
+    wl = {"push": f"rmat-s{scale}-cc", "pull": f"rmat-s{scale}-cc",
+          "sssp_push": f"rmat-s{scale}", "sssp_pull": f"rmat-s{scale}",
+          "mss_push": f"rmat-s{scale}"}
+    placement = "" if edges == "device" else "-host-edges"
+    rows = {k: roofline(names[k], k.replace("sssp_", ""), v["bytes"], v["ms"], v["launches"],
+                        wl[k] + placement, {"total_ms": round(v["ms"], 3)})
+            for k, v in kinds.items() if v["launches"]}
+    dom = max(rows, key=lambda k: kinds[k]["ms"])
+    return rows[dom], rows
+
+
+# ---------------------------------------------------------------------------
+# C2 parity and the CPU baseline: the oracle on the whole step
+# ---------------------------------------------------------------------------
+def c2_oracle_check(out):
+    """The oracle (a C restatement of refgas.h, all host threads) runs the
+    headline step once: SSSP from each of the 8 sources and CC on the islands
+    graph.  Its outputs must equal the GPU's bit for bit (iterations
+    included); its run times (graph builds excluded, as the GPU's are) are
+    the CPU baseline."""
+    import oracle
+    n_threads = oracle_threads()
+    ssp, ccg, sources = out["ssp"], out["ccg"], out["sources"]
+    t = time.perf_counter()
+    g = oracle.Graph(ssp.nV, ssp.src, ssp.dst)
+    build_s = time.perf_counter() - t
+    run_s, units = 0.0, 0
+    outdeg = ssp.out_degree()
+    lane_ok, iter_ok = [], []
+    for k, s in enumerate(sources):
+        t = time.perf_counter()
+        d, it = g.sssp(ssp.weights, int(s))
+        run_s += time.perf_counter() - t
+        units += edges_visited(outdeg, d, SSSP_UNREACHED)
+        lane_ok.append(bool(np.array_equal(d, out["lanes"][:, k])))
+        iter_ok.append(it == out["iters"]["sssp"][k])
+    g.close()
+    t = time.perf_counter()
+    gc = oracle.Graph(ccg.nV, ccg.src, ccg.dst)
+    build_s += time.perf_counter() - t
+    t = time.perf_counter()
+    lab, it_cc = gc.cc()
+    run_s += time.perf_counter() - t
+    gc.close()
+    units += ccg.nE
+    cc_ok = bool(np.array_equal(lab, out["cc_labels"]))
+    parity = {"parity": all(lane_ok) and all(iter_ok) and cc_ok and it_cc == out["iters"]["cc"],
+              "sssp_lanes_bit_exact": lane_ok, "sssp_iterations_equal": iter_ok,
+              "cc_labels_bit_exact": cc_ok, "cc_iterations": [it_cc, out["iters"]["cc"]],
+              "oracle": "oracle/gas_oracle.c (refgas.h restated), all host threads"}
+    cpu = {"value": round(units / run_s / 1e9, 5), "unit": "GTEPS", "cores": n_threads,
+           "kind": "port",
+           "sample": (f"the whole step once (SSSP from the 8 sources + CC) through the oracle "
+                      f"port of refgas.h on {n_threads} threads, {run_s:.1f}s of runs "
+                      f"(graph builds {build_s:.1f}s excluded)")}
+    return parity, cpu
+
+
+# ---------------------------------------------------------------------------
+# C1: BFS, R-MAT scale 16, seed 1, highest-degree source
+# ---------------------------------------------------------------------------
+C1_SCALE, C1_SEED = 16, 1
+
+
+def run_c1(args, model):
+    import torch
+
+    import graphreduce_gb300 as gg
+    import oracle
+    from graphreduce_gb300.engine import initial_vertex_data
+    from graphreduce_gb300.graph import EdgeList
+
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    el = EdgeList.rmat(C1_SCALE, EDGE_FACTOR, *RMAT_ABC, seed=C1_SEED, symmetrize=True)
+    src, deg = el.max_out_degree_vertex()   # first vertex of maximum out-degree
+    e = gg.GASEngineGPU("bfs")
+    e.setGraph(el.nV, initial_vertex_data("bfs", el.nV), el.nE, None, el.src, el.dst, sp)
+    e.set_schedule_model(model)
+    init = torch.from_numpy(initial_vertex_data("bfs", el.nV))
+    init_d, init_p = init.to("cuda"), init.pin_memory()
+    out_p = torch.empty(el.nV, dtype=torch.int32).pin_memory()
+    last = {}
+
+    def run(schedule, e2e=False):
+        e.upload_vertex_data_ptr((init_p if e2e else init_d).data_ptr(), sp)
+        e.setActive(src, src + 1, sp)
+        last[schedule] = e.run_schedule(schedule, max_iterations=el.nV + 2, stream=sp)
+        if e2e:
+            e.download_vertex_data_ptr(out_p.data_ptr(), sp)
+
+    run("learned", e2e=True)
+    depth = out_p.numpy().copy()
+    ref, rit = oracle.bfs(el.nV, el.src, el.dst, src)
+    units = edges_visited(el.out_degree(), depth, -1)
+    times = {}
+    for s in ("learned", "push", "pull", "generic"):
+        times[s] = cuda_timed(stream, lambda s=s: run(s), args.steps, args.warmup)
+    ms_e2e = cuda_timed(stream, lambda: run("learned", True), args.steps, 1)
+    same = {}
+    for s in ("push", "pull", "generic"):
+        run(s, e2e=True)
+        same[s] = bool(np.array_equal(out_p.numpy(), depth)) and \
+            last[s].iterations == last["learned"].iterations
+    e.set_profiling(True)
+    e.profile(reset=True)
+    run("learned")
+    torch.cuda.synchronize()
+    p = e.profile()
+    e.set_profiling(False)
+    e.close()
+    if p.push_ms >= p.pull_ms:
+        roof = roofline("k_bfs_push (top-down levels)", "bfs_push", p.push_bytes, p.push_ms,
+                        p.push_launches, "rmat-s16")
+    else:
+        roof = roofline("k_bfs_pull (bottom-up levels)", "bfs_pull", p.pull_bytes, p.pull_ms,
+                        p.pull_launches, "rmat-s16")
+    roof["note"] = ("65,536 vertices: the whole graph (7.6 MB) sits in L2 and each level is a "
+                    "few microseconds, so the run is bound by launch and loop latency")
+    return {
+        "workload": f"BFS rmat-s{C1_SCALE}-ef{EDGE_FACTOR}-sym seed {C1_SEED}, source = first "
+                    f"vertex of maximum out-degree ({src}, degree {deg})",
+        "V": el.nV, "E": el.nE, "levels": last["learned"].iterations,
+        "schedule": "learned (direction rule: bottom-up while the frontier's out-edges > E/16)",
+        "ms": round(times["learned"], 4), "gteps": gteps(units, times["learned"]),
+        "e2e": {"ms": round(ms_e2e, 4), "gteps": gteps(units, ms_e2e),
+                "h2d_bytes": el.nV * 4, "d2h_bytes": el.nV * 4},
+        "fixed_schedules": {s: {"ms": round(times[s], 4), "gteps": gteps(units, times[s]),
+                                "identical_output": same[s]}
+                            for s in ("push", "pull", "generic")},
+        "parity": bool(np.array_equal(depth, ref)) and rit == last["learned"].iterations
+        and all(same.values()),
+        "parity_detail": "depths and level count bit-exact against the oracle BFS",
+        "roofline": roof,
+    }
+
+
+# ---------------------------------------------------------------------------
+# C3: precision-form PageRank, R-MAT scale 24 directed
+# ---------------------------------------------------------------------------
+PR_SCALE, PR_SEED = 24, 4
+PR_METRIC = "GTEPS (precision PageRank, R-MAT scale {scale} directed, E x iterations / time)"
+PR_DAMPING, PR_TOL = 0.85, 1e-6
+
+
+def run_pagerank(args, check=True):
+    """Uniform start (timed), the warm start (timed), the gather's roofline
+    from one profiled run, and the FP64 oracle on the same graph."""
+    import torch
+
+    import graphreduce_gb300 as gg
+    from graphreduce_gb300.engine import initial_vertex_data
+    from graphreduce_gb300.graph import EdgeList
+    from graphreduce_gb300.learn import DATA, MLP
+
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    scale = args.pr_scale
+    t = time.time()
+    el = EdgeList.rmat(scale, EDGE_FACTOR, *RMAT_ABC, seed=PR_SEED, symmetrize=False)
+    log(f"pagerank workload: scale {scale}: V={el.nV} E={el.nE}, generated in "
+        f"{time.time() - t:.1f}s")
+    e = gg.GASEngineGPU("pagerank")
+    e.setGraph(el.nV, initial_vertex_data("pagerank", el.nV, 0, el.out_degree()), el.nE,
+               None, el.src, el.dst, sp)
+    warm_model = MLP.load(DATA / "warm_start_head.npz")
+    ranks_d = torch.empty(el.nV, dtype=torch.float32, device="cuda")
+    init_d = torch.empty(el.nV, dtype=torch.float32, device="cuda")
+    ranks_p = torch.empty(el.nV, dtype=torch.float32).pin_memory()
+    out = {}
+
+    def uniform(e2e=False):
+        out["u"] = e.pagerank_precision(PR_DAMPING, PR_TOL, 1000,
+                                        (ranks_p if e2e else ranks_d).data_ptr(), sp)[1]
+
+    if args.launch_list:
+        # one uniform-start run and nothing else (for an ncu launch list)
+        uniform()
+        torch.cuda.synchronize()
+        e.close()
+        return {"launch_list": True, "iterations": out["u"].iterations}
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms = cuda_timed(stream, uniform, args.steps, args.warmup)
+    clocks = clk.summary()
+    ms_e2e = cuda_timed(stream, lambda: uniform(True), max(1, args.steps), 1)
+    st_u = out["u"]
+    r_uni = ranks_d.cpu().numpy()
+
+    def warm():  # the head's proposal, then the same iteration from it
+        e.pagerank_warm_start(warm_model, PR_DAMPING, init_d.data_ptr())
+        out["w"] = e.pagerank_precision_from(init_d.data_ptr(), PR_DAMPING, PR_TOL, 1000, sp,
+                                             out=ranks_d.data_ptr())[1]
+
+    ms_warm = cuda_timed(stream, warm, args.steps, 1)
+    st_w = out["w"]
+    r_warm = ranks_d.cpu().numpy()
+    # roofline: one profiled run (events around every iteration's gather)
+    e.set_profiling(True)
+    e.profile(reset=True)
+    e.pagerank_precision(PR_DAMPING, PR_TOL, 1000, ranks_d.data_ptr(), sp)
+    prof = e.profile()
+    e.set_profiling(False)
+    e.close()
+    units = el.nE * st_u.iterations
+    roof = roofline("k_pr_merge + k_pr_merge_fix (one PageRank iteration's gather)",
+                    "pr_gather", prof.pagerank_bytes, prof.pagerank_ms,
+                    prof.pagerank_launches, f"rmat-s{scale}")
+    res = {
+        "metric": PR_METRIC.format(scale=scale), "value": gteps(units, ms), "unit": "GTEPS",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (two-sum compensated gather) + f64 residual",
+        "data": "synthetic (seeded R-MAT)",
+        "config": {"workload": f"precision PageRank, R-MAT scale {scale}, edge factor "
+                               f"{EDGE_FACTOR}, directed, seed {PR_SEED}, d={PR_DAMPING}, "
+                               f"L1 tol {PR_TOL}",
+                   "V": el.nV, "E": el.nE, "iterations": st_u.iterations,
+                   "residual": st_u.residual, "l2": "inputs larger than L2"},
+        "e2e": {"value": gteps(units, ms_e2e), "unit": "GTEPS", "ms_per_step": round(ms_e2e, 3),
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": el.nV * 4,
+                "copies": "graph resident; the ranks come down to pinned host memory"},
+        "warm_start": {"iterations": st_w.iterations, "uniform_iterations": st_u.iterations,
+                       "ms": round(ms_warm, 3), "speedup": round(ms / ms_warm, 4),
+                       "l1_between_results": float(np.abs(r_uni.astype(np.float64) -
+                                                          r_warm).sum())},
+        "roofline": roof,
+        "clocks": clocks,
+    }
+    if check:
+        import oracle
+        n = oracle_threads()
+        t = time.time()
+        r64, it64, _ = oracle.pagerank_fp64(el.nV, el.src, el.dst, PR_DAMPING, PR_TOL)
+        d = np.abs(r_uni.astype(np.float64) - r64)
+        l1, mx = float(d.sum()), float(d.max())
+        res["error_vs_fp64_oracle"] = {"l1": l1, "max_abs": mx, "oracle_iterations": it64,
+                                       "oracle_seconds": round(time.time() - t, 1),
+                                       "oracle_threads": n}
+        res["parity"] = l1 <= 1e-6
+        res["parity_detail"] = ("L1 error of the FP32 ranks against the FP64 oracle's <= 1e-6 "
+                                "(same damping and residual tolerance)")
+    return res
+
+
+# ---------------------------------------------------------------------------
+# C4: learned schedule and warm start on held-out graphs
+# ---------------------------------------------------------------------------
+C4_SEED = 5
+C4_SCHEDULES = ("auto", "push", "pull", "learned")
+
+
+def run_c4(args, model, pr_warm):
+    """SSSP and CC under every schedule on graphs the heads never saw; the
+    learned schedule against the fixed heuristic (AUTO) and against the best
+    fixed schedule; outputs identical across schedules.  The PageRank warm
+    start against the uniform start (iterations to the same tolerance)."""
+    import torch
+
+    import graphreduce_gb300 as gg
+    from graphreduce_gb300.engine import initial_vertex_data
+    from graphreduce_gb300.graph import EdgeList
+    from graphreduce_gb300.learn import DATA, MLP
+
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    scale = args.pr_scale
+    graphs = {
+        f"rmat{scale}": lambda: EdgeList.rmat(scale, EDGE_FACTOR, *RMAT_ABC, seed=C4_SEED,
+                                              symmetrize=True),
+        "er2^24": lambda: EdgeList.erdos_renyi(1 << scale, 8 << scale, seed=C4_SEED,
+                                               symmetrize=True),
+    }
+    res = {}
+    all_ok = True
+    for name, make in graphs.items():
+        t = time.time()
+        el = make().with_uniform_weights(1, 64, C4_SEED)
+        src = int(el.sample_sources(1, C4_SEED)[0])
+        log(f"c4 {name}: V={el.nV} E={el.nE}, generated in {time.time() - t:.1f}s")
+        row = {"V": el.nV, "E": el.nE}
+        for program in ("sssp", "cc"):
+            e = gg.GASEngineGPU(program)
+            vd = initial_vertex_data(program, el.nV, src)
+            e.setGraph(el.nV, vd, el.nE, el.weights if program == "sssp" else None,
+                       el.src, el.dst, sp)
+            e.set_schedule_model(model)
+            init_d = torch.from_numpy(vd).to("cuda")
+            host = np.empty(el.nV, np.int32)
+            outs, r = {}, {}
+            for s in C4_SCHEDULES:
+                st = {}
+
+                def run(s=s, st=st):
+                    e.upload_vertex_data_ptr(init_d.data_ptr(), sp)
+                    e.setActive(0, el.nV, sp)
+                    st["s"] = e.run_schedule(s, max_iterations=el.nV + 2, stream=sp)
+
+                ms = cuda_timed(stream, run, max(2, min(args.steps, 5)), 1)
+                e.download_vertex_data(host, sp)
+                outs[s] = host.copy()
+                r[s] = {"ms": round(ms, 3), "iterations": st["s"].iterations,
+                        "pull_iters": st["s"].pull_iters}
+            e.close()
+            same = all(np.array_equal(outs["auto"], o) for o in outs.values()) and \
+                len({v["iterations"] for v in r.values()}) == 1
+            best_fixed = min(("auto", "push", "pull"), key=lambda s: r[s]["ms"])
+            r["identical_outputs"] = same
+            r["learned_speedup_vs_auto"] = round(r["auto"]["ms"] / r["learned"]["ms"], 4)
+            r["best_fixed"] = best_fixed
+            r["learned_vs_best_fixed"] = round(r[best_fixed]["ms"] / r["learned"]["ms"], 4)
+            all_ok &= same
+            row[program] = r
+        del el
+        res[name] = row
+        free_gpu()
+    # warm start on the held-out ER graph (the R-MAT one is C3's graph)
+    d = EdgeList.erdos_renyi(1 << scale, 16 << scale, seed=C4_SEED, symmetrize=False)
+    warm_model = MLP.load(DATA / "warm_start_head.npz")
+    e = gg.GASEngineGPU("pagerank")
+    e.setGraph(d.nV, initial_vertex_data("pagerank", d.nV, 0, d.out_degree()), d.nE, None,
+               d.src, d.dst, sp)
+    r_uni, st_uni = e.pagerank_precision_from(None, PR_DAMPING, PR_TOL, 1000, sp)
+    init = e.pagerank_warm_start(warm_model, PR_DAMPING)
+    r_warm, st_warm = e.pagerank_precision_from(init, PR_DAMPING, PR_TOL, 1000, sp)
+    e.close()
+    res["pagerank_warm_start"] = {
+        f"rmat{scale}_directed_seed{PR_SEED}": pr_warm,
+        "er2^24_directed": {"uniform_iterations": st_uni.iterations,
+                            "warm_iterations": st_warm.iterations,
+                            "l1_between_results": float(np.abs(r_uni.astype(np.float64) -
+                                                               r_warm).sum())}}
+    res["parity"] = all_ok
+    res["parity_detail"] = ("SSSP distances and CC labels identical under auto, push, pull and "
+                            "learned, with equal iteration counts (the oracle pins the "
+                            "schedules on C1/C2 and in the GPU tests)")
+    return res
+
+
+# ---------------------------------------------------------------------------
+# C5: 64 graphs x (16 BFS sources + 16 PPR seeds) in one graph launch
+# ---------------------------------------------------------------------------
+BATCH_GRAPHS, BATCH_LANES, BATCH_SEED = 64, 16, 6
+BATCH_METRIC = "GTEPS (batched: 64 R-MAT graphs x (16 BFS + 16 PPR))"
+PPR_DAMPING, PPR_TOL = 0.85, 1e-6
+# A PPR lane stops when its L1 step <= tol; PPR is a d-contraction in L1, so
+# the lane is within d/(1-d) * tol of its fixed point (5.67e-6), plus FP32
+# rounding of ranks that sum to at most 1.
+PPR_L1_BOUND = 8e-6
+
+
+def make_batched_workload(n_graphs=BATCH_GRAPHS):
+    """Scale U[12,20], edge factor U[8,32] per graph (seed 6), symmetrised
+    R-MAT; 16 BFS sources and 16 PPR seeds per graph, uniform over the
+    graph's largest component (seeded per graph)."""
+    from graphreduce_gb300.graph import EdgeList
+    rng = np.random.default_rng(BATCH_SEED)
+    scales = rng.integers(12, 21, n_graphs)
+    efs = rng.integers(8, 33, n_graphs)
+    t = time.time()
+    graphs, srcs, seeds = [], [], []
+    for g in range(n_graphs):
+        el = EdgeList.rmat(int(scales[g]), int(efs[g]), *RMAT_ABC, seed=1000 + g,
+                           symmetrize=True)
+        graphs.append(el)
+        srcs.append(el.sample_sources(BATCH_LANES, 2000 + g))
+        seeds.append(el.sample_sources(BATCH_LANES, 3000 + g))
+    log(f"batched workload: {n_graphs} graphs, V={sum(x.nV for x in graphs)} "
+        f"E={sum(x.nE for x in graphs)}, generated in {time.time() - t:.1f}s")
+    return graphs, np.stack(srcs).astype(np.int32), np.stack(seeds).astype(np.int32), \
+        scales, efs
+
+
+def run_batched(args, check=True):
+    import torch
+
+    import graphreduce_gb300 as gg
+    from graphreduce_gb300.engine import initial_vertex_data
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    graphs, srcs, seeds, scales, efs = make_batched_workload(args.batch_graphs)
+    G, L = len(graphs), BATCH_LANES
+    b = gg.Batch()
+    for el in graphs:
+        b.add_graph(el.nV, el.src, el.dst)
+    t = time.time()
+    b.build(sp)
+    V, E = b.num_vertices, b.num_edges
+    if args.launch_list:
+        # one batch run and nothing else (for an ncu launch list / capture)
+        r = b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, piece_edges=256, stream=sp)
+        torch.cuda.synchronize()
+        b.close()
+        return {"launch_list": True, "gpu_launches": r.stats.kernel_launches}
+    piece, ms_iter = b.tune(L, PPR_DAMPING, 5, sp)
+    log(f"batch build {time.time() - t:.1f}s; tuned piece {piece} edges, "
+        f"{ms_iter:.3f} ms per PPR iteration")
+    depth_d = torch.empty((V, L), dtype=torch.int32, device=dev)
+    rank_d = torch.empty((V, L), dtype=torch.float32, device=dev)
+    depth_h = torch.empty((V, L), dtype=torch.int32).pin_memory()
+    rank_h = torch.empty((V, L), dtype=torch.float32).pin_memory()
+
+    def step(e2e):
+        if e2e:
+            return b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, depth_out=depth_h.data_ptr(),
+                         rank_out=rank_h.data_ptr(), stream=sp)
+        return b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, depth_out=depth_d.data_ptr(),
+                     rank_out=rank_d.data_ptr(), stream=sp)
+
+    # units: BFS per (graph, lane) the out-degrees of the reached vertices;
+    # PPR per (graph, lane) E_graph x iterations
+    r = step(True)
+    depth = depth_h.numpy().copy()
+    rank = rank_h.numpy().copy()
+    bfs_units = 0
+    for g, el in enumerate(graphs):
+        od = el.out_degree().astype(np.int64)
+        d = depth[b.vertex_offset(g):b.vertex_offset(g) + el.nV]
+        bfs_units += int(((d >= 0) * od[:, None]).sum())
+    ppr_iters = r.stats.ppr_iterations
+    ppr_units = int(sum(el.nE for el in graphs)) * L * ppr_iters
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms = cuda_timed(stream, lambda: step(False), args.steps, args.warmup)
+    clocks = clk.summary()
+    ms_e2e = cuda_timed(stream, lambda: step(True), max(1, args.steps), 1)
+    st = step(False).stats
+
+    # BFS-only and PPR-only batch times (device-resident)
+    ms_bfs = cuda_timed(stream, lambda: b.run(srcs, None, depth_out=depth_d.data_ptr(),
+                                              stream=sp), args.steps, 1)
+    ms_ppr = cuda_timed(stream, lambda: b.run(None, seeds, PPR_DAMPING, PPR_TOL,
+                                              rank_out=rank_d.data_ptr(), stream=sp),
+                        args.steps, 1)
+
+    # the same instances run one by one on the plain single-graph engines
+    from graphreduce_gb300.learn import DATA, MLP
+    model = MLP.load(DATA / "schedule_head.npz")
+    eb, ep, init_b = [], [], []
+    for el in graphs:
+        e = gg.GASEngineGPU("bfs")
+        e.setGraph(el.nV, initial_vertex_data("bfs", el.nV), el.nE, None, el.src, el.dst, sp)
+        e.set_schedule_model(model)
+        eb.append(e)
+        p = gg.GASEngineGPU("pagerank")
+        p.setGraph(el.nV, initial_vertex_data("pagerank", el.nV, 0, el.out_degree()), el.nE,
+                   None, el.src, el.dst, sp)
+        ep.append(p)
+        init_b.append(torch.from_numpy(initial_vertex_data("bfs", el.nV)).to(dev))
+    out_p = torch.empty(max(el.nV for el in graphs), dtype=torch.float32, device=dev)
+    plain_ppr_iters = [0]
+
+    def plain_bfs():
+        for g, el in enumerate(graphs):
+            for l in range(L):
+                s = int(srcs[g, l])
+                eb[g].upload_vertex_data_ptr(init_b[g].data_ptr(), sp)
+                eb[g].setActive(s, s + 1, sp)
+                eb[g].run_schedule("learned", max_iterations=el.nV + 2, stream=sp)
+
+    def plain_ppr():
+        plain_ppr_iters[0] = 0
+        for g, el in enumerate(graphs):
+            for l in range(L):
+                _, pst = ep[g].ppr_precision(int(seeds[g, l]), PPR_DAMPING, PPR_TOL,
+                                             out=out_p.data_ptr(), stream=sp)
+                plain_ppr_iters[0] += pst.iterations
+
+    ms_plain_bfs = cuda_timed(stream, plain_bfs, 1, 1)
+    ms_plain_ppr = cuda_timed(stream, plain_ppr, 1, 1)
+    for e in eb + ep:
+        e.close()
+    offsets = [b.vertex_offset(g) for g in range(G)]
+    b.close()
+
+    units = bfs_units + ppr_units
+    value = units / (ms * 1e-3) / 1e9
+    # roofline of the PPR iteration (pieces + fix + residual kernels), timed by
+    # the autotuner with CUDA events: per edge its source index and the L
+    # lanes of the source's contribution; per vertex offsets (8 B), seed mask
+    # (4 B), old rank, new rank and new contribution (3 x 4L B)
+    ppr_bytes = E * (4 + 4 * L) + V * (12 + 12 * L)
+    roof = roofline("PPR iteration (k_ppr_pieces + k_ppr_fix + k_ppr_finish)",
+                    "ppr_iteration", ppr_bytes, ms_iter, 1,
+                    "batched-64" if G == BATCH_GRAPHS else f"batched-{G}",
+                    {"traffic_note": "DRAM bytes per iteration; the [V][16] contribution "
+                                     "gathers are mostly L2 hits", "piece_edges": piece})
+    res = {
+        "metric": BATCH_METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32 (BFS) + f32 (PPR, FP64 residual)",
+        "data": "synthetic (seeded R-MAT graphs)",
+        "config": {"workload": f"batched {G} R-MAT graphs, scale U[12,20], edge factor "
+                               f"U[8,32] (seed {BATCH_SEED}), symmetrised; {L} BFS sources + "
+                               f"{L} PPR seeds each (d={PPR_DAMPING}, L1 tol {PPR_TOL})",
+                   "union_V": V, "union_E": E,
+                   "scales": scales.tolist(), "edge_factors": efs.tolist(),
+                   "bfs_units": bfs_units, "ppr_units": ppr_units,
+                   "ppr_iterations": ppr_iters, "bfs_iterations": st.bfs_iterations,
+                   "piece_edges": piece,
+                   "l2": "inputs larger than L2 (union CSR+CSC and [V][16] rank arrays)"},
+        "e2e": {"value": round(units / (ms_e2e * 1e-3) / 1e9, 4), "unit": "GTEPS",
+                "ms_per_step": round(ms_e2e, 3),
+                "h2d_bytes_per_step": int(srcs.nbytes + V * 4),  # sources + PPR seed mask
+                "d2h_bytes_per_step": int(V * L * 8)},
+        "gpu_launches": st.kernel_launches * args.steps,
+        "graph_launches_per_step": st.graph_launches,
+        "split": {"bfs_ms": round(ms_bfs, 3), "ppr_ms": round(ms_ppr, 3),
+                  "bfs_gteps": gteps(bfs_units, ms_bfs), "ppr_gteps": gteps(ppr_units, ms_ppr)},
+        "plain_sequential": {
+            "bfs_ms": round(ms_plain_bfs, 3), "ppr_ms": round(ms_plain_ppr, 3),
+            "ppr_iterations_total": plain_ppr_iters[0],
+            "bfs_speedup_of_batch": round(ms_plain_bfs / ms_bfs, 3),
+            "ppr_speedup_of_batch": round(ms_plain_ppr / ms_ppr, 3),
+            "total_speedup_of_batch": round((ms_plain_bfs + ms_plain_ppr) / ms, 3),
+            "per_instance_ms_batched": round(ms / (G * L * 2), 5),
+            "per_instance_ms_plain": round((ms_plain_bfs + ms_plain_ppr) / (G * L * 2), 5)},
+        "roofline": roof,
+        "clocks": clocks,
+    }
+    if check:
+        res.update(batched_parity_sample(graphs, srcs, seeds, depth, rank, offsets))
+    return res
+
+
+def batched_parity_sample(graphs, srcs, seeds, depth, rank, offsets):
+    """A per-lane sample of the batched results against the oracle: BFS lanes
+    0 and 15 of four graphs (the smallest, the largest and two between)
+    bit-exact; PPR lanes 0 and 15 of two graphs within the stated L1 bound
+    of the FP64 oracle."""
+    import oracle
+    oracle_threads()
+    order = np.argsort([el.nV for el in graphs], kind="stable")
+    pick = [int(order[0]), int(order[len(order) // 3]), int(order[2 * len(order) // 3]),
+            int(order[-1])]
+    bfs_ok, ppr_err = [], []
+    for g in pick:
+        el = graphs[g]
+        og = oracle.Graph(el.nV, el.src, el.dst)
+        sl = slice(offsets[g], offsets[g] + el.nV)
+        for lane in (0, BATCH_LANES - 1):
+            ref, _ = og.bfs(int(srcs[g, lane]))
+            bfs_ok.append(bool(np.array_equal(depth[sl, lane], ref)))
+        if g in pick[:2]:
+            for lane in (0, BATCH_LANES - 1):
+                r64, _, _ = og.ppr_fp64(int(seeds[g, lane]), PPR_DAMPING, 1e-12)
+                ppr_err.append(float(np.abs(rank[sl, lane].astype(np.float64) - r64).sum()))
+        og.close()
+    return {"parity": all(bfs_ok) and max(ppr_err) <= PPR_L1_BOUND,
+            "parity_detail": {"graphs": pick, "bfs_lanes_bit_exact": bfs_ok,
+                              "ppr_lane_l1_vs_fp64": ppr_err, "ppr_l1_bound": PPR_L1_BOUND}}
 
 
 # ---------------------------------------------------------------------------
@@ -564,22 +1189,7 @@ def run_lanes24(args):
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
     scale, L = args.pr_scale, LANES24
-    peak, peak_kind = measured_peaks()
     model = MLP.load(DATA / "schedule_head.npz")
-
-    def timed(fn, steps, warmup):
-        for _ in range(warmup):
-            fn()
-        torch.cuda.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        z = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(steps):
-            fn()
-        z.record(stream)
-        torch.cuda.synchronize()
-        return a.elapsed_time(z) / steps
-
     out = {"metric": f"GTEPS (batched lanes on one R-MAT scale-{scale} graph: "
                      f"{L} BFS sources, {L} PPR seeds)", "unit": "GTEPS", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
@@ -617,7 +1227,7 @@ def run_lanes24(args):
     od = el.out_degree().astype(np.int64)
     bfs_units = int(((depth >= 0) * od[:, None]).sum())
     with ClockSampler(torch.cuda.current_device()) as clk:
-        ms_b = timed(run_b, args.steps, args.warmup)
+        ms_b = cuda_timed(stream, run_b, args.steps, args.warmup)
     b.set_profiling(True)
     b.profile(reset=True)
     run_b()
@@ -641,7 +1251,7 @@ def run_lanes24(args):
     e.run_schedule("learned", max_iterations=el.nV + 2, stream=sp)
     e.download_vertex_data(one.numpy(), sp)
     same = bool(np.array_equal(one.numpy(), depth[:, 0]))
-    ms_plain_b = timed(plain_bfs, 1, 1)
+    ms_plain_b = cuda_timed(stream, plain_bfs, 1, 1)
     # the single-source engine's push roofline over the same 16 runs
     e.set_profiling(True)
     e.profile(reset=True)
@@ -651,24 +1261,20 @@ def run_lanes24(args):
     e.set_profiling(False)
     e.close()
     b.close()
-    ach1 = pe.push_bytes / (pe.push_ms * 1e-3) / 1e9 if pe.push_ms > 0 else 0.0
-    ach = pb.push_bytes / (pb.push_ms * 1e-3) / 1e9 if pb.push_ms > 0 else 0.0
     out["bfs"] = {"graph": f"rmat-s{scale}-ef{EDGE_FACTOR}-sym seed {GRAPH_SEED}",
                   "V": el.nV, "E": el.nE, "lanes": L, "ms": round(ms_b, 3),
-                  "gteps": round(bfs_units / (ms_b * 1e-3) / 1e9, 4),
+                  "gteps": gteps(bfs_units, ms_b),
                   "plain_one_by_one_ms": round(ms_plain_b, 3),
                   "speedup_vs_plain": round(ms_plain_b / ms_b, 3),
                   "lane0_equals_single_source_run": same,
-                  "plain_push_roofline": {"kernel": "k_push (single-source BFS, learned)",
-                                          "achieved": round(ach1, 1), "unit": "GB/s",
-                                          "frac": round(ach1 / peak, 4),
-                                          "launches": pe.push_launches,
-                                          "pull_launches": pe.pull_launches},
-                  "roofline": {"kernel": "k_ms_push (16-lane BFS push)", "bound": "hbm",
-                               "achieved": round(ach, 1), "unit": "GB/s", "peak": peak,
-                               "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                               "launches": pb.push_launches,
-                               "push_share_of_run": round(pb.push_ms / ms_b, 3)}}
+                  "plain_push_roofline": roofline("k_push (single-source BFS, learned)",
+                                                  "bfs_push", pe.push_bytes, pe.push_ms,
+                                                  pe.push_launches, f"rmat-s{scale}",
+                                                  {"pull_launches": pe.pull_launches}),
+                  "roofline": roofline("k_ms_push (16-lane BFS push)", "ms_push",
+                                       pb.push_bytes, pb.push_ms, pb.push_launches,
+                                       f"rmat-s{scale}",
+                                       {"push_share_of_run": round(pb.push_ms / ms_b, 3)})}
     del el, depth, depth_d
     clocks_b = clk.summary()
 
@@ -683,7 +1289,7 @@ def run_lanes24(args):
     run_p = lambda: b.run(ppr_seeds=seeds[None, :], damping=PPR_DAMPING, tol=PPR_TOL,
                           rank_out=rank_d.data_ptr(), stream=sp)
     st = run_p().stats
-    ms_p = timed(run_p, args.steps, args.warmup)
+    ms_p = cuda_timed(stream, run_p, args.steps, args.warmup)
     p = gg.GASEngineGPU("pagerank")
     p.setGraph(d.nV, initial_vertex_data("pagerank", d.nV, 0, d.out_degree()), d.nE, None,
                d.src, d.dst, sp)
@@ -697,400 +1303,138 @@ def run_lanes24(args):
                                      stream=sp)
             plain_iters[0] += pst.iterations
 
-    ms_plain_p = timed(plain_ppr, 1, 0)
+    ms_plain_p = cuda_timed(stream, plain_ppr, 1, 0)
     p.close()
     b.close()
     ppr_units = d.nE * L * st.ppr_iterations
     ppr_bytes = d.nE * (4 + 4 * L) + d.nV * (12 + 12 * L)
-    ach = ppr_bytes / (ms_iter * 1e-3) / 1e9
     out["ppr"] = {"graph": f"rmat-s{scale}-ef{EDGE_FACTOR} directed seed {PR_SEED}",
                   "V": d.nV, "E": d.nE, "lanes": L, "iterations": st.ppr_iterations,
-                  "ms": round(ms_p, 3), "gteps": round(ppr_units / (ms_p * 1e-3) / 1e9, 4),
+                  "ms": round(ms_p, 3), "gteps": gteps(ppr_units, ms_p),
                   "plain_one_by_one_ms": round(ms_plain_p, 3),
                   "plain_iterations": plain_iters[0],
                   "speedup_vs_plain": round(ms_plain_p / ms_p, 3),
                   "residual": st.ppr_residual,
-                  "roofline": {"kernel": "PPR iteration (k_ppr_pieces + k_ppr_fix + k_ppr_finish)",
-                               "bound": "hbm", "achieved": round(ach, 1), "unit": "GB/s",
-                               "peak": peak, "frac": round(ach / peak, 4),
-                               "peak_source": peak_kind, "piece_edges": piece,
-                               "ms_per_iteration": round(ms_iter, 4),
-                               "algorithmic_bytes_per_iteration": int(ppr_bytes)}}
+                  "roofline": roofline("PPR iteration (k_ppr_pieces + k_ppr_fix + "
+                                       "k_ppr_finish)", "ppr_iteration", ppr_bytes, ms_iter, 1,
+                                       f"rmat-s{scale}-16-seeds", {"piece_edges": piece})}
     total_units = bfs_units + ppr_units
-    out["value"] = round(total_units / ((ms_b + ms_p) * 1e-3) / 1e9, 4)
+    out["value"] = gteps(total_units, ms_b + ms_p)
     out["ms_per_step"] = round(ms_b + ms_p, 3)
     out["clocks"] = clocks_b
     return out
 
 
 # ---------------------------------------------------------------------------
-# batched workload: 64 graphs x (16 BFS sources + 16 PPR seeds)
+# the reference arm: the oracle port of refgas.h on the host cores
 # ---------------------------------------------------------------------------
-BATCH_GRAPHS, BATCH_LANES, BATCH_SEED = 64, 16, 6
-BATCH_METRIC = "GTEPS (batched: 64 R-MAT graphs x (16 BFS + 16 PPR))"
-PPR_DAMPING, PPR_TOL = 0.85, 1e-6
-# DRAM bytes (read + write) of one PPR iteration of this workload (64 graphs,
-# 16 lanes): one-pass ncu metrics over all 31 k_ppr_pieces and k_ppr_fix
-# launches of a run (9.50 GB + 0.80 GB per iteration), captured with
-#   GAS_HOST_LOOP=1 ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,\
-#     dram__bytes_write.sum --clock-control none -k regex:"k_ppr_pieces|k_ppr_fix" \
-#     python bench.py --workload batched --launch-list
-PPR_TRAFFIC_64 = 10.30e9
-
-
-def make_batched_workload(n_graphs=BATCH_GRAPHS):
-    """Scale U[12,20], edge factor U[8,32] per graph (seed 6), symmetrised
-    R-MAT; 16 BFS sources and 16 PPR seeds per graph, uniform over the
-    graph's largest component (seeded per graph)."""
-    from graphreduce_gb300.graph import EdgeList
-    rng = np.random.default_rng(BATCH_SEED)
-    scales = rng.integers(12, 21, n_graphs)
-    efs = rng.integers(8, 33, n_graphs)
-    t = time.time()
-    graphs, srcs, seeds = [], [], []
-    for g in range(n_graphs):
-        el = EdgeList.rmat(int(scales[g]), int(efs[g]), *RMAT_ABC, seed=1000 + g,
-                           symmetrize=True)
-        graphs.append(el)
-        srcs.append(el.sample_sources(BATCH_LANES, 2000 + g))
-        seeds.append(el.sample_sources(BATCH_LANES, 3000 + g))
-    log(f"batched workload: {n_graphs} graphs, V={sum(x.nV for x in graphs)} "
-        f"E={sum(x.nE for x in graphs)}, generated in {time.time() - t:.1f}s")
-    return graphs, np.stack(srcs).astype(np.int32), np.stack(seeds).astype(np.int32), \
-        scales, efs
-
-
-def run_batched(args):
-    import torch
-
-    import graphreduce_gb300 as gg
-    from graphreduce_gb300.engine import initial_vertex_data
-
-    dev = torch.device("cuda", torch.cuda.current_device())
-    stream = torch.cuda.current_stream()
-    sp = stream.cuda_stream
-    graphs, srcs, seeds, scales, efs = make_batched_workload(args.batch_graphs)
-    G, L = len(graphs), BATCH_LANES
-    b = gg.Batch()
-    for el in graphs:
-        b.add_graph(el.nV, el.src, el.dst)
-    t = time.time()
-    b.build(sp)
-    V, E = b.num_vertices, b.num_edges
-    if args.launch_list:
-        # one batch run and nothing else (for an ncu launch list / capture)
-        r = b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, piece_edges=256, stream=sp)
-        torch.cuda.synchronize()
-        return {"launch_list": True, "gpu_launches": r.stats.kernel_launches}
-    piece, ms_iter = b.tune(L, PPR_DAMPING, 5, sp)
-    log(f"batch build {time.time() - t:.1f}s; tuned piece {piece} edges, "
-        f"{ms_iter:.3f} ms per PPR iteration")
-    depth_d = torch.empty((V, L), dtype=torch.int32, device=dev)
-    rank_d = torch.empty((V, L), dtype=torch.float32, device=dev)
-    depth_h = torch.empty((V, L), dtype=torch.int32).pin_memory()
-    rank_h = torch.empty((V, L), dtype=torch.float32).pin_memory()
-
-    def step(e2e):
-        if e2e:
-            return b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, depth_out=depth_h.data_ptr(),
-                         rank_out=rank_h.data_ptr(), stream=sp)
-        return b.run(srcs, seeds, PPR_DAMPING, PPR_TOL, depth_out=depth_d.data_ptr(),
-                     rank_out=rank_d.data_ptr(), stream=sp)
-
-    # units: BFS per (graph, lane) the out-degrees of the reached vertices;
-    # PPR per (graph, lane) E_graph x iterations
-    r = step(True)
-    depth = depth_h.numpy()
-    bfs_units = 0
-    for g, el in enumerate(graphs):
-        od = el.out_degree().astype(np.int64)
-        d = depth[b.vertex_offset(g):b.vertex_offset(g) + el.nV]
-        bfs_units += int(((d >= 0) * od[:, None]).sum())
-    ppr_iters = r.stats.ppr_iterations
-    ppr_units = int(sum(el.nE for el in graphs)) * L * ppr_iters
-
-    def timed(fn, steps, warmup):
-        for _ in range(warmup):
-            fn()
-        torch.cuda.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        z = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(steps):
-            fn()
-        z.record(stream)
-        torch.cuda.synchronize()
-        return a.elapsed_time(z) / steps
-
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        ms = timed(lambda: step(False), args.steps, args.warmup)
-    clocks = clk.summary()
-    ms_e2e = timed(lambda: step(True), max(1, args.steps), 1)
-    st = step(False).stats
-
-    # BFS-only and PPR-only batch times (device-resident)
-    ms_bfs = timed(lambda: b.run(srcs, None, depth_out=depth_d.data_ptr(), stream=sp),
-                   args.steps, 1)
-    ms_ppr = timed(lambda: b.run(None, seeds, PPR_DAMPING, PPR_TOL,
-                                 rank_out=rank_d.data_ptr(), stream=sp), args.steps, 1)
-
-    # the same instances run one by one on the plain single-graph engines
-    from graphreduce_gb300.learn import DATA, MLP
-    model = MLP.load(DATA / "schedule_head.npz")
-    eb, ep, init_b = [], [], []
-    for el in graphs:
-        e = gg.GASEngineGPU("bfs")
-        e.setGraph(el.nV, initial_vertex_data("bfs", el.nV), el.nE, None, el.src, el.dst, sp)
-        e.set_schedule_model(model)
-        eb.append(e)
-        p = gg.GASEngineGPU("pagerank")
-        p.setGraph(el.nV, initial_vertex_data("pagerank", el.nV, 0, el.out_degree()), el.nE,
-                   None, el.src, el.dst, sp)
-        ep.append(p)
-        init_b.append(torch.from_numpy(initial_vertex_data("bfs", el.nV)).to(dev))
-    out_p = torch.empty(max(el.nV for el in graphs), dtype=torch.float32, device=dev)
-    plain_ppr_iters = [0]
-
-    def plain_bfs():
-        for g, el in enumerate(graphs):
-            for l in range(L):
-                s = int(srcs[g, l])
-                eb[g].upload_vertex_data_ptr(init_b[g].data_ptr(), sp)
-                eb[g].setActive(s, s + 1, sp)
-                eb[g].run_schedule("learned", max_iterations=el.nV + 2, stream=sp)
-
-    def plain_ppr():
-        plain_ppr_iters[0] = 0
-        for g, el in enumerate(graphs):
-            for l in range(L):
-                _, pst = ep[g].ppr_precision(int(seeds[g, l]), PPR_DAMPING, PPR_TOL,
-                                             out=out_p.data_ptr(), stream=sp)
-                plain_ppr_iters[0] += pst.iterations
-
-    ms_plain_bfs = timed(plain_bfs, 1, 1)
-    ms_plain_ppr = timed(plain_ppr, 1, 1)
-    for e in eb + ep:
-        e.close()
-
-    units = bfs_units + ppr_units
-    value = units / (ms * 1e-3) / 1e9
-    # roofline of the PPR iteration (pieces + fix + residual kernels), timed by
-    # the autotuner with CUDA events: per edge its source index and the L
-    # lanes of the source's contribution; per vertex offsets (8 B), seed mask
-    # (4 B), old rank, new rank and new contribution (3 x 4L B)
-    ppr_bytes = E * (4 + 4 * L) + V * (12 + 12 * L)
-    peak, peak_kind = measured_peaks()
-    achieved = ppr_bytes / (ms_iter * 1e-3) / 1e9
-    return {
-        "metric": BATCH_METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "int32 (BFS) + f32 (PPR, FP64 residual)",
-        "data": "synthetic (seeded R-MAT graphs)",
-        "config": {"workload": f"batched {G} R-MAT graphs, scale U[12,20], edge factor "
-                               f"U[8,32] (seed {BATCH_SEED}), symmetrised; {L} BFS sources + "
-                               f"{L} PPR seeds each (d={PPR_DAMPING}, L1 tol {PPR_TOL})",
-                   "union_V": V, "union_E": E,
-                   "scales": scales.tolist(), "edge_factors": efs.tolist(),
-                   "bfs_units": bfs_units, "ppr_units": ppr_units,
-                   "ppr_iterations": ppr_iters, "bfs_iterations": st.bfs_iterations,
-                   "piece_edges": piece,
-                   "l2": "inputs larger than L2 (union CSR+CSC and [V][16] rank arrays)"},
-        "e2e": {"value": round(units / (ms_e2e * 1e-3) / 1e9, 4), "unit": "GTEPS",
-                "ms_per_step": round(ms_e2e, 3),
-                "h2d_bytes_per_step": int(srcs.nbytes + V * 4),
-                "d2h_bytes_per_step": int(V * L * 8)},
-        "gpu_launches": st.kernel_launches * args.steps,
-        "graph_launches_per_step": st.graph_launches,
-        "split": {"bfs_ms": round(ms_bfs, 3), "ppr_ms": round(ms_ppr, 3),
-                  "bfs_gteps": round(bfs_units / (ms_bfs * 1e-3) / 1e9, 4),
-                  "ppr_gteps": round(ppr_units / (ms_ppr * 1e-3) / 1e9, 4)},
-        "plain_sequential": {
-            "bfs_ms": round(ms_plain_bfs, 3), "ppr_ms": round(ms_plain_ppr, 3),
-            "ppr_iterations_total": plain_ppr_iters[0],
-            "bfs_speedup_of_batch": round(ms_plain_bfs / ms_bfs, 3),
-            "ppr_speedup_of_batch": round(ms_plain_ppr / ms_ppr, 3),
-            "total_speedup_of_batch": round((ms_plain_bfs + ms_plain_ppr) / ms, 3)},
-        "roofline": {"kernel": "PPR iteration (k_ppr_pieces + k_ppr_fix + k_ppr_finish)",
-                     "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": PPR_TRAFFIC_64 if G == BATCH_GRAPHS else None,
-                     "traffic_note": "DRAM bytes per iteration; the [V][16] contribution "
-                                     "gathers are mostly L2 hits",
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": int(ppr_bytes),
-                     "avg_launch_ms": round(ms_iter, 4)},
-        "clocks": clocks,
-    }
-
-
-# ---------------------------------------------------------------------------
-# precision-form PageRank: R-MAT scale 24, directed
-# ---------------------------------------------------------------------------
-PR_SCALE, PR_SEED = 24, 4
-# DRAM bytes (read + write) of one iteration's gather at scale 24 (k_pr_merge
-# 1.477 + 0.154 GB, k_pr_merge_fix 0.016 GB), from one full ncu capture:
-#   GAS_HOST_LOOP=1 ncu --set full --clock-control none -k regex:k_pr_merge -s 6 -c 2 \
-#     python bench.py --workload pagerank --launch-list
-PR_TRAFFIC = {24: 1.647e9}
-PR_METRIC = "GTEPS (precision PageRank, R-MAT scale {scale} directed, E x iterations / time)"
-
-
-def run_pagerank(args):
-    import torch
-
-    import graphreduce_gb300 as gg
-    from graphreduce_gb300.engine import initial_vertex_data
-    from graphreduce_gb300.graph import EdgeList
-    from graphreduce_gb300.learn import DATA, MLP
-
-    stream = torch.cuda.current_stream()
-    sp = stream.cuda_stream
-    scale = args.pr_scale
-    t = time.time()
-    el = EdgeList.rmat(scale, EDGE_FACTOR, *RMAT_ABC, seed=PR_SEED, symmetrize=False)
-    log(f"pagerank workload: scale {scale}: V={el.nV} E={el.nE}, generated in "
-        f"{time.time() - t:.1f}s")
-    e = gg.GASEngineGPU("pagerank")
-    e.setGraph(el.nV, initial_vertex_data("pagerank", el.nV, 0, el.out_degree()), el.nE,
-               None, el.src, el.dst, sp)
-    warm_model = MLP.load(DATA / "warm_start_head.npz")
-    ranks_d = torch.empty(el.nV, dtype=torch.float32, device="cuda")
-    init_d = torch.empty(el.nV, dtype=torch.float32, device="cuda")
-
-    def timed(fn, steps, warmup):
-        for _ in range(warmup):
-            fn()
-        torch.cuda.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        z = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(steps):
-            fn()
-        z.record(stream)
-        torch.cuda.synchronize()
-        return a.elapsed_time(z) / steps
-
-    out = {}
-
-    def uniform():
-        out["u"] = e.pagerank_precision(0.85, 1e-6, 1000, ranks_d.data_ptr(), sp)[1]
-
-    if args.launch_list:
-        # one uniform-start run and nothing else (for an ncu launch list)
-        uniform()
-        torch.cuda.synchronize()
-        return {"launch_list": True, "iterations": out["u"].iterations}
-
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        ms = timed(uniform, args.steps, args.warmup)
-    clocks = clk.summary()
-    st_u = out["u"]
-    r_uni = ranks_d.cpu().numpy()
-
-    def warm():  # the head's proposal, then the same iteration from it
-        e.pagerank_warm_start(warm_model, 0.85, init_d.data_ptr())
-        out["w"] = e.pagerank_precision_from(init_d.data_ptr(), 0.85, 1e-6, 1000, sp,
-                                             out=ranks_d.data_ptr())[1]
-
-    ms_warm = timed(warm, args.steps, 1)
-    st_w = out["w"]
-    r_warm = ranks_d.cpu().numpy()
-    # roofline: one profiled run (events around every iteration's slab pass)
-    e.set_profiling(True)
-    e.profile(reset=True)
-    e.pagerank_precision(0.85, 1e-6, 1000, ranks_d.data_ptr(), sp)
-    prof = e.profile()
-    e.set_profiling(False)
-    peak, peak_kind = measured_peaks()
-    achieved = prof.pagerank_bytes / (prof.pagerank_ms * 1e-3) / 1e9 if prof.pagerank_ms else 0
-    units = el.nE * st_u.iterations
-    res = {
-        "metric": PR_METRIC.format(scale=scale), "value": round(units / (ms * 1e-3) / 1e9, 4), "unit": "GTEPS",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (two-sum compensated gather) + f64 residual",
-        "data": "synthetic (seeded R-MAT)",
-        "config": {"workload": f"precision PageRank, R-MAT scale {scale}, edge factor "
-                               f"{EDGE_FACTOR}, directed, seed {PR_SEED}, d=0.85, L1 tol 1e-6",
-                   "V": el.nV, "E": el.nE, "iterations": st_u.iterations,
-                   "residual": st_u.residual,
-                   "l2": "inputs larger than L2"},
-        "warm_start": {"iterations": st_w.iterations, "ms": round(ms_warm, 3),
-                       "speedup": round(ms / ms_warm, 4),
-                       "l1_between_results": float(np.abs(r_uni.astype(np.float64) -
-                                                          r_warm).sum())},
-        "roofline": {"kernel": "k_pr_merge + k_pr_merge_fix (one PageRank iteration's gather)",
-                     "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": PR_TRAFFIC.get(scale),
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": int(prof.pagerank_bytes /
-                                                         max(1, prof.pagerank_launches)),
-                     "avg_launch_ms": round(prof.pagerank_ms / max(1, prof.pagerank_launches), 4)},
-        "clocks": clocks,
-    }
-    if args.pr_check:
-        import oracle
-        t = time.time()
-        r64, it64, _ = oracle.pagerank_fp64(el.nV, el.src, el.dst, 0.85, 1e-6)
-        d = np.abs(r_uni.astype(np.float64) - r64)
-        res["error_vs_fp64_oracle"] = {"l1": float(d.sum()), "max_abs": float(d.max()),
-                                       "oracle_iterations": it64,
-                                       "oracle_seconds": round(time.time() - t, 1)}
-    return res
-
-
-# ---------------------------------------------------------------------------
-# CPU baseline (the oracle, a C port of refgas.h)
-# ---------------------------------------------------------------------------
-def cpu_sssp_sample(ssp, sources, out_sssp, n_threads):
-    import oracle
-    from graphreduce_gb300.engine import SSSP_GATHER_ZERO
-    res = [None] * n_threads
-
-    def work(i):
-        t = time.perf_counter()
-        d, it = oracle.sssp(ssp.nV, ssp.src, ssp.dst, ssp.weights, int(sources[i]))
-        res[i] = (d, it, time.perf_counter() - t)
-
-    t0 = time.perf_counter()
-    th = [threading.Thread(target=work, args=(i,)) for i in range(n_threads)]
-    for x in th:
-        x.start()
-    for x in th:
-        x.join()
-    wall = time.perf_counter() - t0
-    ev = sum(edges_visited(out_sssp, r[0], SSSP_GATHER_ZERO) for r in res)
-    return ev / wall / 1e9, wall, res
-
-
 def run_reference(args):
-    import oracle  # noqa: F401  (the oracle port: the reference's refgas.h in C)
-    ssp, sources, _ = make_workload(args.scale)
-    out_sssp = ssp.out_degree()
-    cores = os.cpu_count() or 1
-    n = min(N_SOURCES, cores)
-    for _ in range(args.warmup):
-        cpu_sssp_sample(ssp, sources, out_sssp, n)
-    vals, walls = [], []
-    for _ in range(max(1, args.steps)):
-        v, w, _ = cpu_sssp_sample(ssp, sources, out_sssp, n)
-        vals.append(v)
-        walls.append(w)
-    value = statistics.median(vals)
-    sample = (f"SSSP from {n} of the {N_SOURCES} sources, one thread each, on the scale-"
-              f"{args.scale} graph (CC part of the step not sampled)")
-    return {"metric": METRIC.format(scale=args.scale), "value": round(value, 5), "unit": "GTEPS", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1e3 * statistics.median(walls), 1),
+    """The reference's CPU engine (refgas.h, as restated by the oracle port:
+    the reference's own build needs moderngpu and a GPU path it cannot have
+    here) on the headline step: the same graphs, weights, sources and runs
+    as our arm, built by the oracle's own generators so that the product
+    library is never loaded.  Each step is a bounded sample of the headline
+    step: one of its nine runs (SSSP from source k, k = 0..7, then CC) in
+    rotation, on every host thread; the value is the edges of all timed runs
+    over their total time, so K >= 9 steps cover the whole step."""
+    import oracle
+    n_threads = oracle_threads()
+    t = time.time()
+    nV, s, d = oracle.rmat(args.scale, EDGE_FACTOR, *RMAT_ABC, seed=GRAPH_SEED,
+                           symmetrize=True)
+    w = oracle.uniform_weights(s, d, 1, 64, WEIGHT_SEED)
+    sources = oracle.sample_sources(nV, s, d, N_SOURCES, SOURCE_SEED)
+    nVc, sc, dc = oracle.with_grid_islands(nV, s, d, N_ISLANDS, ISLAND_SIDE)
+    g = oracle.Graph(nV, s, d)
+    gc = oracle.Graph(nVc, sc, dc)
+    outdeg = np.bincount(s, minlength=nV)
+    log(f"reference arm: scale {args.scale}: V={nV} E={len(s)}; CC graph V={nVc} E={len(sc)}; "
+        f"inputs and graph builds {time.time() - t:.1f}s, {n_threads} threads")
+    runs = [("sssp", k) for k in range(N_SOURCES)] + [("cc", None)]
+
+    def one(i):
+        kind, k = runs[i % len(runs)]
+        t0 = time.perf_counter()
+        if kind == "sssp":
+            dist, _ = g.sssp(w, int(sources[k]))
+            sec = time.perf_counter() - t0
+            return sec, edges_visited(outdeg, dist, SSSP_UNREACHED)
+        gc.cc()
+        return time.perf_counter() - t0, len(sc)
+
+    for i in range(args.warmup):
+        one(i)
+    secs, units = [], 0
+    for i in range(max(1, args.steps)):
+        sec, u = one(i)
+        secs.append(sec)
+        units += u
+    g.close()
+    gc.close()
+    value = units / sum(secs) / 1e9
+    covered = sorted({runs[i % len(runs)][0] + ("" if runs[i % len(runs)][1] is None else
+                                                str(runs[i % len(runs)][1]))
+                      for i in range(max(1, args.steps))})
+    sample = (f"one run of the step per timed step, in rotation (SSSP from source 0..7, then "
+              f"CC), oracle port of refgas.h on {n_threads} threads; runs timed: "
+              f"{', '.join(covered)}")
+    return {"metric": METRIC.format(scale=args.scale), "value": round(value, 5), "unit": "GTEPS",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * sum(secs) / len(secs), 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32", "data": "synthetic", "impl": "reference",
             "config": config_dict(args.scale),
-            "cpu_baseline": {"value": round(value, 5), "unit": "GTEPS", "cores": n,
+            "cpu_baseline": {"value": round(value, 5), "unit": "GTEPS", "cores": n_threads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": round(value, 5), "unit": "GTEPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+
+
+# ---------------------------------------------------------------------------
+def run_configs(args, headline_outputs):
+    """The configuration entries of the one-GPU line (each leg frees its
+    graphs before the next)."""
+    from graphreduce_gb300.learn import DATA, MLP
+    want = set(args.configs.split(",")) if args.configs else set()
+    model = MLP.load(DATA / "schedule_head.npz")
+    out = {}
+    t0 = time.time()
+    if "c2" in want and headline_outputs is not None:
+        par, cpu = c2_oracle_check(headline_outputs)
+        out["c2_sssp_cc"] = par
+        out["_cpu_baseline"] = cpu
+        log(f"c2 oracle check {time.time() - t0:.1f}s")
+    if "c1" in want:
+        t = time.time()
+        out["c1_bfs"] = run_c1(args, model)
+        free_gpu()
+        log(f"c1 {time.time() - t:.1f}s")
+    pr_warm = None
+    if "c3" in want:
+        t = time.time()
+        r = run_pagerank(args, check=True)
+        pr_warm = r["warm_start"]
+        out["c3_pagerank"] = {k: r[k] for k in (
+            "value", "unit", "ms_per_step", "e2e", "config", "roofline", "warm_start",
+            "error_vs_fp64_oracle", "parity", "parity_detail")}
+        out["c3_pagerank"]["gteps"] = r["value"]
+        free_gpu()
+        log(f"c3 {time.time() - t:.1f}s")
+    if "c4" in want:
+        t = time.time()
+        out["c4_learned"] = run_c4(args, model, pr_warm)
+        free_gpu()
+        log(f"c4 {time.time() - t:.1f}s")
+    if "c5" in want:
+        t = time.time()
+        r = run_batched(args, check=True)
+        out["c5_batched"] = {k: r[k] for k in (
+            "value", "unit", "ms_per_step", "e2e", "config", "split", "plain_sequential",
+            "roofline", "graph_launches_per_step", "parity", "parity_detail")}
+        out["c5_batched"]["gteps"] = r["value"]
+        free_gpu()
+        log(f"c5 {time.time() - t:.1f}s")
+    return out
 
 
 def main():
@@ -1102,20 +1446,25 @@ def main():
     ap.add_argument("--scale", type=int, default=SCALE)
     ap.add_argument("--schedule", default="learned",
                     choices=["learned", "auto", "generic", "push", "pull", "ordered"])
+    ap.add_argument("--configs", default=",".join(ALL_CONFIGS),
+                    help="configuration entries added at one GPU (comma list of c1..c5)")
+    ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--edges", default="device", choices=["device", "host"],
                     help="edge arrays in HBM or in pinned host memory (NVLink-C2C)")
     ap.add_argument("--workload", default="sssp-cc",
-                    choices=["sssp-cc", "batched", "pagerank", "lanes24"])
+                    choices=["sssp-cc", "batched", "pagerank", "lanes24", "bfs16"])
     ap.add_argument("--pr-scale", type=int, default=PR_SCALE)
     ap.add_argument("--pr-check", action="store_true",
-                    help="compare with the FP64 oracle (single-threaded C, slow)")
+                    help="--workload pagerank: compare with the FP64 oracle")
     ap.add_argument("--batch-graphs", type=int, default=BATCH_GRAPHS)
     ap.add_argument("--sssp", default="batched", choices=["batched", "sequential"],
                     help="the 8 SSSP sources as lanes of one batched run, or one run each")
     ap.add_argument("--launch-list", action="store_true",
                     help="run one device-resident step only (profiling)")
     args = ap.parse_args()
+    if args.no_configs:
+        args.configs = ""
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1126,17 +1475,18 @@ def main():
         print(json.dumps(run_reference(args)), flush=True)
         return
 
-    if args.workload == "batched":
+    if args.workload != "sssp-cc":
         if rank == 0:
-            print(json.dumps(run_batched(args)), flush=True)
-        return
-    if args.workload == "pagerank":
-        if rank == 0:
-            print(json.dumps(run_pagerank(args)), flush=True)
-        return
-    if args.workload == "lanes24":
-        if rank == 0:
-            print(json.dumps(run_lanes24(args)), flush=True)
+            if args.workload == "batched":
+                r = run_batched(args, check=not args.launch_list)
+            elif args.workload == "pagerank":
+                r = run_pagerank(args, check=args.pr_check)
+            elif args.workload == "bfs16":
+                from graphreduce_gb300.learn import DATA, MLP
+                r = run_c1(args, MLP.load(DATA / "schedule_head.npz"))
+            else:
+                r = run_lanes24(args)
+            print(json.dumps(r), flush=True)
         return
 
     if world > 1:
@@ -1144,21 +1494,38 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    result, cpu_inputs = run_ours(args, rank, world)
-    if rank == 0:
-        if not args.no_cpu_baseline and cpu_inputs is not None:
-            ssp, sources, out_sssp, first_sssp = cpu_inputs
+    result, outputs = run_ours(args, rank, world)
+    if rank == 0 and outputs is not None:
+        if world == 1 and args.configs:
+            configs = run_configs(args, outputs)
+            cpu = configs.pop("_cpu_baseline", None)
+            if cpu is not None and not args.no_cpu_baseline:
+                result["cpu_baseline"] = cpu
+            if "c2_sssp_cc" in configs:
+                c2 = configs["c2_sssp_cc"]
+                c2.update({"gteps": result["value"], "e2e_gteps": result["e2e"]["value"],
+                           "roofline": result["roofline"],
+                           "plain_gteps": result["plain"]["value"],
+                           "plain_e2e_gteps": result["plain"]["e2e"]["value"]})
+                result["verified_against_oracle"] = c2["parity"]
+            result["configs"] = configs
+        elif not args.no_cpu_baseline:
+            # replicas: the oracle on lane 0 only, on rank 0
             import oracle
-            from graphreduce_gb300.engine import SSSP_GATHER_ZERO
+            n = oracle_threads()
+            ssp, s0 = outputs["ssp"], int(outputs["sources"][0])
+            g = oracle.Graph(ssp.nV, ssp.src, ssp.dst)
             t = time.perf_counter()
-            d, it = oracle.sssp(ssp.nV, ssp.src, ssp.dst, ssp.weights, int(sources[0]))
+            d, _ = g.sssp(ssp.weights, s0)
             sec = time.perf_counter() - t
-            ev = edges_visited(out_sssp, d, SSSP_GATHER_ZERO)
+            g.close()
+            ev = edges_visited(ssp.out_degree(), d, SSSP_UNREACHED)
             result["cpu_baseline"] = {
-                "value": round(ev / sec / 1e9, 5), "unit": "GTEPS", "cores": 1, "kind": "port",
-                "sample": f"SSSP from source {int(sources[0])} on the scale-{args.scale} graph, "
-                          f"oracle C port of refgas.h, 1 thread, {sec:.1f}s"}
-            result["verified_against_oracle"] = bool(np.array_equal(d, first_sssp))
+                "value": round(ev / sec / 1e9, 5), "unit": "GTEPS", "cores": n, "kind": "port",
+                "sample": f"SSSP from source {s0} on the scale-{args.scale} graph, oracle port "
+                          f"of refgas.h on {n} threads, {sec:.1f}s"}
+            result["verified_against_oracle"] = bool(np.array_equal(d, outputs["lanes"][:, 0]))
+    if rank == 0:
         print(json.dumps(result), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -77,13 +77,15 @@ def build(verbose: bool = False) -> Path:
 
 def build_oracle(with_reference: bool = True) -> None:
     """Builds oracle/_build/liboracle.so, and oracle/_ref/libref.so when the
-    reference sources are present (test infrastructure only)."""
+    environment names a reference checkout in REF_DIR (test infrastructure
+    only)."""
     oracle = ROOT / "oracle"
     res = subprocess.run(["make", "-s", "-C", str(oracle)], capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
-    ref_dir = Path(os.environ.get("REF_DIR", "/root/reference"))
-    if with_reference and (ref_dir / "refgas.h").exists():
+    ref = os.environ.get("REF_DIR", "")
+    ref_dir = Path(ref) if ref else None
+    if with_reference and ref_dir is not None and (ref_dir / "refgas.h").exists():
         res = subprocess.run(["make", "-s", "-C", str(oracle), "ref", f"REF_DIR={ref_dir}"],
                              capture_output=True, text=True)
         if res.returncode != 0:

@@ -758,6 +758,16 @@ gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
     return gas::fail(GAS_ERR_TOO_LARGE, "set_graph: V + E must stay below 2^31");
   if (e->prog == GAS_PROG_SSSP && nE > 0 && !edge_data)
     return gas::fail(GAS_ERR_INVALID, "SSSP needs edge weights");
+  if (e->prog == GAS_PROG_SSSP) {
+    // The SSSP Program's margin (sssp.cu:32-33): gatherZero = INT_MAX - 100000,
+    // so dist + w stays below INT_MAX only for weights up to 100000.
+    const int32_t *w = static_cast<const int32_t *>(edge_data);
+    for (int64_t i = 0; i < nE; ++i)
+      if (w[i] < 0 || w[i] > 100000)
+        return gas::fail(GAS_ERR_INVALID,
+                         "set_graph: SSSP weight %d of edge %lld outside [0, 100000]", w[i],
+                         (long long)i);
+  }
   free_graph(e);
   if (!e->h_cnt) {
     int dev = 0;

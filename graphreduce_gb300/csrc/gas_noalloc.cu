@@ -19,21 +19,29 @@
 // Limits and sharing:
 //   * nV + nE <= GAS_NOALLOC_MAX_ITEMS (2^29); larger graphs are rejected
 //     with GAS_ERR_TOO_LARGE before any work is issued;
-//   * the scratch array (kScratchBytes, about 6.3 MB) is resident on every
-//     device that loads this library, until the process exits;
+//   * the scratch array (kScratchBytes, about 6.3 MB) belongs to this
+//     file's module.  Under CUDA's lazy module loading (the default since
+//     CUDA 12.2) the module, and with it the array, is loaded on a device
+//     the first time this entry point runs there; that first call therefore
+//     does reserve the 6.3 MB.  A caller whose pool will own every byte of
+//     the device makes one call first (nV = nE = 0 with a device l1_out is
+//     enough), or runs with CUDA_MODULE_LOADING=EAGER, before the pool takes
+//     the device; from then on the array stays reserved until the process
+//     exits and calls allocate nothing;
 //   * every call shares it and it keeps the previous call's contents: each
 //     call rewrites every scratch word it reads (the per-CTA residual slots
 //     are cleared first), but two calls whose kernels overlap on the GPU --
 //     on different streams, or from different host threads -- race on it and
 //     give wrong results; serialise them on one stream;
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before capturing work into a CUDA graph.
+//   * every call looks up the array's device address (cudaGetSymbolAddress)
+//     with the calling thread's device current, so the address stays right
+//     after cudaDeviceReset reloads the module; make the first call on a
+//     device before capturing work into a CUDA graph, since that one loads
+//     the module.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
-#include <mutex>
 
 #include "gas.h"
 #include "gas_device.cuh"
@@ -72,28 +80,16 @@ static_assert(GAS_NOALLOC_MAX_ITEMS == kMaxTiles * kTile,
 // array: host code passes the address cudaGetSymbolAddress returns.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void *g_scratch_addr[kMaxDevices];
-
-// Device address of the scratch on the current device, looked up once.
+// Device address of the scratch on the calling thread's current device.
+// Looked up on every call (a table lookup once the module is loaded), so a
+// context that was reset and created again never sees a stale address.
 gas_status_t scratch_address(unsigned char **out) {
-  int dev = 0;
-  cudaError_t ce = cudaGetDevice(&dev);
-  if (ce != cudaSuccess)
-    return gas::fail(GAS_ERR_CUDA, "pagerank_step_noalloc: %s", cudaGetErrorString(ce));
-  if (dev < 0 || dev >= kMaxDevices)
-    return gas::fail(GAS_ERR_UNSUPPORTED, "pagerank_step_noalloc: device %d", dev);
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (ce != cudaSuccess || !p)
-      return gas::fail(GAS_ERR_CUDA, "pagerank_step_noalloc: scratch address: %s",
-                       cudaGetErrorString(ce));
-    g_scratch_addr[dev] = p;
-  }
-  *out = static_cast<unsigned char *>(g_scratch_addr[dev]);
+  void *p = nullptr;
+  const cudaError_t ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (ce != cudaSuccess || !p)
+    return gas::fail(GAS_ERR_CUDA, "pagerank_step_noalloc: scratch address: %s",
+                     cudaGetErrorString(ce));
+  *out = static_cast<unsigned char *>(p);
   return GAS_OK;
 }
 

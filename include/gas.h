@@ -171,7 +171,9 @@ void gas_engine_destroy(gas_engine *e);
  * data (nE records, may be NULL) to the device and builds CSC (gather) and
  * CSR (scatter) there from the edge list.  The host vertex array stays
  * registered as the destination of gas_engine_get_results.  May be called
- * again on the same engine (sssp.cu:85). */
+ * again on the same engine (sssp.cu:85).  The built-in SSSP needs int32
+ * weights in [0, 100000] (its gatherZero INT_MAX - 100000 leaves that
+ * margin, sssp.cu:32-33); others return GAS_ERR_INVALID. */
 gas_status_t gas_engine_set_graph(gas_engine *e, int32_t nV, void *vertex_data,
                                   int64_t nE, const void *edge_data,
                                   const int32_t *srcs, const int32_t *dsts,
@@ -277,12 +279,16 @@ gas_status_t gas_engine_pagerank_precision(gas_engine *e, double damping,
  * over a CSC graph in device memory (csc_off[nV+1], csc_src[nE]); *l1_out
  * (device) receives the FP64 residual sum_v |rank_out[v] - rank_in[v]|.
  * All pointers are caller-owned device memory; the kernels' scratch is a
- * fixed file-scope device array (about 6.3 MB, resident on every device that
- * loads the library), so no allocation happens.  Graphs with
- * nV + nE > GAS_NOALLOC_MAX_ITEMS return GAS_ERR_TOO_LARGE.  Every call
- * shares that array: calls whose kernels overlap on the GPU race, so issue
- * them on one stream.  The first call on a device looks the array up with
- * that device current; make it before capturing work into a CUDA graph. */
+ * fixed file-scope device array of about 6.3 MB.  CUDA loads it (lazy module
+ * loading, the default) on a device at the first call there, which is when
+ * those 6.3 MB are reserved: make one call first (nV = nE = 0 with a device
+ * l1_out will do), or set CUDA_MODULE_LOADING=EAGER, before a pool takes the
+ * device; later calls allocate nothing, and the array stays reserved until
+ * the process exits.  Graphs with nV + nE > GAS_NOALLOC_MAX_ITEMS return
+ * GAS_ERR_TOO_LARGE.  Every call shares that array: calls whose kernels
+ * overlap on the GPU race, so issue them on one stream.  Each call looks the
+ * array up with the calling thread's device current; make the first call on
+ * a device before capturing work into a CUDA graph. */
 #define GAS_NOALLOC_MAX_ITEMS (1LL << 29)
 gas_status_t gas_pagerank_step_noalloc(int32_t nV, int32_t nE,
                                        const int32_t *csc_off,

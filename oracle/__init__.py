@@ -66,6 +66,19 @@ def _oracle():
             lib.orc_sample_sources.argtypes = [c_i32, c_i64, c_vp, c_vp, c_i32, C.c_uint64,
                                                c_vp]
             lib.orc_sample_sources.restype = C.c_int
+            lib.orc_graph_new.argtypes = [c_i32, c_i64, c_vp, c_vp]
+            lib.orc_graph_new.restype = c_vp
+            lib.orc_graph_delete.argtypes = [c_vp]
+            lib.orc_graph_delete.restype = None
+            lib.orc_g_bfs.argtypes = [c_vp, c_i32, c_vp]
+            lib.orc_g_sssp.argtypes = [c_vp, c_vp, c_i32, c_vp]
+            lib.orc_g_cc.argtypes = [c_vp, c_vp]
+            lib.orc_g_pagerank.argtypes = [c_vp, c_vp]
+            lib.orc_g_pagerank_fp64.argtypes = [c_vp, c_dbl, c_dbl, c_i64, c_vp, c_vp]
+            lib.orc_g_ppr_fp64.argtypes = [c_vp, c_i32, c_dbl, c_dbl, c_i64, c_vp, c_vp]
+            for f in ("orc_g_bfs", "orc_g_sssp", "orc_g_cc", "orc_g_pagerank",
+                      "orc_g_pagerank_fp64", "orc_g_ppr_fp64"):
+                getattr(lib, f).restype = c_i64
             _orc = lib
     return _orc
 
@@ -137,6 +150,63 @@ def _check(it: int, what: str) -> int:
     if it < 0:
         raise RuntimeError(f"oracle {what} failed with code {it}")
     return int(it)
+
+
+class Graph:
+    """The oracle engine's CSC + CSR of one edge list, built once
+    (refgas.h:81-113) and shared by any number of runs."""
+
+    def __init__(self, nV, src, dst):
+        s, d = _i32(src), _i32(dst)
+        self.nV, self.nE = int(nV), int(s.shape[0])
+        self._h = _oracle().orc_graph_new(nV, s.shape[0], s.ctypes.data, d.ctypes.data)
+        if not self._h:
+            raise RuntimeError("oracle graph: bad edge list or out of memory")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _oracle().orc_graph_delete(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def bfs(self, source):
+        out = np.zeros(self.nV, np.int32)
+        return out, _check(_oracle().orc_g_bfs(self._h, int(source), out.ctypes.data), "bfs")
+
+    def sssp(self, weights, source):
+        w = _i32(weights)
+        if w.shape[0] != self.nE:
+            raise ValueError("one weight per edge")
+        out = np.zeros(self.nV, np.int32)
+        return out, _check(_oracle().orc_g_sssp(self._h, w.ctypes.data, int(source),
+                                                out.ctypes.data), "sssp")
+
+    def cc(self):
+        out = np.zeros(self.nV, np.int32)
+        return out, _check(_oracle().orc_g_cc(self._h, out.ctypes.data), "cc")
+
+    def pagerank(self):
+        out = np.zeros(self.nV, np.float32)
+        return out, _check(_oracle().orc_g_pagerank(self._h, out.ctypes.data), "pagerank")
+
+    def pagerank_fp64(self, damping=0.85, tol=1e-6, max_iter=1000):
+        out = np.zeros(self.nV, np.float64)
+        l1 = C.c_double()
+        it = _oracle().orc_g_pagerank_fp64(self._h, damping, tol, max_iter, out.ctypes.data,
+                                           C.byref(l1))
+        return out, _check(it, "pagerank_fp64"), l1.value
+
+    def ppr_fp64(self, seed, damping=0.85, tol=1e-12, max_iter=10000):
+        out = np.zeros(self.nV, np.float64)
+        l1 = C.c_double()
+        it = _oracle().orc_g_ppr_fp64(self._h, int(seed), damping, tol, max_iter,
+                                      out.ctypes.data, C.byref(l1))
+        return out, _check(it, "ppr_fp64"), l1.value
 
 
 def bfs(nV, src, dst, source):

@@ -243,25 +243,41 @@ static inline int pr_apply(orc_pr_vertex *v, float g)
 #include "gas_oracle_engine.inc"
 
 /* ------------------------------------------------------------------------ */
-/* Drivers, each mirroring how the reference app runs the engine.           */
-/* All return the number of GAS iterations, or a negative error code.       */
+/* Drivers, each mirroring how the reference app runs the engine, on a      */
+/* graph built once (orc_graph_new; refgas.h:81-113) so that many runs can  */
+/* share it.  All return the number of GAS iterations, or a negative error  */
+/* code.  The orc_<program> entry points below build the graph per call.    */
 /* ------------------------------------------------------------------------ */
+
+ORC_EXPORT orc_graph *orc_graph_new(int32_t nV, int64_t nE, const int32_t *srcs,
+                                    const int32_t *dsts)
+{
+  orc_graph *g = (orc_graph *)malloc(sizeof(orc_graph));
+  if (!g) return NULL;
+  if (nV < 0 || nE < 0 || graph_init(g, nV, nE, srcs, dsts)) { free(g); return NULL; }
+  return g;
+}
+
+ORC_EXPORT void orc_graph_delete(orc_graph *g)
+{
+  if (!g) return;
+  graph_free(g);
+  free(g);
+}
+
+ORC_EXPORT int64_t orc_graph_num_edges(const orc_graph *g) { return g ? g->nE : -1; }
 
 /* bfs.cu:93-134: depth=-1, setActive(src,src+1), step loop with
  * gather(false)/apply/scatterActivate(false)/nextIter and ++level. */
-ORC_EXPORT int64_t orc_bfs(int32_t nV, int64_t nE, const int32_t *srcs,
-                           const int32_t *dsts, int32_t source,
-                           int32_t *depth)
+ORC_EXPORT int64_t orc_g_bfs(const orc_graph *g, int32_t source, int32_t *depth)
 {
-  orc_graph g;
   bfs_engine e;
   int64_t it = 0;
   int32_t v;
-  if (nV > 0 && (source < 0 || source >= nV)) return -1;
-  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
-  for (v = 0; v < nV; ++v) depth[v] = -1;
-  if (bfs_engine_init(&e, &g, depth, NULL)) { graph_free(&g); return -2; }
-  if (nV > 0) bfs_set_active(&e, source, source + 1);
+  if (g->nV > 0 && (source < 0 || source >= g->nV)) return -1;
+  for (v = 0; v < g->nV; ++v) depth[v] = -1;
+  if (bfs_engine_init(&e, g, depth, NULL)) return -2;
+  if (g->nV > 0) bfs_set_active(&e, source, source + 1);
   g_bfs_level = 0;
   while (bfs_count_active(&e)) {
     bfs_gather(&e);
@@ -271,26 +287,23 @@ ORC_EXPORT int64_t orc_bfs(int32_t nV, int64_t nE, const int32_t *srcs,
     g_bfs_level = (int32_t)(++it);
   }
   bfs_engine_free(&e);
-  graph_free(&g);
   return it;
 }
 
 /* sssp.cu:69-111 (one of its ten identical runs): dist = gatherZero except
- * the source, setActive(0,n), step loop with gather/apply/scatter/nextIter. */
-ORC_EXPORT int64_t orc_sssp(int32_t nV, int64_t nE, const int32_t *srcs,
-                            const int32_t *dsts, const int32_t *weights,
-                            int32_t source, int32_t *dist)
+ * the source, setActive(0,n), step loop with gather/apply/scatter/nextIter.
+ * weights: nE records in edge-list order. */
+ORC_EXPORT int64_t orc_g_sssp(const orc_graph *g, const int32_t *weights,
+                              int32_t source, int32_t *dist)
 {
-  orc_graph g;
   sssp_engine e;
   int64_t it = 0;
   int32_t v;
-  if (nV > 0 && (source < 0 || source >= nV)) return -1;
-  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
-  for (v = 0; v < nV; ++v) dist[v] = INT_MAX - 100000;
-  if (nV > 0) dist[source] = 0;
-  if (sssp_engine_init(&e, &g, dist, weights)) { graph_free(&g); return -2; }
-  sssp_set_active(&e, 0, nV);
+  if (g->nV > 0 && (source < 0 || source >= g->nV)) return -1;
+  for (v = 0; v < g->nV; ++v) dist[v] = INT_MAX - 100000;
+  if (g->nV > 0) dist[source] = 0;
+  if (sssp_engine_init(&e, g, dist, weights)) return -2;
+  sssp_set_active(&e, 0, g->nV);
   while (sssp_count_active(&e)) {
     sssp_gather(&e);
     sssp_apply_all(&e);
@@ -299,52 +312,43 @@ ORC_EXPORT int64_t orc_sssp(int32_t nV, int64_t nE, const int32_t *srcs,
     ++it;
   }
   sssp_engine_free(&e);
-  graph_free(&g);
   return it;
 }
 
 /* connected_component.cu:66-81 and 386-389: label = id, setActive(0,n), run(). */
-ORC_EXPORT int64_t orc_cc(int32_t nV, int64_t nE, const int32_t *srcs,
-                          const int32_t *dsts, int32_t *label)
+ORC_EXPORT int64_t orc_g_cc(const orc_graph *g, int32_t *label)
 {
-  orc_graph g;
   cc_engine e;
   int64_t it;
   int32_t v;
-  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
-  for (v = 0; v < nV; ++v) label[v] = v;
-  if (cc_engine_init(&e, &g, label, NULL)) { graph_free(&g); return -2; }
-  cc_set_active(&e, 0, nV);
+  for (v = 0; v < g->nV; ++v) label[v] = v;
+  if (cc_engine_init(&e, g, label, NULL)) return -2;
+  cc_set_active(&e, 0, g->nV);
   it = cc_run(&e);
   cc_engine_free(&e);
-  graph_free(&g);
   return it;
 }
 
 /* pagerank.cu:85-101 and 374-382: rank = 0.15, numOutEdges = out-degree,
  * setActive(0,n), run().  rank[] receives the final ranks. */
-ORC_EXPORT int64_t orc_pagerank(int32_t nV, int64_t nE, const int32_t *srcs,
-                                const int32_t *dsts, float *rank)
+ORC_EXPORT int64_t orc_g_pagerank(const orc_graph *g, float *rank)
 {
-  orc_graph g;
   pr_engine e;
   orc_pr_vertex *vd;
   int64_t it;
   int32_t v;
-  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
-  vd = (orc_pr_vertex *)malloc(sizeof(orc_pr_vertex) * (size_t)(nV > 0 ? nV : 1));
-  if (!vd) { graph_free(&g); return -2; }
-  for (v = 0; v < nV; ++v) {
+  vd = (orc_pr_vertex *)malloc(sizeof(orc_pr_vertex) * (size_t)(g->nV > 0 ? g->nV : 1));
+  if (!vd) return -2;
+  for (v = 0; v < g->nV; ++v) {
     vd[v].rank = 0.15f;
-    vd[v].numOutEdges = (int32_t)(g.csr_off[v + 1] - g.csr_off[v]);
+    vd[v].numOutEdges = (int32_t)(g->csr_off[v + 1] - g->csr_off[v]);
   }
-  if (pr_engine_init(&e, &g, vd, NULL)) { free(vd); graph_free(&g); return -2; }
-  pr_set_active(&e, 0, nV);
+  if (pr_engine_init(&e, g, vd, NULL)) { free(vd); return -2; }
+  pr_set_active(&e, 0, g->nV);
   it = pr_run(&e);
-  for (v = 0; v < nV; ++v) rank[v] = vd[v].rank;
+  for (v = 0; v < g->nV; ++v) rank[v] = vd[v].rank;
   pr_engine_free(&e);
   free(vd);
-  graph_free(&g);
   return it;
 }
 
@@ -389,83 +393,121 @@ static double fp64_step(const orc_graph *g, double damping, int32_t seed,
   return l1;
 }
 
+/* Power iteration from r0 until the first step whose L1 residual <= tol;
+ * -3 after max_iter steps.  seed < 0: precision-form PageRank from 1/N;
+ * otherwise personalized PageRank of that seed from e_seed. */
+static int64_t fp64_iterate(const orc_graph *g, int32_t seed, double damping,
+                            double tol, int64_t max_iter, double *rank,
+                            double *l1_out)
+{
+  const int32_t nV = g->nV;
+  double *r, *rn, *contrib;
+  int64_t it = 0;
+  int32_t v;
+  double l1 = 0.0;
+  if (nV <= 0) { if (l1_out) *l1_out = 0.0; return seed < 0 ? 0 : -1; }
+  if (seed >= nV) return -1;
+  r = (double *)malloc(sizeof(double) * (size_t)nV);
+  rn = (double *)malloc(sizeof(double) * (size_t)nV);
+  contrib = (double *)malloc(sizeof(double) * (size_t)nV);
+  if (!r || !rn || !contrib) { free(r); free(rn); free(contrib); return -2; }
+  for (v = 0; v < nV; ++v)
+    r[v] = seed < 0 ? 1.0 / (double)nV : (v == seed ? 1.0 : 0.0);
+  for (;;) {
+    if (it >= max_iter) { it = -3; break; }
+    l1 = fp64_step(g, damping, seed, r, rn, contrib);
+    if (l1 < 0) { it = -2; break; }
+    { double *t = r; r = rn; rn = t; }
+    ++it;
+    if (l1 <= tol) break;
+  }
+  for (v = 0; v < nV; ++v) rank[v] = r[v];
+  if (l1_out) *l1_out = l1;
+  free(r); free(rn); free(contrib);
+  return it;
+}
+
 /* Precision-form PageRank in FP64: r0 = 1/N; every vertex active every
  * iteration; r'_v = (1-d)/N + d * sum_{u->v} r_u / outdeg(u) (no dangling
  * redistribution); stop after the first iteration whose L1 residual
  * sum |r' - r| <= tol, or fail with -3 after max_iter iterations.
  * Returns iterations; *l1_out = last residual. */
+ORC_EXPORT int64_t orc_g_pagerank_fp64(const orc_graph *g, double damping,
+                                       double tol, int64_t max_iter,
+                                       double *rank, double *l1_out)
+{
+  return fp64_iterate(g, -1, damping, tol, max_iter, rank, l1_out);
+}
+
+/* Personalized PageRank in FP64 (no reference counterpart; the formula of
+ * orc_g_pagerank_fp64 with the teleport term on one seed): r0 = e_seed;
+ * r'_v = (1-d) [v == seed] + d * sum_{u->v} r_u / outdeg(u); stop after the
+ * first iteration whose L1 residual <= tol, or fail with -3 after max_iter
+ * iterations.  Returns iterations; *l1_out = last residual. */
+ORC_EXPORT int64_t orc_g_ppr_fp64(const orc_graph *g, int32_t seed,
+                                  double damping, double tol, int64_t max_iter,
+                                  double *rank, double *l1_out)
+{
+  if (seed < 0) return -1;
+  return fp64_iterate(g, seed, damping, tol, max_iter, rank, l1_out);
+}
+
+/* The same drivers on an edge list (graph built and freed per call). */
+#define ORC_ON_EDGES(call)                                      \
+  do {                                                          \
+    orc_graph *g_ = orc_graph_new(nV, nE, srcs, dsts);          \
+    int64_t r_;                                                 \
+    if (!g_) return -2;                                         \
+    r_ = (call);                                                \
+    orc_graph_delete(g_);                                       \
+    return r_;                                                  \
+  } while (0)
+
+ORC_EXPORT int64_t orc_bfs(int32_t nV, int64_t nE, const int32_t *srcs,
+                           const int32_t *dsts, int32_t source,
+                           int32_t *depth)
+{
+  if (nV > 0 && (source < 0 || source >= nV)) return -1;
+  ORC_ON_EDGES(orc_g_bfs(g_, source, depth));
+}
+
+ORC_EXPORT int64_t orc_sssp(int32_t nV, int64_t nE, const int32_t *srcs,
+                            const int32_t *dsts, const int32_t *weights,
+                            int32_t source, int32_t *dist)
+{
+  if (nV > 0 && (source < 0 || source >= nV)) return -1;
+  ORC_ON_EDGES(orc_g_sssp(g_, weights, source, dist));
+}
+
+ORC_EXPORT int64_t orc_cc(int32_t nV, int64_t nE, const int32_t *srcs,
+                          const int32_t *dsts, int32_t *label)
+{
+  ORC_ON_EDGES(orc_g_cc(g_, label));
+}
+
+ORC_EXPORT int64_t orc_pagerank(int32_t nV, int64_t nE, const int32_t *srcs,
+                                const int32_t *dsts, float *rank)
+{
+  ORC_ON_EDGES(orc_g_pagerank(g_, rank));
+}
+
 ORC_EXPORT int64_t orc_pagerank_fp64(int32_t nV, int64_t nE,
                                      const int32_t *srcs, const int32_t *dsts,
                                      double damping, double tol,
                                      int64_t max_iter, double *rank,
                                      double *l1_out)
 {
-  orc_graph g;
-  double *r, *rn, *contrib;
-  int64_t it = 0;
-  int32_t v;
-  double l1 = 0.0;
   if (nV <= 0) { if (l1_out) *l1_out = 0.0; return 0; }
-  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
-  r = (double *)malloc(sizeof(double) * (size_t)nV);
-  rn = (double *)malloc(sizeof(double) * (size_t)nV);
-  contrib = (double *)malloc(sizeof(double) * (size_t)nV);
-  if (!r || !rn || !contrib) {
-    free(r); free(rn); free(contrib); graph_free(&g); return -2;
-  }
-  for (v = 0; v < nV; ++v) r[v] = 1.0 / (double)nV;
-  for (;;) {
-    if (it >= max_iter) { it = -3; break; }
-    l1 = fp64_step(&g, damping, -1, r, rn, contrib);
-    if (l1 < 0) { it = -2; break; }
-    { double *t = r; r = rn; rn = t; }
-    ++it;
-    if (l1 <= tol) break;
-  }
-  for (v = 0; v < nV; ++v) rank[v] = r[v];
-  if (l1_out) *l1_out = l1;
-  free(r); free(rn); free(contrib);
-  graph_free(&g);
-  return it;
+  ORC_ON_EDGES(orc_g_pagerank_fp64(g_, damping, tol, max_iter, rank, l1_out));
 }
 
-/* Personalized PageRank in FP64 (no reference counterpart; the formula of
- * orc_pagerank_fp64 with the teleport term on one seed): r0 = e_seed;
- * r'_v = (1-d) [v == seed] + d * sum_{u->v} r_u / outdeg(u); stop after the
- * first iteration whose L1 residual <= tol, or fail with -3 after max_iter
- * iterations.  Returns iterations; *l1_out = last residual. */
 ORC_EXPORT int64_t orc_ppr_fp64(int32_t nV, int64_t nE, const int32_t *srcs,
                                 const int32_t *dsts, int32_t seed, double damping,
                                 double tol, int64_t max_iter, double *rank,
                                 double *l1_out)
 {
-  orc_graph g;
-  double *r, *rn, *contrib;
-  int64_t it = 0;
-  int32_t v;
-  double l1 = 0.0;
   if (nV <= 0 || seed < 0 || seed >= nV) return -1;
-  if (graph_init(&g, nV, nE, srcs, dsts)) return -2;
-  r = (double *)malloc(sizeof(double) * (size_t)nV);
-  rn = (double *)malloc(sizeof(double) * (size_t)nV);
-  contrib = (double *)malloc(sizeof(double) * (size_t)nV);
-  if (!r || !rn || !contrib) {
-    free(r); free(rn); free(contrib); graph_free(&g); return -2;
-  }
-  for (v = 0; v < nV; ++v) r[v] = v == seed ? 1.0 : 0.0;
-  for (;;) {
-    if (it >= max_iter) { it = -3; break; }
-    l1 = fp64_step(&g, damping, seed, r, rn, contrib);
-    if (l1 < 0) { it = -2; break; }
-    { double *t = r; r = rn; rn = t; }
-    ++it;
-    if (l1 <= tol) break;
-  }
-  for (v = 0; v < nV; ++v) rank[v] = r[v];
-  if (l1_out) *l1_out = l1;
-  free(r); free(rn); free(contrib);
-  graph_free(&g);
-  return it;
+  ORC_ON_EDGES(orc_g_ppr_fp64(g_, seed, damping, tol, max_iter, rank, l1_out));
 }
 
 /* One precision-form step on given ranks (FP64), for per-iteration checks

@@ -4,10 +4,10 @@ Runs the reference's own CPU engine GASEngineRef (refgas.h) and graph writer
 (graphio.cpp), compiled by `make -C oracle ref` into oracle/_ref/libref.so,
 on small hand-made and synthetic graphs, and stores inputs and outputs as
 compressed .npz files (plus one reference-written .gr file).  Needs the
-reference sources (REF_DIR, default /root/reference); the fixtures it writes
-are committed so that tests can run without them.
+reference sources (the REF_DIR environment variable names the checkout); the
+fixtures it writes are committed so that tests can run without them.
 
-    python tests/golden/make_golden.py
+    REF_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 

@@ -8,7 +8,7 @@ from pathlib import Path
 
 import pytest
 
-from conftest import REF_DIR, ROOT
+from conftest import HAVE_REF, REF_DIR, REF_SKIP, ROOT
 from graphreduce_gb300 import _lib
 
 
@@ -48,7 +48,7 @@ def test_engine_rejects_calls_out_of_order(libgas):
         g.GASEngineGPU("nope")
 
 
-@pytest.mark.skipif(not (REF_DIR / "bfs.cu").exists(), reason="reference sources absent")
+@pytest.mark.skipif(not HAVE_REF, reason=REF_SKIP)
 def test_reference_apps_compile_unchanged_against_gpugas_h(libgas, tmp_path):
     """bfs.cu, sssp.cu, pagerank.cu and connected_component.cu, byte for byte
     as the reference ships them, build against include/gpugas.h + libgas."""
@@ -73,3 +73,27 @@ def test_reference_apps_compile_unchanged_against_gpugas_h(libgas, tmp_path):
         run([nvcc, *arch, f"{app}.o", "util.o", "graphio.o", f"-L{libdir}", "-lgas",
              f"-Xlinker", f"-rpath={libdir}", "-lz", "-o", app])
         assert (tmp_path / app).exists()
+
+
+def test_sssp_weights_outside_the_programs_margin_are_rejected(libgas):
+    """sssp.cu:32-33 sets gatherZero = INT_MAX - 100000, so dist + w only
+    fits for weights in [0, 100000]: set_graph and the batch refuse others
+    before any device work."""
+    import numpy as np
+
+    import graphreduce_gb300 as g
+    from graphreduce_gb300.engine import initial_vertex_data
+    src = np.array([0, 1, 2], np.int32)
+    dst = np.array([1, 2, 0], np.int32)
+    for bad in (100001, -1, 2**31 - 1):
+        w = np.array([1, bad, 3], np.int32)
+        eng = g.GASEngineGPU("sssp")
+        with pytest.raises(g.GasError) as ei:
+            eng.setGraph(3, initial_vertex_data("sssp", 3, 0), 3, w, src, dst)
+        assert ei.value.status == 1 and "100000" in str(ei.value)
+        eng.close()
+        b = g.Batch()
+        with pytest.raises(g.GasError) as ei:
+            b.add_graph(3, src, dst, w)
+        assert ei.value.status == 1
+        b.close()

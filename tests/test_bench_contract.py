@@ -28,3 +28,22 @@ def test_reference_arm_json_line():
     assert cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "GTEPS", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_never_loads_the_product_library():
+    """The CPU arm builds its inputs with the oracle's own generators: after
+    a run, neither the package nor libgas.so is in the process."""
+    code = (
+        "import runpy, sys\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--scale', '11', '--steps', '9',"
+        " '--warmup', '0']\n"
+        "runpy.run_path('bench.py', run_name='__main__')\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert 'libgas' not in maps, 'libgas.so mapped'\n"
+        "assert not any(m.startswith('graphreduce_gb300') for m in sys.modules)\n"
+        "assert 'liboracle' in maps\n")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True,
+                         text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    assert "CC" in d["cpu_baseline"]["sample"] and "sssp7" in d["cpu_baseline"]["sample"]

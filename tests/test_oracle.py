@@ -174,3 +174,32 @@ def test_oracle_results_do_not_depend_on_thread_count():
         for a, b in zip(runs[0], other):
             for x, y in zip(a, b):
                 np.testing.assert_array_equal(x, y)
+
+
+def test_oracle_graph_handle_matches_per_call_runs():
+    nV, s, d = oracle.rmat(11, 16, seed=8, symmetrize=True)
+    w = oracle.uniform_weights(s, d, 1, 64, 3)
+    srcs = oracle.sample_sources(nV, s, d, 3, 8)
+    g = oracle.Graph(nV, s, d)
+    for x in srcs:
+        a, ia = g.sssp(w, x)
+        b, ib = oracle.sssp(nV, s, d, w, x)
+        assert ia == ib
+        np.testing.assert_array_equal(a, b)
+        a, ia = g.bfs(x)
+        b, ib = oracle.bfs(nV, s, d, x)
+        assert ia == ib
+        np.testing.assert_array_equal(a, b)
+    a, ia = g.cc()
+    b, ib = oracle.cc(nV, s, d)
+    assert ia == ib
+    np.testing.assert_array_equal(a, b)
+    a, ia, la = g.pagerank_fp64()
+    b, ib, lb = oracle.pagerank_fp64(nV, s, d)
+    assert ia == ib and la == lb
+    np.testing.assert_array_equal(a, b)
+    a, ia, _ = g.ppr_fp64(int(srcs[0]), tol=1e-10)
+    b, ib, _ = oracle.ppr_fp64(nV, s, d, int(srcs[0]), tol=1e-10)
+    assert ia == ib
+    np.testing.assert_array_equal(a, b)
+    g.close()
