@@ -49,7 +49,7 @@ P_f32 = C.POINTER(C.c_float)
 class RunStats(C.Structure):
     _fields_ = [("iterations", c_i32), ("push_iters", c_i32), ("pull_iters", c_i32),
                 ("kernel_launches", c_i32), ("edges_processed", c_i64),
-                ("residual", c_dbl)]
+                ("residual", c_dbl), ("graph_launches", c_i32), ("pad", c_i32)]
 
 
 class KernelProfile(C.Structure):
@@ -135,6 +135,8 @@ _SIGS = {
     "gas_engine_upload_vertex_data": ("status", [c_vp, c_vp, c_vp]),
     "gas_engine_download_vertex_data": ("status", [c_vp, c_vp, c_vp]),
     "gas_engine_run_schedule": ("status", [c_vp, c_i32, c_i32, C.POINTER(RunStats), c_vp]),
+    "gas_engine_run_user": ("status", [c_vp, c_vp, c_vp, c_i32, c_i32, C.POINTER(RunStats),
+                                       c_vp]),
     "gas_engine_pagerank_precision": ("status", [c_vp, c_dbl, c_dbl, c_i32, c_vp,
                                                  C.POINTER(RunStats), c_vp]),
     "gas_pagerank_step_noalloc": ("status", [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,

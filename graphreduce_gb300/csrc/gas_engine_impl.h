@@ -29,8 +29,8 @@
 // ---------------------------------------------------------------------------
 // Instantiated CUDA graphs cached per engine (valid until the next
 // set_graph, since their kernels capture the engine's buffers).
-enum { kGraphGeneric = 0, kGraphOrdered = 1, kGraphPagerank = 2,
-       kGraphFast0 = 3, kGraphSlots = 12 };
+enum { kGraphGeneric = 0, kGraphOrdered = 1, kGraphPagerank = 2, kGraphUser = 3,
+       kGraphFast0 = 4, kGraphSlots = 12 };
 
 struct gas_engine {
   gas_program_t prog = GAS_PROG_USER;
@@ -126,6 +126,10 @@ struct gas_engine {
   bool in_graph = false;             // loop kernels set a graph condition
   cudaGraphExec_t graphs[kGraphSlots] = {};
   bool level_from_counters = false;  // BFS level = counters.iteration
+  // what graphs[kGraphUser] was captured with (gas_engine_run_user)
+  gas_user_step_fn user_step = nullptr;
+  void *user_ctx = nullptr;
+  int32_t user_wrote_slots = -1;
 };
 
 namespace gas {

@@ -225,6 +225,88 @@ extern "C" gas_status_t gas_engine_run_schedule(gas_engine *e,
     // per iteration: gather tiles + fixup (or BFS apply), commit, 3 scan
     // passes, expand, 3 compaction passes, loop condition; plus the reset
     stats->kernel_launches = c.iteration * (e->prog == GAS_PROG_BFS ? 9 : 11) + 1;
+    stats->graph_launches = gas::host_loop_for(e) ? 0 : 1;
+  }
+  e->level = c.iteration;
+  e->active_full = false;
+  return gas::loop_status(e, c, stream);
+}
+
+// ---------------------------------------------------------------------------
+// run() of a user program: the Program-typed kernels come from the caller's
+// translation unit through a step callback; the rest of the iteration is
+// libgas's, and the loop is a WHILE node on the device.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct UserCtx {
+  gas_user_step_fn step;
+  void *ctx;
+  int32_t wrote_slots;
+};
+
+gas_status_t user_body(gas_engine *e, cudaStream_t cs, cudaGraphConditionalHandle h,
+                       void *ctx) {
+  const UserCtx *u = static_cast<const UserCtx *>(ctx);
+  GAS_TRY(u->step(u->ctx, cs));
+  CUDA_TRY(cudaGetLastError());
+  e->slots_pending = u->wrote_slots != 0;
+  GAS_TRY(gas::engine_scatter(e, cs));
+  k_loop_cond<<<1, 1, 0, cs>>>(e->cnt, h, e->in_graph ? 1 : 0);
+  CUDA_TRY(cudaGetLastError());
+  return GAS_OK;
+}
+
+}  // namespace
+
+extern "C" gas_status_t gas_engine_run_user(gas_engine *e, gas_user_step_fn step,
+                                            void *ctx, int32_t wrote_slots,
+                                            int32_t max_iterations, gas_run_stats *stats,
+                                            void *stream) {
+  if (!e || !step) return gas::fail(GAS_ERR_INVALID, "run_user: null argument");
+  if (!e->has_graph) return gas::fail(GAS_ERR_STATE, "run before set_graph");
+  if (e->prog != GAS_PROG_USER)
+    return gas::fail(GAS_ERR_UNSUPPORTED, "run_user: built-in programs use run_schedule");
+  if (max_iterations <= 0) max_iterations = 1000000;
+  if (stats) *stats = gas_run_stats{};
+  int32_t n = 0;
+  GAS_TRY(gas_engine_count_active(e, &n));
+  if (e->pending_gather || e->slots_pending)
+    return gas::fail(GAS_ERR_STATE, "run_user in the middle of a step");
+  if (n == 0) return GAS_OK;
+  UserCtx u{step, ctx, wrote_slots != 0 ? 1 : 0};
+  const bool direct = gas::host_loop_for(e);
+  if (direct) {
+    k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
+    CUDA_TRY(cudaGetLastError());
+    GAS_TRY(gas::run_host_loop(e, user_body, &u, stream));
+  } else {
+    if (e->graphs[kGraphUser] && (e->user_step != step || e->user_ctx != ctx ||
+                                  e->user_wrote_slots != u.wrote_slots)) {
+      cudaGraphExecDestroy(e->graphs[kGraphUser]);
+      e->graphs[kGraphUser] = nullptr;
+    }
+    if (!e->graphs[kGraphUser]) {
+      GAS_TRY(gas::build_while_graph(e, user_body, &u, &e->graphs[kGraphUser]));
+      e->user_step = step;
+      e->user_ctx = ctx;
+      e->user_wrote_slots = u.wrote_slots;
+    }
+    k_reset_loop<<<1, 1, 0, S(stream)>>>(e->cnt, max_iterations);
+    cudaError_t ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaGraphLaunch(e->graphs[kGraphUser], S(stream));
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(stream));
+    if (ce != cudaSuccess)
+      return gas::fail(GAS_ERR_CUDA, "user run: %s", cudaGetErrorString(ce));
+  }
+  gas_counters c;
+  GAS_TRY(gas_engine_read_counters(e, &c, stream));
+  if (stats) {
+    stats->iterations = c.iteration;
+    // per iteration: the caller's partition, tiles and fixup; commit, 3 scan
+    // passes, partition, expand, 3 compaction passes, loop condition; reset
+    stats->kernel_launches = 13 * c.iteration + 1;
+    stats->graph_launches = direct ? 0 : 1;
   }
   e->level = c.iteration;
   e->active_full = false;
@@ -796,6 +878,7 @@ gas_status_t pagerank_run(gas_engine *e, double damping, double tol, int32_t max
     stats->kernel_launches = 3 * cnt.iteration + 3;
     stats->edges_processed = (int64_t)cnt.iteration * e->nE;
     stats->residual = resid;
+    stats->graph_launches = host_loop ? 0 : 1;
   }
   if (!(resid <= tol))
     return gas::fail(GAS_ERR_ITER_CAP, "pagerank: residual %.3e after %d iterations",

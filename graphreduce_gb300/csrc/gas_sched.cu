@@ -1100,6 +1100,7 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
     const int per = e->prog == GAS_PROG_BFS ? 5 : 6;
     const int loop_iters = ctx.seeded ? c.iteration : (c.iteration > 0 ? c.iteration - 1 : 0);
     stats->kernel_launches = pro + per * loop_iters + 2;
+    stats->graph_launches = host_loop ? 0 : 1;
   }
   e->level = c.iteration;
   e->active_full = false;

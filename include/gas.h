@@ -247,6 +247,9 @@ typedef struct {
   int32_t kernel_launches; /* launches of libgas kernels in the run        */
   int64_t edges_processed; /* edges read by gather / expand kernels        */
   double residual;         /* PageRank: last L1 residual                   */
+  int32_t graph_launches;  /* CUDA-graph launches the run took: 1 for the  */
+                           /* device loop, 0 with direct launches          */
+  int32_t pad;
 } gas_run_stats;
 
 /* Runs the built-in program to convergence from the engine's current
@@ -589,6 +592,30 @@ gas_status_t gas_engine_prepare_scatter(gas_engine *e, const int32_t **csr_to_cs
 /* Host copy of the counters (synchronises the stream). */
 gas_status_t gas_engine_read_counters(gas_engine *e, gas_counters *out,
                                       void *stream);
+
+/* One iteration's Program-typed kernels of a user engine -- the gather with
+ * apply fused into its epilogue, or apply alone -- launched by the caller
+ * (include/gpugas.h) on `stream` with grids that do not depend on host-side
+ * counts: the call is captured into a CUDA graph, so the kernels must take
+ * every size from the device counters. */
+typedef gas_status_t (*gas_user_step_fn)(void *ctx, void *stream);
+
+/* run() (gpugas.h:1792-1807) for a user program with the loop on the
+ * device: one CUDA-graph launch whose WHILE node runs step(ctx) and then
+ * libgas's commit, scatter-activate and compaction kernels until the active
+ * set is empty, testing the condition on the device (no host round trip per
+ * iteration).  wrote_slots: step writes per-slot vertex data (gather fused
+ * with apply, committed after every gather of the iteration has read the
+ * old values) rather than updating it in place.  The graph is captured on
+ * the first call and reused while (step, ctx, wrote_slots) stay the same,
+ * until the next set_graph.  max_iterations <= 0 selects 1,000,000;
+ * reaching it returns GAS_ERR_ITER_CAP (the reference loops forever).
+ * stats (may be NULL) receives the iteration count run() prints and the
+ * launches.  Programs that run Program::scatter on the GPU keep the step
+ * loop (their scatter publishes edge data from the host side). */
+gas_status_t gas_engine_run_user(gas_engine *e, gas_user_step_fn step, void *ctx,
+                                 int32_t wrote_slots, int32_t max_iterations,
+                                 gas_run_stats *stats, void *stream);
 
 #ifdef __cplusplus
 }

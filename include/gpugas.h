@@ -58,6 +58,7 @@ class GASEngineGPU {
   bool m_haveGatherTmp;  // gather_tmp holds this iteration's gather results
   int m_gatherGrid;
   int m_applyGrid;
+  gas_run_stats m_lastRun;  // what the last run() did (not in the reference)
 
   void check(gas_status_t s, const char *file, int line) {
     if (s != GAS_OK) {
@@ -90,33 +91,52 @@ class GASEngineGPU {
 
   // The load-balanced gather over the current active list; with fuse, apply
   // runs in the epilogue and the new vertex data waits in per-slot storage
-  // until scatterActivate commits it.
-  void launchGather(bool fuse) {
-    gas_counters c;
-    GPUGAS_CHECK(gas_engine_read_counters(m_engine, &c, 0));
-    if (c.n_active == 0) return;
+  // until scatterActivate commits it.  With fixedGrids the launch reads no
+  // host-side count (every kernel loops over what the device counters say),
+  // so that it can be captured into run()'s device loop.
+  cudaError_t launchGatherOn(cudaStream_t stream, bool fuse, bool fixedGrids) {
+    typedef gasdev::TileShape<sizeof(GatherResult)> Shape;
+    long long tiles = 0;
+    if (!fixedGrids) {
+      gas_counters c;
+      GPUGAS_CHECK(gas_engine_read_counters(m_engine, &c, stream));
+      if (c.n_active == 0) return cudaSuccess;
+      const long long items = (long long)c.n_active + c.n_edges;
+      tiles = (items + Shape::kTile - 1) / Shape::kTile;
+    }
     const gasdev::SegSource src = gasdev::frontier_source(
         m_view.active, m_view.active_scan, m_view.csc_off,
         &m_view.counters->n_active, &m_view.counters->n_edges, m_view.tile_part);
-    typedef gasdev::TileShape<sizeof(GatherResult)> Shape;
-    const long long items = (long long)c.n_active + c.n_edges;
-    const long long tiles = (items + Shape::kTile - 1) / Shape::kTile;
-    const long long pblocks = (tiles + 1 + 255) / 256;
+    const long long pblocks = fixedGrids ? 2LL * m_view.num_sms : (tiles + 1 + 255) / 256;
     gasdev::k_partition<Shape::kTile, false>
-        <<<(int)(pblocks < 2 * m_view.num_sms ? pblocks : 2 * m_view.num_sms), 256>>>(
-            src, m_view.tile_part);
-    GPUGAS_CUDA(cudaGetLastError());
-    const int grid = (int)(tiles < m_gatherGrid ? tiles : m_gatherGrid);
-    gasdev::k_gather_tiles<Program><<<grid, gasdev::kNT>>>(
+        <<<(int)(pblocks < 2 * m_view.num_sms ? pblocks : 2 * m_view.num_sms), 256, 0,
+           stream>>>(src, m_view.tile_part);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    const int grid = fixedGrids ? m_gatherGrid
+                                : (int)(tiles < m_gatherGrid ? tiles : m_gatherGrid);
+    gasdev::k_gather_tiles<Program><<<grid, gasdev::kNT, 0, stream>>>(
         policy(fuse), src, static_cast<GatherResult *>(m_view.tile_first),
         static_cast<GatherResult *>(m_view.tile_carry), m_view.tile_a0);
-    GPUGAS_CUDA(cudaGetLastError());
-    const long long fix = (tiles + 7) / 8;
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    const long long fix = fixedGrids ? 32LL * m_view.num_sms : (tiles + 7) / 8;
     const int fgrid = (int)(fix < 4 * m_view.num_sms ? fix : 4 * m_view.num_sms);
-    gasdev::k_gather_fixup<Program><<<fgrid > 0 ? fgrid : 1, gasdev::kNT>>>(
+    gasdev::k_gather_fixup<Program><<<fgrid > 0 ? fgrid : 1, gasdev::kNT, 0, stream>>>(
         policy(fuse), src, static_cast<GatherResult *>(m_view.tile_first),
         static_cast<GatherResult *>(m_view.tile_carry), m_view.tile_a0);
-    GPUGAS_CUDA(cudaGetLastError());
+    return cudaGetLastError();
+  }
+
+  void launchGather(bool fuse) { GPUGAS_CUDA(launchGatherOn(0, fuse, false)); }
+
+  // run()'s loop body, Program-typed part: gather with apply fused, fixed
+  // grids, on the stream libgas is capturing.
+  static gas_status_t deviceLoopStep(void *self, void *stream) {
+    GASEngineGPU *me = static_cast<GASEngineGPU *>(self);
+    return me->launchGatherOn(static_cast<cudaStream_t>(stream), true, true) == cudaSuccess
+               ? GAS_OK
+               : GAS_ERR_CUDA;
   }
 
   void launchScatter() {
@@ -146,7 +166,7 @@ class GASEngineGPU {
  public:
   GASEngineGPU()
       : m_engine(0), m_haveGraph(false), m_pendingGather(false),
-        m_haveGatherTmp(false), m_gatherGrid(1), m_applyGrid(1) {
+        m_haveGatherTmp(false), m_gatherGrid(1), m_applyGrid(1), m_lastRun() {
     static_assert(sizeof(Int) == 4, "libgas indexes vertices and edges with 32 bits");
     GPUGAS_CHECK(gas_engine_create_user(sizeof(VertexData), sizeof(GatherResult),
                                         sizeof(EdgeData), &m_engine));
@@ -234,18 +254,36 @@ class GASEngineGPU {
     GPUGAS_CHECK(gas_engine_get_results(m_engine, 0));
   }
 
-  // gpugas.h:1792-1807
+  // gpugas.h:1792-1807: iterate until no vertex is active, then print the
+  // count.  The loop runs on the device -- one CUDA-graph launch whose WHILE
+  // node holds an iteration's kernels (this Program's gather with apply
+  // fused, then libgas's commit, scatter-activate and compaction) and tests
+  // the frontier there -- so no host round trip happens per iteration.
+  // Programs that run Program::scatter on the GPU take the step loop.
   void run() {
-    int i = 1;
-    while (countActive()) {
-      gather();
-      apply();
-      scatterActivate();
-      nextIter();
-      ++i;
+    if (gasdev::RunsScatter<Program>::value) {
+      m_lastRun = gas_run_stats();
+      int i = 1;
+      while (countActive()) {
+        gather();
+        apply();
+        scatterActivate();
+        nextIter();
+        ++i;
+      }
+      printf("Iterations: %d\n", i - 1);
+      return;
     }
-    printf("Iterations: %d\n", i - 1);
+    flushGather();
+    GPUGAS_CHECK(gas_engine_run_user(m_engine, &GASEngineGPU::deviceLoopStep, this, 1, 0,
+                                     &m_lastRun, 0));
+    m_haveGatherTmp = false;
+    printf("Iterations: %d\n", m_lastRun.iterations);
   }
+
+  // Not in the reference: iterations and launches of the last run() (all
+  // zero after a run() that took the step loop).
+  const gas_run_stats &lastRun() const { return m_lastRun; }
 
 #undef GPUGAS_CHECK
 #undef GPUGAS_CUDA

@@ -5,7 +5,8 @@
 //   gpugas_driver <in.bin> <out.bin>
 // in.bin : int32 nV, nE, source, then src[nE], dst[nE], w[nE]
 // out.bin: bfs depth[nV], iters; sssp dist[nV], iters; cc label[nV], iters;
-//          pagerank rank[nV] (float), iters
+//          pagerank rank[nV] (float), iters; graph launches of the CC and
+//          PageRank run() calls
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -147,21 +148,17 @@ int main(int argc, char **argv) {
     fwrite(vd.data(), 4, nV, o);
     fwrite(&it, 4, 1, o);
   }
+  int launches[2] = {-1, -1};  // graph launches of the two run() calls
   {  // connected_component.cu:66-81, through run()
     std::vector<int> vd(nV);
     for (int i = 0; i < nV; ++i) vd[i] = i;
     GASEngineGPU<TCC> engine;
     engine.setGraph(nV, vd.data(), nE, 0, src.data(), dst.data());
     engine.setActive(0, nV);
-    int it = 0;
-    while (engine.countActive()) {
-      engine.gather();
-      engine.apply();
-      engine.scatterActivate();
-      engine.nextIter();
-      ++it;
-    }
+    engine.run();
     engine.getResults();
+    const int it = engine.lastRun().iterations;
+    launches[0] = engine.lastRun().graph_launches;
     fwrite(vd.data(), 4, nV, o);
     fwrite(&it, 4, 1, o);
   }
@@ -181,9 +178,11 @@ int main(int argc, char **argv) {
     std::vector<float> r(nV);
     for (int i = 0; i < nV; ++i) r[i] = vd[i].rank;
     fwrite(r.data(), 4, nV, o);
-    int it = -1;
+    const int it = engine.lastRun().iterations;
+    launches[1] = engine.lastRun().graph_launches;
     fwrite(&it, 4, 1, o);
   }
+  fwrite(launches, 4, 2, o);
   fclose(o);
   return 0;
 }

@@ -15,7 +15,9 @@ from graphreduce_gb300 import _lib
 def declared_functions():
     text = (ROOT / "include" / "gas.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(gas_[a-z0-9_]+)\s*\(", text)))
+    # function names; a type name before "(" (a function-pointer typedef) is not one
+    return sorted({f for f in re.findall(r"\b(gas_[a-z0-9_]+)\s*\(", text)
+                   if not f.endswith("_t")})
 
 
 def test_library_exports_every_declared_symbol(libgas):

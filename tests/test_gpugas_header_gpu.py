@@ -27,8 +27,14 @@ def driver(libgas, tmp_path_factory):
     return out
 
 
+@pytest.mark.parametrize("host_loop", [False, True])
 @pytest.mark.parametrize("name", golden_names())
-def test_header_engine_matches_reference(driver, tmp_path, name):
+def test_header_engine_matches_reference(driver, tmp_path, name, host_loop):
+    """BFS and SSSP through the step API (as bfs.cu / sssp.cu drive it), CC
+    and PageRank through run() (connected_component.cu, pagerank.cu): run()
+    is one CUDA-graph launch with the loop on the device, or direct launches
+    with GAS_HOST_LOOP=1; both give the reference's results."""
+    import os
     g = load_golden(name)
     nV = int(g["nV"])
     fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
@@ -36,14 +42,26 @@ def test_header_engine_matches_reference(driver, tmp_path, name):
         np.array([nV, len(g["src"]), int(g["source"])], np.int32).tofile(f)
         for k in ("src", "dst", "w"):
             np.asarray(g[k], np.int32).tofile(f)
-    r = subprocess.run([str(driver), str(fin), str(fout)], capture_output=True, text=True)
+    env = dict(os.environ)
+    env.pop("GAS_HOST_LOOP", None)
+    if host_loop:
+        env["GAS_HOST_LOOP"] = "1"
+    r = subprocess.run([str(driver), str(fin), str(fout)], capture_output=True, text=True,
+                       env=env)
     assert r.returncode == 0, r.stdout + r.stderr
     raw = np.fromfile(fout, np.int32)
     parts = []
     for _ in range(4):
         parts.append((raw[:nV], raw[nV]))
         raw = raw[nV + 1:]
-    (bfs, bit), (sssp, sit), (cc, cit), (pr, _) = parts
+    launches = raw[:2]
+    (bfs, bit), (sssp, sit), (cc, cit), (pr, pit) = parts
+    # run() with an empty start set returns at once; otherwise one launch
+    want = 0 if host_loop else 1
+    assert launches[0] == (want if g["cc_iters"] > 0 else 0)
+    assert launches[1] == (want if g["pr_iters"] > 0 else 0)
+    assert pit == g["pr_iters"]
+    assert r.stdout.count("Iterations: ") == 2
     np.testing.assert_array_equal(bfs, g["bfs_depth"])
     assert bit == g["bfs_iters"]
     np.testing.assert_array_equal(sssp, g["sssp_dist"])
@@ -53,4 +71,3 @@ def test_header_engine_matches_reference(driver, tmp_path, name):
     prf = pr.view(np.float32)
     assert pr_histogram_ok(prf, g["pr_rank"])
     np.testing.assert_allclose(prf, g["pr_rank"], rtol=1e-5, atol=1e-5)
-    assert f"Iterations: " in r.stdout
