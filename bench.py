@@ -618,6 +618,46 @@ def kernel_roofline(e_s, e_c, bat, dev_s, dev_c, ssp, ccg, lane_src, dist_dev, s
 
 
 # ---------------------------------------------------------------------------
+# the drop-in path: user programs through include/gpugas.h
+# ---------------------------------------------------------------------------
+def _write_graph_bin(path, nV, src, dst, w, sources):
+    with open(path, "wb") as f:
+        np.array([nV, len(src), len(sources)], np.int32).tofile(f)
+        np.ascontiguousarray(src, np.int32).tofile(f)
+        np.ascontiguousarray(dst, np.int32).tofile(f)
+        (np.ones(len(src), np.int32) if w is None else np.ascontiguousarray(w, np.int32)).tofile(f)
+        np.ascontiguousarray(sources, np.int32).tofile(f)
+
+
+def user_program_path(el, sources, cc_el=None, reps=1):
+    """Runs graphreduce_gb300/_lib/bench_user_programs: the reference apps'
+    BFS, SSSP and CC programs written as user programs and compiled through
+    include/gpugas.h (BFS and SSSP driven through the step API like bfs.cu
+    and sssp.cu, CC through run(), one CUDA-graph launch).  Returns its
+    timings and outputs (BFS depths from sources[0], SSSP distances per
+    source, CC labels)."""
+    from graphreduce_gb300.build import OUT_DIR
+    exe = OUT_DIR / "bench_user_programs"
+    with tempfile.TemporaryDirectory() as d:
+        g = Path(d) / "g.bin"
+        _write_graph_bin(g, el.nV, el.src, el.dst, el.weights, sources)
+        cmd = [str(exe), str(g), str(reps), str(Path(d) / "out.bin")]
+        if cc_el is not None:
+            _write_graph_bin(Path(d) / "cc.bin", cc_el.nV, cc_el.src, cc_el.dst, None, [])
+            cmd.append(str(Path(d) / "cc.bin"))
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+        if r.returncode != 0:
+            raise RuntimeError(f"bench_user_programs failed ({r.returncode}): {r.stderr[-500:]}")
+        res = json.loads(r.stdout.strip().splitlines()[-1])
+        raw = np.fromfile(Path(d) / "out.bin", np.int32)
+    nV, k = el.nV, len(sources)
+    res["bfs_depth"] = raw[:nV]
+    res["sssp_dist"] = raw[nV:nV * (1 + k)].reshape(k, nV)
+    res["cc_label"] = raw[nV * (1 + k):]
+    return res
+
+
+# ---------------------------------------------------------------------------
 # C2 parity and the CPU baseline: the oracle on the whole step
 # ---------------------------------------------------------------------------
 def c2_oracle_check(out):
@@ -662,6 +702,30 @@ def c2_oracle_check(out):
                       f"port of refgas.h on {n_threads} threads, {run_s:.1f}s of runs "
                       f"(graph builds {build_s:.1f}s excluded)")}
     return parity, cpu
+
+
+def c2_user_programs(out):
+    """The headline step through the drop-in path: SSSP from the 8 sources
+    (sssp.cu's step loop, one run per source) and CC (connected_component.cu's
+    run()), as user programs compiled through include/gpugas.h; outputs
+    bit-exact with the built-in engine's (which the oracle checked)."""
+    ssp, ccg, sources = out["ssp"], out["ccg"], out["sources"]
+    up = user_program_path(ssp, sources, ccg, reps=1)
+    outdeg = ssp.out_degree()
+    sssp_units = sum(edges_visited(outdeg, up["sssp_dist"][k], SSSP_UNREACHED)
+                     for k in range(len(sources)))
+    ms_sssp = up["sssp_ms_per_source"] * len(sources)
+    ms = ms_sssp + up["cc_ms"]
+    same = all(np.array_equal(up["sssp_dist"][k], out["lanes"][:, k])
+               for k in range(len(sources))) and np.array_equal(up["cc_label"], out["cc_labels"])
+    return {"path": "user programs through include/gpugas.h: SSSP by the step API per source, "
+                    "CC by run() (one CUDA-graph launch)",
+            "ms_per_step": round(ms, 3), "gteps": gteps(sssp_units + ccg.nE, ms),
+            "sssp_ms_per_source": up["sssp_ms_per_source"], "sssp_iterations": up["sssp_iterations"],
+            "cc_ms": up["cc_ms"], "cc_iterations": up["cc_iterations"],
+            "cc_graph_launches": up["cc_graph_launches"],
+            "identical_to_builtin": bool(same) and up["sssp_iterations"] == out["iters"]["sssp"]
+            and up["cc_iterations"] == out["iters"]["cc"]}
 
 
 # ---------------------------------------------------------------------------
@@ -717,6 +781,13 @@ def run_c1(args, model):
     p = e.profile()
     e.set_profiling(False)
     e.close()
+    # the drop-in path: bfs.cu's BFS program and step loop through gpugas.h
+    up = user_program_path(el, [src], None, reps=max(1, min(args.steps, 5)))
+    user = {"path": "user program through include/gpugas.h, bfs.cu's step loop",
+            "ms": up["bfs_ms"], "gteps": gteps(units, up["bfs_ms"]),
+            "levels": up["bfs_levels"],
+            "identical_to_builtin": bool(np.array_equal(up["bfs_depth"], depth))
+            and up["bfs_levels"] == last["learned"].iterations}
     if p.push_ms >= p.pull_ms:
         roof = roofline("k_bfs_push (top-down levels)", "bfs_push", p.push_bytes, p.push_ms,
                         p.push_launches, "rmat-s16")
@@ -736,8 +807,9 @@ def run_c1(args, model):
         "fixed_schedules": {s: {"ms": round(times[s], 4), "gteps": gteps(units, times[s]),
                                 "identical_output": same[s]}
                             for s in ("push", "pull", "generic")},
+        "user_program": user,
         "parity": bool(np.array_equal(depth, ref)) and rit == last["learned"].iterations
-        and all(same.values()),
+        and all(same.values()) and user["identical_to_builtin"],
         "parity_detail": "depths and level count bit-exact against the oracle BFS",
         "roofline": roof,
     }
@@ -1404,6 +1476,9 @@ def run_configs(args, headline_outputs):
         out["c2_sssp_cc"] = par
         out["_cpu_baseline"] = cpu
         log(f"c2 oracle check {time.time() - t0:.1f}s")
+        t = time.time()
+        out["c2_sssp_cc"]["user_programs"] = c2_user_programs(headline_outputs)
+        log(f"c2 user programs {time.time() - t:.1f}s")
     if "c1" in want:
         t = time.time()
         out["c1_bfs"] = run_c1(args, model)

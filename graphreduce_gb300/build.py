@@ -30,6 +30,9 @@ NVCC_FLAGS = [
 ]
 SOURCES = ["gas_engine.cu", "gas_runs.cu", "gas_sched.cu", "gas_noalloc.cu", "gas_batch.cu", "gas_build.cu",
            "gas_learn.cu", "gas_host_graph.cpp"]
+# Programs built against libgas and include/gpugas.h: the drop-in path's
+# benchmark driver (bench.py runs it for the user-program figures).
+TOOLS = ["bench_user_programs.cu"]
 
 
 def nvcc() -> str:
@@ -70,6 +73,17 @@ def build(verbose: bool = False) -> Path:
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
         os.replace(tmp, LIB)
+    for tool in TOOLS:
+        src = CSRC / tool
+        exe = OUT_DIR / Path(tool).stem
+        deps = [src, LIB] + sorted(INCLUDE.glob("*.h")) + sorted(INCLUDE.glob("*.cuh"))
+        if exe.exists() and all(exe.stat().st_mtime >= d.stat().st_mtime for d in deps):
+            continue
+        cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", f"-I{INCLUDE}", str(src),
+               f"-L{OUT_DIR}", "-lgas", "-Xlinker", f"-rpath={OUT_DIR}", "-o", str(exe)]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {tool}:\n{res.stdout}\n{res.stderr}")
     if verbose:
         print(f"built {LIB}")
     return LIB
