@@ -76,9 +76,8 @@ MAX_ITERS = 20000  # far above any run of this workload; bounds a device loop
 ALL_CONFIGS = ("c1", "c2", "c3", "c4", "c5")
 
 # DRAM bytes (read + write) per launch of a dominant kernel, from ncu
-# captures recorded under profiles/ (each names its command).  Keys:
-# (kernel, workload).  Where only a smaller case was captured, the bytes are
-# scaled to the bench's launch by the edges processed (the profile says so).
+# captures recorded under profiles/ (each names its command and the bounded
+# form to use for a new capture).  Keys: (kernel, workload).
 DRAM_PER_LAUNCH = {
     # one-pass counters over the 11 batched-SSSP push launches of a scale-22
     # step (profiles/launches_sssp8-cc_rmat-s22_batched.md)
