@@ -787,14 +787,19 @@ def run_c1(args, model):
             "levels": up["bfs_levels"],
             "identical_to_builtin": bool(np.array_equal(up["bfs_depth"], depth))
             and up["bfs_levels"] == last["learned"].iterations}
-    if p.push_ms >= p.pull_ms:
+    if p.pull_launches == 0 and p.push_launches == 1:  # graphs of up to 2^18 vertices
+        roof = roofline("k_bfs_small (every level in one cooperative kernel)", "bfs_small",
+                        p.push_bytes, p.push_ms, 1, "rmat-s16",
+                        {"timed_with_byte_counting": True})
+    elif p.push_ms >= p.pull_ms:
         roof = roofline("k_bfs_push (top-down levels)", "bfs_push", p.push_bytes, p.push_ms,
                         p.push_launches, "rmat-s16")
     else:
         roof = roofline("k_bfs_pull (bottom-up levels)", "bfs_pull", p.pull_bytes, p.pull_ms,
                         p.pull_launches, "rmat-s16")
-    roof["note"] = ("65,536 vertices: the whole graph (7.6 MB) sits in L2 and each level is a "
-                    "few microseconds, so the run is bound by launch and loop latency")
+    roof["note"] = ("65,536 vertices: the whole graph (7.6 MB) sits in L2 and a level is a few "
+                    "microseconds of work, so the run is bound by latency (grid barriers, "
+                    "L2 round trips), not by DRAM bandwidth")
     return {
         "workload": f"BFS rmat-s{C1_SCALE}-ef{EDGE_FACTOR}-sym seed {C1_SEED}, source = first "
                     f"vertex of maximum out-degree ({src}, degree {deg})",

@@ -28,8 +28,8 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fPIC,-fopenmp,-fvisibility=default",
     f"-I{INCLUDE}", f"-I{CSRC}",
 ]
-SOURCES = ["gas_engine.cu", "gas_runs.cu", "gas_sched.cu", "gas_noalloc.cu", "gas_batch.cu", "gas_build.cu",
-           "gas_learn.cu", "gas_host_graph.cpp"]
+SOURCES = ["gas_engine.cu", "gas_runs.cu", "gas_sched.cu", "gas_small.cu", "gas_noalloc.cu",
+           "gas_batch.cu", "gas_build.cu", "gas_learn.cu", "gas_host_graph.cpp"]
 # Programs built against libgas and include/gpugas.h: the drop-in path's
 # benchmark driver (bench.py runs it for the user-program figures).
 TOOLS = ["bench_user_programs.cu"]

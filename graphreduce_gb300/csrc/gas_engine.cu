@@ -492,6 +492,7 @@ void free_graph(gas_engine *e) {
   for (int i = 0; i < 2; ++i) { dfree(e->pr_rank[i]); dfree(e->pr_contrib[i]); }
   dfree(e->pr_seed); dfree(e->pr_inv_deg); dfree(e->pr_l1); dfree(e->csr_to_csc);
   dfree(e->pr_tile_row); dfree(e->pr_head); dfree(e->pr_tail);
+  dfree(e->sb_bits); dfree(e->sb_ctl); dfree(e->sb_heavy);
   e->pr_tile_cap = 0;
   e->h_csr_perm.clear();
   e->h_csr_to_csc.clear();

@@ -29,6 +29,9 @@
 // ---------------------------------------------------------------------------
 // Instantiated CUDA graphs cached per engine (valid until the next
 // set_graph, since their kernels capture the engine's buffers).
+// BFS runs on graphs up to this many vertices take the one-kernel path.
+constexpr int kBfsSmallMaxV = 1 << 18;
+
 enum { kGraphGeneric = 0, kGraphOrdered = 1, kGraphPagerank = 2, kGraphUser = 3,
        kGraphFast0 = 4, kGraphSlots = 12 };
 
@@ -126,6 +129,11 @@ struct gas_engine {
   bool in_graph = false;             // loop kernels set a graph condition
   cudaGraphExec_t graphs[kGraphSlots] = {};
   bool level_from_counters = false;  // BFS level = counters.iteration
+  // small-graph BFS (gas_small.cu): three frontier bitmaps, the control
+  // word, the level's members with many out-edges
+  uint32_t *sb_bits = nullptr;
+  void *sb_ctl = nullptr;
+  int32_t *sb_heavy = nullptr;
   // what graphs[kGraphUser] was captured with (gas_engine_run_user)
   gas_user_step_fn user_step = nullptr;
   void *user_ctx = nullptr;

@@ -1030,6 +1030,8 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
   if (e->prog == GAS_PROG_BFS && schedule == GAS_SCHED_LEARNED) schedule = GAS_SCHED_AUTO;
   if (schedule == GAS_SCHED_LEARNED && !e->sched_model)
     return fail(GAS_ERR_STATE, "LEARNED schedule without a schedule model");
+  if (bfs_small_eligible(e, schedule))
+    return run_bfs_small(e, schedule, max_iterations, stats, stream);
   GAS_TRY(ensure_fast_buffers(e));
   FastCtx ctx;
   ctx.nW = (e->nV + 31) / 32;

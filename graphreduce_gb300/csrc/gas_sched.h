@@ -27,6 +27,12 @@ gas_status_t run_fast(gas_engine *e, gas_schedule_t schedule,
 
 bool host_loop_for(const gas_engine *e);
 
+// BFS on a graph of at most kBfsSmallMaxV vertices as one cooperative
+// kernel (gas_small.cu): same depths and iteration count as run_fast.
+bool bfs_small_eligible(const gas_engine *e, gas_schedule_t schedule);
+gas_status_t run_bfs_small(gas_engine *e, gas_schedule_t schedule, int32_t max_iterations,
+                           gas_run_stats *stats, void *stream);
+
 // The loop of build_while_graph as direct launches (GAS_HOST_LOOP=1).
 gas_status_t run_host_loop(
     gas_engine *e,

@@ -317,3 +317,65 @@ def test_profiling_mode_counts_kernels_and_keeps_results():
     ranks, pst = e2.pagerank_precision(0.85, 1e-6)
     pp = e2.profile()
     assert pp.pagerank_launches == pst.iterations and pp.pagerank_ms > 0
+
+
+def _bfs_run(el, schedule, start, end, small, cap=0):
+    import os
+    old = os.environ.get("GAS_BFS_SMALL")
+    os.environ["GAS_BFS_SMALL"] = "1" if small else "0"
+    try:
+        eng = GASEngineGPU("bfs")
+        vd = initial_vertex_data("bfs", el.nV)
+        eng.setGraph(el.nV, vd, el.nE, None, el.src, el.dst)
+        eng.setActive(start, end)
+        st = eng.run_schedule(schedule, max_iterations=cap or el.nV + 2)
+        eng.getResults()
+        eng.close()
+        return vd, st
+    finally:
+        if old is None:
+            os.environ.pop("GAS_BFS_SMALL", None)
+        else:
+            os.environ["GAS_BFS_SMALL"] = old
+
+
+@pytest.mark.parametrize("schedule", ["auto", "learned", "pull"])
+def test_small_graph_bfs_kernel_matches_oracle_and_fast_schedule(schedule):
+    """BFS on graphs up to 2^18 vertices runs as one cooperative kernel
+    (every level inside, a grid barrier between levels): depths and level
+    count equal the oracle's, and the iteration and direction counts equal
+    the multi-kernel fast schedule's (GAS_BFS_SMALL=0) -- from one source (a
+    hub, an ordinary vertex, one without out-edges) and from a range."""
+    graphs = [EdgeList.rmat(16, 16, seed=1),
+              EdgeList.rmat(14, 8, seed=3, symmetrize=False),
+              EdgeList.rmat(12, 16, seed=2).with_grid_islands(20, 9)]
+    for el in graphs:
+        hub, _ = el.max_out_degree_vertex()
+        od = el.out_degree()
+        sink = int(np.flatnonzero(od == 0)[0]) if (od == 0).any() else hub
+        ordinary = int(el.sample_sources(1, 4)[0])
+        for start, end in ((hub, hub + 1), (ordinary, ordinary + 1), (sink, sink + 1),
+                           (5, 40)):
+            a, sa = _bfs_run(el, schedule, start, end, True)
+            b, sb = _bfs_run(el, schedule, start, end, False)
+            np.testing.assert_array_equal(a, b)
+            assert (sa.iterations, sa.push_iters, sa.pull_iters) == \
+                (sb.iterations, sb.push_iters, sb.pull_iters)
+            if end == start + 1:
+                ref, rit = oracle.bfs(el.nV, el.src, el.dst, start)
+                np.testing.assert_array_equal(a, ref)
+                assert sa.iterations == rit
+
+
+def test_small_graph_bfs_kernel_iteration_cap():
+    """A run that needs more levels than the cap returns GAS_ERR_ITER_CAP;
+    the next run on a fresh engine is exact."""
+    el = EdgeList.rmat(12, 16, seed=2).with_grid_islands(4, 30)
+    s = el.nV - 1  # a grid corner: the run needs about 60 levels
+    with pytest.raises(GasError) as ei:
+        _bfs_run(el, "auto", s, s + 1, True, cap=5)
+    assert ei.value.status == 4
+    vd, st = _bfs_run(el, "auto", s, s + 1, True)
+    ref, rit = oracle.bfs(el.nV, el.src, el.dst, s)
+    np.testing.assert_array_equal(vd, ref)
+    assert st.iterations == rit
