@@ -36,67 +36,29 @@
 
 #include "gas.h"
 #include "gas_engine_impl.h"
+#include "gas_grid.cuh"
 #include "gas_internal.h"
 #include "gas_sched.h"
 
 namespace {
 
-constexpr int kSbNT = 1024;                   // one CTA per SM
-constexpr long long kSbMaxSpins = 1LL << 24;  // x 64 ns back-off: about a second
-constexpr int kSbPullDiv = 16;                // the fast schedule's BFS rule
-constexpr int kSbHeavy = 256;                 // out-edges of a member walked by the grid
+constexpr int kSbNT = 1024;     // one CTA per SM
+constexpr int kSbPullDiv = 16;  // the fast schedule's BFS rule
+constexpr int kSbHeavy = 256;   // out-edges of a member walked by the grid
+
+using gasgrid::warp_add;
 
 struct SmallCtl {
-  unsigned int bar_count;
-  unsigned int bar_gen;
-  int err;  // 1: a barrier wait gave up; 2: iteration cap
+  gasgrid::Barrier bar;  // bar.err: 1 a barrier wait gave up, 2 iteration cap
   int iterations;
   int n_push, n_pull;
+  int n_heavy[2];        // heavy members listed at a level (by level parity)
   long long f_edges[3];  // out-edges of the vertices found at a level
   long long bytes;       // algorithmic bytes (profiling)
-  int n_heavy[2];        // heavy members listed at a level (by level parity)
 };
 
-__device__ __forceinline__ bool sb_barrier(SmallCtl *c) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned int *gen = &c->bar_gen;
-    const unsigned int g = *gen;
-    __threadfence();
-    if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
-      c->bar_count = 0;
-      __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
-    } else {
-      long long spins = 0;
-      while (*gen == g) {
-        if (++spins > kSbMaxSpins) {
-          atomicExch(&c->err, 1);
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return *(volatile int *)&c->err == 0;
-}
-
-__device__ __forceinline__ long long warp_sum(long long v) {
-  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-  return v;
-}
-
-// Adds a per-thread count to *dst, one atomic per warp.
-__device__ __forceinline__ void warp_add(long long v, long long *dst) {
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0 && v)
-    atomicAdd((unsigned long long *)dst, (unsigned long long)v);
-}
-
 template <bool kCount>
-__global__ void __launch_bounds__(kSbNT)
+__global__ void __launch_bounds__(kSbNT, 1)
     k_bfs_small(const int32_t *__restrict__ csr_off, const int32_t *__restrict__ csr_dst,
                 const int32_t *__restrict__ csc_off, const int32_t *__restrict__ csc_src,
                 int32_t *depth, const int32_t *__restrict__ act, int n_act, uint32_t *bits,
@@ -117,14 +79,14 @@ __global__ void __launch_bounds__(kSbNT)
     }
   }
   warp_add(found, &c->f_edges[0]);
-  if (!sb_barrier(c)) return;
+  if (!gasgrid::barrier(&c->bar)) return;
   int it = 1;
   for (int k = 0;; ++k) {
     const int cur = k % 3, nxt = (k + 1) % 3, old = (k + 2) % 3;
     const long long fe = *(volatile long long *)&c->f_edges[cur];
     if (fe == 0) break;  // A_{k+1} = N(C_k) is empty
     if (it >= max_iter) {
-      if (tid == 0) atomicExch(&c->err, 2);
+      if (tid == 0) atomicExch(&c->bar.err, 2);
       break;
     }
     ++it;
@@ -165,7 +127,7 @@ __global__ void __launch_bounds__(kSbNT)
         }
       }
       // the heavy members: every thread of the grid over their edges
-      if (!sb_barrier(c)) return;
+      if (!gasgrid::barrier(&c->bar)) return;
       const int nh = *(volatile int *)n_heavy;
       for (int h = 0; h < nh; ++h) {
         const int u = __ldcg(heavy + h);
@@ -218,7 +180,7 @@ __global__ void __launch_bounds__(kSbNT)
       else
         ++c->n_push;
     }
-    if (!sb_barrier(c)) return;
+    if (!gasgrid::barrier(&c->bar)) return;
   }
   if (kCount) warp_add(bytes, &c->bytes);
   if (tid == 0) c->iterations = it;
@@ -229,8 +191,8 @@ __global__ void k_small_finish(const SmallCtl *c, gas_counters *cnt) {
   cnt->iteration = c->iterations;
   cnt->n_push = c->n_push;
   cnt->n_pull = c->n_pull;
-  cnt->error = c->err == 1 ? GAS_ERR_DEVICE : c->err == 2 ? GAS_ERR_ITER_CAP : 0;
-  cnt->n_active = c->err ? cnt->n_active : 0;
+  cnt->error = c->bar.err == 1 ? GAS_ERR_DEVICE : c->bar.err == 2 ? GAS_ERR_ITER_CAP : 0;
+  cnt->n_active = c->bar.err ? cnt->n_active : 0;
 }
 
 }  // namespace
