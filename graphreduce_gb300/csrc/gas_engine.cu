@@ -493,6 +493,7 @@ void free_graph(gas_engine *e) {
   dfree(e->pr_seed); dfree(e->pr_inv_deg); dfree(e->pr_l1); dfree(e->csr_to_csc);
   dfree(e->pr_tile_row); dfree(e->pr_head); dfree(e->pr_tail);
   dfree(e->sb_bits); dfree(e->sb_ctl); dfree(e->sb_heavy);
+  e->sb_clean = false;
   e->pr_tile_cap = 0;
   e->h_csr_perm.clear();
   e->h_csr_to_csc.clear();

@@ -134,6 +134,7 @@ struct gas_engine {
   uint32_t *sb_bits = nullptr;
   void *sb_ctl = nullptr;
   int32_t *sb_heavy = nullptr;
+  bool sb_clean = false;  // the kernel left them clear for the next run
   // what graphs[kGraphUser] was captured with (gas_engine_run_user)
   gas_user_step_fn user_step = nullptr;
   void *user_ctx = nullptr;

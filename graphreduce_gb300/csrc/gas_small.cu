@@ -63,7 +63,16 @@ __global__ void __launch_bounds__(kSbNT, 1)
                 const int32_t *__restrict__ csc_off, const int32_t *__restrict__ csc_src,
                 int32_t *depth, const int32_t *__restrict__ act, int n_act, uint32_t *bits,
                 int32_t *heavy, int nW, int nV, long long nE, int forced, int max_iter,
-                SmallCtl *c) {
+                SmallCtl *c, gas_counters *cnt) {
+  // a barrier wait that gave up: every CTA leaves; the error goes straight
+  // to the engine's counters (the epilogue below does not run)
+#define SB_SYNC()                                                     \
+  do {                                                                \
+    if (!gasgrid::barrier(&c->bar)) {                                 \
+      if (threadIdx.x == 0) atomicExch(&cnt->error, (int)GAS_ERR_DEVICE); \
+      return;                                                         \
+    }                                                                 \
+  } while (0)
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31, gwarp = tid >> 5, nwarps = nthr >> 5;
@@ -79,7 +88,7 @@ __global__ void __launch_bounds__(kSbNT, 1)
     }
   }
   warp_add(found, &c->f_edges[0]);
-  if (!gasgrid::barrier(&c->bar)) return;
+  SB_SYNC();
   int it = 1;
   for (int k = 0;; ++k) {
     const int cur = k % 3, nxt = (k + 1) % 3, old = (k + 2) % 3;
@@ -127,7 +136,7 @@ __global__ void __launch_bounds__(kSbNT, 1)
         }
       }
       // the heavy members: every thread of the grid over their edges
-      if (!gasgrid::barrier(&c->bar)) return;
+      SB_SYNC();
       const int nh = *(volatile int *)n_heavy;
       for (int h = 0; h < nh; ++h) {
         const int u = __ldcg(heavy + h);
@@ -180,19 +189,29 @@ __global__ void __launch_bounds__(kSbNT, 1)
       else
         ++c->n_push;
     }
-    if (!gasgrid::barrier(&c->bar)) return;
+    SB_SYNC();
   }
   if (kCount) warp_add(bytes, &c->bytes);
-  if (tid == 0) c->iterations = it;
-}
-
-// The engine's counters after the run, as the fast schedule leaves them.
-__global__ void k_small_finish(const SmallCtl *c, gas_counters *cnt) {
-  cnt->iteration = c->iterations;
-  cnt->n_push = c->n_push;
-  cnt->n_pull = c->n_pull;
-  cnt->error = c->bar.err == 1 ? GAS_ERR_DEVICE : c->bar.err == 2 ? GAS_ERR_ITER_CAP : 0;
-  cnt->n_active = c->bar.err ? cnt->n_active : 0;
+  // the next run finds the bitmaps clear (nothing reads them any more)
+  for (int w = tid; w < 3 * nW; w += nthr) bits[w] = 0u;
+  if (tid == 0) {
+    // the engine's counters, as the fast schedule leaves them
+    const int err = c->bar.err;
+    cnt->iteration = it;
+    cnt->n_push = c->n_push;
+    cnt->n_pull = c->n_pull;
+    cnt->error = err == 2 ? GAS_ERR_ITER_CAP : 0;
+    if (!err) cnt->n_active = 0;
+    // and the control word clear for the next run: its counts are read by
+    // no thread after the loop (a thread still to test f_edges reads 0 and
+    // leaves as well)
+    c->iterations = it;
+    c->n_push = c->n_pull = 0;
+    c->n_heavy[0] = c->n_heavy[1] = 0;
+    c->f_edges[0] = c->f_edges[1] = c->f_edges[2] = 0;
+    c->bar.err = 0;
+  }
+#undef SB_SYNC
 }
 
 }  // namespace
@@ -222,8 +241,14 @@ gas_status_t run_bfs_small(gas_engine *e, gas_schedule_t schedule, int32_t max_i
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSbNT, 0));
   if (per_sm < 1) return fail(GAS_ERR_CUDA, "small BFS: no resident CTA");
   const int grid = e->num_sms;  // one CTA per SM: the barrier's atomics are per CTA
-  CUDA_TRY(cudaMemsetAsync(e->sb_bits, 0, (size_t)3 * nW * sizeof(uint32_t), s));
-  CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(SmallCtl), s));
+  // the kernel leaves its bitmaps and control word clear; they are cleared
+  // here after allocation, after a run that failed, and when bytes count
+  if (!e->sb_clean || count) {
+    CUDA_TRY(cudaMemsetAsync(e->sb_bits, 0, (size_t)3 * nW * sizeof(uint32_t), s));
+    CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(SmallCtl), s));
+  }
+  e->sb_clean = false;
+  gas_counters *cnt = e->cnt;
   const int32_t *csr_off = e->csr_off, *csr_dst = e->csr_dst, *csc_off = e->csc_off,
                 *csc_src = e->csc_src;
   int32_t *depth = static_cast<int32_t *>(e->vd);
@@ -235,28 +260,27 @@ gas_status_t run_bfs_small(gas_engine *e, gas_schedule_t schedule, int32_t max_i
   int forced = schedule == GAS_SCHED_PULL ? 2 : 0;
   int max_iter = max_iterations;
   int nw = nW;
-  void *args[] = {&csr_off, &csr_dst, &csc_off, &csc_src, &depth,    &act, &n_act, &bits,
-                  &heavy,   &nw,      &nV,      &nE,      &forced,   &max_iter, &ctl};
+  void *args[] = {&csr_off, &csr_dst, &csc_off, &csc_src,  &depth, &act, &n_act, &bits,
+                  &heavy,   &nw,      &nV,      &nE,      &forced, &max_iter, &ctl, &cnt};
   if (count) prof_begin(e, s, kProfPush, 0);
   CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kSbNT), args, 0, s));
   prof_end(e, s);
-  k_small_finish<<<1, 1, 0, s>>>(ctl, e->cnt);
-  CUDA_TRY(cudaGetLastError());
-  SmallCtl h;
-  CUDA_TRY(cudaMemcpyAsync(&h, ctl, sizeof(h), cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
   if (count) {
+    SmallCtl h;
+    CUDA_TRY(cudaMemcpyAsync(&h, ctl, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
     e->prof_bytes_pending = h.bytes;
     prof_collect(e);
   }
   gas_counters c;
   GAS_TRY(engine_sync_counts(e, stream));
   c = *e->h_cnt;
+  e->sb_clean = c.error == 0 || c.error == GAS_ERR_ITER_CAP;
   if (stats) {
     stats->iterations = c.iteration;
     stats->push_iters = c.n_push;
     stats->pull_iters = c.n_pull;
-    stats->kernel_launches = 2;
+    stats->kernel_launches = 1;
     stats->graph_launches = 0;
   }
   e->level = c.iteration;
