@@ -935,9 +935,10 @@ C4_SCHEDULES = ("auto", "push", "pull", "learned")
 
 
 def run_c4(args, model, pr_warm):
-    """SSSP and CC under every schedule on graphs the heads never saw; the
-    learned schedule against the fixed heuristic (AUTO) and against the best
-    fixed schedule; outputs identical across schedules.  The PageRank warm
+    """BFS, SSSP and CC under every schedule on graphs the heads never saw;
+    the learned schedule against the fixed heuristic (AUTO) and against the
+    best fixed schedule; outputs identical across schedules (BFS has no
+    learned head: LEARNED runs its AUTO direction rule).  The PageRank warm
     start against the uniform start (iterations to the same tolerance)."""
     import torch
 
@@ -963,7 +964,7 @@ def run_c4(args, model, pr_warm):
         src = int(el.sample_sources(1, C4_SEED)[0])
         log(f"c4 {name}: V={el.nV} E={el.nE}, generated in {time.time() - t:.1f}s")
         row = {"V": el.nV, "E": el.nE}
-        for program in ("sssp", "cc"):
+        for program in ("bfs", "sssp", "cc"):
             e = gg.GASEngineGPU(program)
             vd = initial_vertex_data(program, el.nV, src)
             e.setGraph(el.nV, vd, el.nE, el.weights if program == "sssp" else None,
@@ -971,13 +972,14 @@ def run_c4(args, model, pr_warm):
             e.set_schedule_model(model)
             init_d = torch.from_numpy(vd).to("cuda")
             host = np.empty(el.nV, np.int32)
+            lo, hi = (src, src + 1) if program == "bfs" else (0, el.nV)
             outs, r = {}, {}
             for s in C4_SCHEDULES:
                 st = {}
 
-                def run(s=s, st=st):
+                def run(s=s, st=st, lo=lo, hi=hi):
                     e.upload_vertex_data_ptr(init_d.data_ptr(), sp)
-                    e.setActive(0, el.nV, sp)
+                    e.setActive(lo, hi, sp)
                     st["s"] = e.run_schedule(s, max_iterations=el.nV + 2, stream=sp)
 
                 ms = cuda_timed(stream, run, max(2, min(args.steps, 5)), 1)
@@ -993,6 +995,8 @@ def run_c4(args, model, pr_warm):
             r["learned_speedup_vs_auto"] = round(r["auto"]["ms"] / r["learned"]["ms"], 4)
             r["best_fixed"] = best_fixed
             r["learned_vs_best_fixed"] = round(r[best_fixed]["ms"] / r["learned"]["ms"], 4)
+            if program == "bfs":  # the BFS head is the per-level direction rule
+                r["learned_runs_as"] = "auto"
             all_ok &= same
             row[program] = r
         del el
@@ -1015,8 +1019,8 @@ def run_c4(args, model, pr_warm):
                             "l1_between_results": float(np.abs(r_uni.astype(np.float64) -
                                                                r_warm).sum())}}
     res["parity"] = all_ok
-    res["parity_detail"] = ("SSSP distances and CC labels identical under auto, push, pull and "
-                            "learned, with equal iteration counts (the oracle pins the "
+    res["parity_detail"] = ("BFS depths, SSSP distances and CC labels identical under auto, "
+                            "push, pull and learned, with equal iteration counts (the oracle pins the "
                             "schedules on C1/C2 and in the GPU tests)")
     return res
 
