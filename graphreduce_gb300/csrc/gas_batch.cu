@@ -462,9 +462,12 @@ struct MssPushPolStaged {
         nb |= 1u << k;
       }
     }
-    // the lanes and the touched bit as fire-and-forget reductions (the
-    // touched bit is idempotent, so no thread waits for an atomic's result)
-    if (nb && (cmask[p.v] & nb) != nb) {
+    // the lanes and the touched bit as fire-and-forget reductions (both are
+    // idempotent, so no thread waits for an atomic's result); issued
+    // without first loading cmask[v] to skip repeats: that dependent load
+    // cost more than the repeated reductions (8 lanes at R-MAT scale 22:
+    // 0.406 -> 0.370 ms per push)
+    if (nb) {
       atomicOr(cmask + p.v, nb);
       atomicOr(tbits + ((uint32_t)p.v >> 5), 1u << (p.v & 31));
     }
