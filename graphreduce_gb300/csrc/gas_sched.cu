@@ -97,11 +97,20 @@ __global__ void k_seed_finite(const int32_t *vd, int nV, int32_t zero_cap,
 // hold (value, CSR start, out-degree).  Both parts are in vertex order.
 // When the next iteration is a dense pull, also the snapshots of all members
 // and the members' ids (by which the snapshots are reset afterwards).  One lane per vertex:
-// each warp takes 8 bitmap words; a word's 32 lanes read their out-degrees
-// coalesced, ballots give queue positions, a warp scan gives edge offsets.
+// each warp takes a run of 16 bitmap words (lane l < 16 holds word w0 + l)
+// and walks it in two rounds of 8 words whose out-degree loads are in
+// flight together, skipping a round whose words are all clear; a word's 32
+// lanes read their out-degrees coalesced, ballots give queue positions, a
+// warp scan gives edge offsets.  The count pass also keeps each warp's
+// totals, so the write pass takes its offsets without counting again.
+// (8 words per warp, one round, ran CC on R-MAT 22 + islands 6 % slower --
+// 4 times as many blocks per pass; 32 words, four rounds, ran single-source
+// SSSP 4 % slower -- longer serial chains in its dense iterations.)
 // ---------------------------------------------------------------------------
-constexpr int kQWordsPerWarp = 8;
-constexpr int kQWordsPerBlock = kQWordsPerWarp * (kNT / 32);  // 64 words
+constexpr int kQWordsPerWarp = 16;
+constexpr int kQRound = 8;
+constexpr int kQWarpsPerBlock = kNT / 32;
+constexpr int kQWordsPerBlock = kQWordsPerWarp * kQWarpsPerBlock;  // 128 words
 constexpr int kLightDeg = 8;  // rows with at most this many out-edges are light
 
 __device__ __forceinline__ int warp_incl_sum_i(int v) {
@@ -118,65 +127,68 @@ __device__ __forceinline__ int4 add4(int4 a, int4 b) {
   return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
 
-// A warp owns 8 bitmap words; lane l takes vertex 32 w + l of each word, so
-// the out-offset loads of a word are coalesced, and the 8 words' loads are
-// issued before any of them is used.
-struct QWarp {
-  int off[kQWordsPerWarp];
-  int deg[kQWordsPerWarp];  // 0 when the bit is clear
-  uint32_t myword;          // lanes 0..7: word w0 + lane
+// One round: words w0 + r .. w0 + r + 7 of the warp's run (taken from the
+// lanes' own words by shuffles); lane l takes vertex 32 w + l of each word,
+// so the out-offset loads of a word are coalesced, and the 8 words' loads
+// are issued before any of them is used.
+struct QRound {
+  int off[kQRound];
+  int deg[kQRound];  // 0 when the bit is clear
 };
 
-__device__ __forceinline__ void q_warp_load(const uint32_t *cbits, const int32_t *csr_off,
-                                            int nW, int w0, QWarp &w) {
+__device__ __forceinline__ void q_round_load(uint32_t myword, const int32_t *csr_off, int w0,
+                                             int r, QRound &q) {
   const int lane = threadIdx.x & 31;
-  w.myword = (lane < kQWordsPerWarp && w0 + lane < nW) ? cbits[w0 + lane] : 0u;
 #pragma unroll
-  for (int i = 0; i < kQWordsPerWarp; ++i) {
-    const uint32_t word = __shfl_sync(0xffffffffu, w.myword, i);
-    w.off[i] = 0;
-    w.deg[i] = 0;
+  for (int i = 0; i < kQRound; ++i) {
+    const uint32_t word = __shfl_sync(0xffffffffu, myword, r + i);
+    q.off[i] = 0;
+    q.deg[i] = 0;
     if ((word >> lane) & 1u) {
-      const int v = (w0 + i) * 32 + lane;
-      w.off[i] = csr_off[v];
-      w.deg[i] = csr_off[v + 1] - w.off[i];
+      const int v = (w0 + r + i) * 32 + lane;
+      q.off[i] = csr_off[v];
+      q.deg[i] = csr_off[v + 1] - q.off[i];
     }
   }
 }
 
-// The warp's (heavy rows, heavy edges, light rows, light edges).
-__device__ __forceinline__ int4 q_warp_totals(const QWarp &w) {
-  int hq = 0, hd = 0, lq = 0, ld = 0;
+// Adds a round's (heavy rows, heavy edges, light rows, light edges) to the
+// lane's counts.
+__device__ __forceinline__ void q_round_count(const QRound &q, int4 &c) {
 #pragma unroll
-  for (int i = 0; i < kQWordsPerWarp; ++i) {
-    const int d = w.deg[i];
+  for (int i = 0; i < kQRound; ++i) {
+    const int d = q.deg[i];
     if (d > kLightDeg) {
-      ++hq;
-      hd += d;
+      ++c.x;
+      c.y += d;
     } else if (d > 0) {
-      ++lq;
-      ld += d;
+      ++c.z;
+      c.w += d;
     }
   }
+}
+
+__device__ __forceinline__ int4 warp_sum4(int4 c) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    hq += __shfl_xor_sync(0xffffffffu, hq, o);
-    hd += __shfl_xor_sync(0xffffffffu, hd, o);
-    lq += __shfl_xor_sync(0xffffffffu, lq, o);
-    ld += __shfl_xor_sync(0xffffffffu, ld, o);
+    c.x += __shfl_xor_sync(0xffffffffu, c.x, o);
+    c.y += __shfl_xor_sync(0xffffffffu, c.y, o);
+    c.z += __shfl_xor_sync(0xffffffffu, c.z, o);
+    c.w += __shfl_xor_sync(0xffffffffu, c.w, o);
   }
-  return make_int4(hq, hd, lq, ld);
+  return c;
 }
 
-// Counts per block, and the queue's out-degree histogram (schedule
-// features).  The snapshots are written only for a queue that a dense pull
-// reads: after a pull iteration (mode still says so here) the previous
-// queue's snapshots (its length is still in the counters) go back to
-// Program::gatherZero first.  BFS's bottom-up pass reads depths, never
-// snapshots (bfs != 0: none are written or reset).
+// Counts per block (part, for the spine) and per warp (wpart, for the write
+// pass), and the queue's out-degree histogram (schedule features).  The
+// snapshots are written only for a queue that a dense pull reads: after a
+// pull iteration (mode still says so here) the previous queue's snapshots
+// (its length is still in the counters) go back to Program::gatherZero
+// first.  BFS's bottom-up pass reads depths, never snapshots (bfs != 0:
+// none are written or reset).
 __global__ void __launch_bounds__(kNT)
     k_q_count(const uint32_t *cbits, const int32_t *csr_off, int nW,
-              int4 *part, const int32_t *q_ids, int32_t *snap, int32_t zero,
+              int4 *part, int4 *wpart, const int32_t *q_ids, int32_t *snap, int32_t zero,
               int32_t *hist, const gas_counters *cnt, int bfs) {
   if (!bfs && cnt->mode == kModePull) {
     const int n_old = cnt->n_changed;
@@ -184,75 +196,73 @@ __global__ void __launch_bounds__(kNT)
          i += gridDim.x * blockDim.x)
       snap[q_ids[i]] = zero;
   }
-  __shared__ int4 s_t[kNT / 32];
+  __shared__ int4 s_t[kQWarpsPerBlock];
   __shared__ int s_hist[8];
   if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
+  if (hist) __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
-  QWarp w;
-  q_warp_load(cbits, csr_off, nW, w0, w);
-  const int4 t = q_warp_totals(w);
-  if (lane == 0) s_t[warp] = t;
-  __syncthreads();
-  if (hist) {
+  const int w0 = (blockIdx.x * kQWarpsPerBlock + warp) * kQWordsPerWarp;
+  const uint32_t myword =
+      lane < kQWordsPerWarp && w0 + lane < nW ? cbits[w0 + lane] : 0u;
+  const unsigned nz = __ballot_sync(0xffffffffu, myword != 0u);
+  int4 c = make_int4(0, 0, 0, 0);
+#pragma unroll 1
+  for (int r = 0; r < kQWordsPerWarp; r += kQRound) {
+    if (!((nz >> r) & ((1u << kQRound) - 1u))) continue;  // warp-uniform
+    QRound q;
+    q_round_load(myword, csr_off, w0, r, q);
+    q_round_count(q, c);
+    if (hist) {
 #pragma unroll
-    for (int i = 0; i < kQWordsPerWarp; ++i)
-      if (w.deg[i] > 0) atomicAdd(&s_hist[gasfeat::degree_bucket(w.deg[i])], 1);
+      for (int i = 0; i < kQRound; ++i)
+        if (q.deg[i] > 0) atomicAdd(&s_hist[gasfeat::degree_bucket(q.deg[i])], 1);
+    }
   }
+  const int4 t = warp_sum4(c);
+  if (lane == 0) {
+    s_t[warp] = t;
+    wpart[blockIdx.x * kQWarpsPerBlock + warp] = t;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
     int4 b = make_int4(0, 0, 0, 0);
-    for (int k = 0; k < kNT / 32; ++k) b = add4(b, s_t[k]);
+    for (int k = 0; k < kQWarpsPerBlock; ++k) b = add4(b, s_t[k]);
     part[blockIdx.x] = b;
   }
-  if (hist) {
-    __syncthreads();
-    if (threadIdx.x < 8 && s_hist[threadIdx.x]) atomicAdd(hist + threadIdx.x, s_hist[threadIdx.x]);
-  }
+  if (hist && threadIdx.x < 8 && s_hist[threadIdx.x])
+    atomicAdd(hist + threadIdx.x, s_hist[threadIdx.x]);
 }
 
 constexpr int kSpineNT = 1024;  // k_q_spine (with the loop control, below)
 constexpr int kBfsPullDiv = 16;  // BFS: bottom-up while out-edges(C_k) * 16 > E
 constexpr int kSpineRegs = 4;
 
-// (at most 48 registers: 5 CTAs per SM, so a sparse iteration's mostly
-// empty bitmap tiles pass in fewer waves)
-__global__ void __launch_bounds__(kNT, 5)
-    k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int4 *part,
-              const int32_t *vd, int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
-              int32_t *q_delta, int32_t *snap, int32_t *chunk_row,
-              const gas_counters *cnt, int bfs) {
-  __shared__ int4 s_t[kNT / 32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int w0 = blockIdx.x * kQWordsPerBlock + warp * kQWordsPerWarp;
-  if (bfs && cnt->mode == kModePull) {  // grid-uniform: the next BFS level is
-    // bottom-up and reads depths, so only the changed bitmap is cleared
-    if (lane < kQWordsPerWarp && w0 + lane < nW && cbits[w0 + lane]) cbits[w0 + lane] = 0u;
-    return;
-  }
-  QWarp w;
-  q_warp_load(cbits, csr_off, nW, w0, w);
-  int val[kQWordsPerWarp];
-#pragma unroll
-  for (int i = 0; i < kQWordsPerWarp; ++i)
-    val[i] = w.deg[i] > 0 ? vd[(w0 + i) * 32 + lane] : 0;
-  const int4 t = q_warp_totals(w);
-  if (lane == 0) s_t[warp] = t;
-  __syncthreads();
-  int4 base = part[blockIdx.x];
-  for (int k = 0; k < warp; ++k) base = add4(base, s_t[k]);
-  int bq = base.x, bd = base.y, lq = cnt->q_heavy + base.z;
-  const int cl = cnt->push_chunk_log2;
-  const bool want_snap = !bfs && cnt->mode == kModePull;  // the next iteration's mode
-  if (w.myword) cbits[w0 + lane] = 0u;
+// Queue positions of a warp's next rows: heavy row, heavy-edge offset,
+// light row.
+struct QPos {
+  int bq, bd, lq;
+};
+
+// The queue entries of one round (its words' members in q, their values in
+// val), from heavy position p.bq, heavy-edge offset p.bd and light position
+// p.lq on; advances p.  chunk_row: the push's partition in (1 << cl)-edge
+// chunks.
+__device__ __forceinline__ void q_round_write(const QRound &q, const int *val, QPos &p,
+                                              int wr, int cl, bool want_snap,
+                                              int32_t *q_ids, int32_t *q_vals, int32_t *q_end,
+                                              int32_t *q_delta, int32_t *snap,
+                                              int32_t *chunk_row) {
+  const int lane = threadIdx.x & 31;
+  int bq = p.bq, bd = p.bd, lq = p.lq;
   const unsigned below = (1u << lane) - 1u;
 #pragma unroll
-  for (int i = 0; i < kQWordsPerWarp; ++i) {
-    const int deg = w.deg[i];
+  for (int i = 0; i < kQRound; ++i) {
+    const int deg = q.deg[i];
     const bool heavy = deg > kLightDeg;
     const unsigned hb = __ballot_sync(0xffffffffu, heavy);
     const unsigned lb = __ballot_sync(0xffffffffu, deg > 0 && !heavy);
     if (!(hb | lb)) continue;  // warp-uniform
-    const int v = (w0 + i) * 32 + lane;
+    const int v = (wr + i) * 32 + lane;
     if (hb) {  // warp-uniform
       const int incl = warp_incl_sum_i(heavy ? deg : 0);
       if (heavy) {
@@ -261,7 +271,7 @@ __global__ void __launch_bounds__(kNT, 5)
         if (want_snap) q_ids[pos] = v;  // only a pull's snapshots are reset by id
         q_vals[pos] = val[i];
         q_end[pos] = end;
-        q_delta[pos] = w.off[i] - (end - deg);
+        q_delta[pos] = q.off[i] - (end - deg);
         // the push's chunk partition: every (1 << cl)-edge chunk that
         // starts inside this row's heavy-edge range starts in row pos
         for (int c = (end - deg + (1 << cl) - 1) >> cl; (c << cl) < end; ++c)
@@ -275,11 +285,52 @@ __global__ void __launch_bounds__(kNT, 5)
       if (want_snap) q_ids[pos] = v;
       q_vals[pos] = val[i];
       q_end[pos] = deg;
-      q_delta[pos] = w.off[i];
+      q_delta[pos] = q.off[i];
     }
     lq += __popc(lb);
     if (want_snap && deg > 0) snap[v] = val[i];
   }
+  p.bq = bq;
+  p.bd = bd;
+  p.lq = lq;
+}
+
+// (at most 48 registers: 5 CTAs per SM, so a sparse iteration's mostly
+// empty bitmap runs pass in fewer waves)
+__global__ void __launch_bounds__(kNT, 5)
+    k_q_write(uint32_t *cbits, const int32_t *csr_off, int nW, const int4 *part,
+              const int4 *wpart, const int32_t *vd, int32_t *q_ids, int32_t *q_vals,
+              int32_t *q_end, int32_t *q_delta, int32_t *snap, int32_t *chunk_row,
+              const gas_counters *cnt, int bfs) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = (blockIdx.x * kQWarpsPerBlock + warp) * kQWordsPerWarp;
+  const uint32_t myword =
+      lane < kQWordsPerWarp && w0 + lane < nW ? cbits[w0 + lane] : 0u;
+  if (bfs && cnt->mode == kModePull) {  // grid-uniform: the next BFS level is
+    // bottom-up and reads depths, so only the changed bitmap is cleared
+    if (myword) cbits[w0 + lane] = 0u;
+    return;
+  }
+  const unsigned nz = __ballot_sync(0xffffffffu, myword != 0u);
+  if (!nz) return;  // warp-uniform: no member, no word to clear
+  int4 base = part[blockIdx.x];
+  for (int k = 0; k < warp; ++k) base = add4(base, wpart[blockIdx.x * kQWarpsPerBlock + k]);
+  QPos p{base.x, base.y, cnt->q_heavy + base.z};
+  const int cl = cnt->push_chunk_log2;
+  const bool want_snap = !bfs && cnt->mode == kModePull;  // the next iteration's mode
+#pragma unroll 1
+  for (int r = 0; r < kQWordsPerWarp; r += kQRound) {
+    if (!((nz >> r) & ((1u << kQRound) - 1u))) continue;  // warp-uniform
+    QRound q;
+    q_round_load(myword, csr_off, w0, r, q);
+    int val[kQRound];
+#pragma unroll
+    for (int i = 0; i < kQRound; ++i)
+      val[i] = q.deg[i] > 0 ? vd[(w0 + r + i) * 32 + lane] : 0;
+    q_round_write(q, val, p, w0 + r, cl, want_snap, q_ids, q_vals, q_end, q_delta, snap,
+                  chunk_row);
+  }
+  if (myword) cbits[w0 + lane] = 0u;
 }
 
 // Edge-stream load that does not allocate in L1: the edge arrays are read
@@ -818,13 +869,14 @@ int32_t snap_zero(const gas_engine *e) {
 gas_status_t compaction(gas_engine *e, cudaStream_t cs, const FastCtx &c,
                         cudaGraphConditionalHandle h, int phase) {
   int4 *part = reinterpret_cast<int4 *>(e->qpart);
+  int4 *wpart = part + c.n_qblocks;  // per-warp totals after the block totals
   int32_t *hist = (e->trace_on || e->sched_model) ? e->hist : nullptr;
   const int bfs = e->prog == GAS_PROG_BFS ? 1 : 0;
-  k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, part, e->q_ids,
+  k_q_count<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, part, wpart, e->q_ids,
                                          e->snap, snap_zero(e), hist, e->cnt, bfs);
   k_q_spine<<<1, kSpineNT, 0, cs>>>(part, c.n_qblocks, e->cnt, c.push_grid * (kNT / 32),
                                     loop_ctl(e, h), phase, c.seeded ? 1 : 0);
-  k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, part,
+  k_q_write<<<c.n_qblocks, kNT, 0, cs>>>(e->cbits, e->csr_off, c.nW, part, wpart,
                                          (const int32_t *)e->vd, e->q_ids, e->q_vals,
                                          e->q_end, e->q_delta, e->snap, e->slab_qpart,
                                          e->cnt, bfs);
@@ -937,7 +989,8 @@ gas_status_t ensure_fast_buffers(gas_engine *e) {
   CUDA_TRY(cudaMalloc(&e->q_delta, (V ? V : 1) * 4));
   CUDA_TRY(cudaMalloc(&e->snap, (V ? V : 1) * 4));
   CUDA_TRY(cudaMalloc(&e->cbits, (nW ? nW : 1) * 4));
-  CUDA_TRY(cudaMalloc(&e->qpart, (nqb ? nqb : 1) * sizeof(int4)));
+  // block totals, then the blocks' per-warp totals
+  CUDA_TRY(cudaMalloc(&e->qpart, (nqb ? nqb : 1) * (1 + kQWarpsPerBlock) * sizeof(int4)));
   CUDA_TRY(cudaMemset(e->cbits, 0, (nW ? nW : 1) * 4));
   return GAS_OK;
 }
