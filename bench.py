@@ -356,27 +356,30 @@ def run_ours(args, rank, world):
                 e_s.download_vertex_data_ptr(res_s[k].data_ptr(), sp)
 
     # end to end with batched lanes, copies overlap compute on a second
-    # stream: the CC labels go up while the SSSP lanes run, the distances
-    # come down while CC runs; the step ends when both streams are done
+    # stream (in order, so each copy also waits for the one before it): the
+    # CC labels go up while the SSSP lanes run, the distances come down
+    # while CC runs, and the CC labels come down while the next step's SSSP
+    # lanes run; the timed region ends when both streams are done
     cstream = torch.cuda.Stream(device=dev)
     csp = cstream.cuda_stream
-    prev_done = torch.cuda.Event()
+    dist_free = torch.cuda.Event()   # the last distances are down: dist_dev may change
+    dist_free.record(cstream)
 
     def one_step(e2e, schedule=args.schedule, use_batch=batched):
         launches[0] = 0
         if e2e and use_batch:
-            cstream.wait_event(prev_done)   # the previous step's results are down
+            # after the previous step's labels came down (same stream)
             e_c.upload_vertex_data_ptr(pin_c.data_ptr(), csp)
             up = torch.cuda.Event()
             up.record(cstream)
+            stream.wait_event(dist_free)
             sssp_batched(False)
             lanes_done = torch.cuda.Event()
             lanes_done.record(stream)
             cstream.wait_event(lanes_done)
             with torch.cuda.stream(cstream):
                 dist_pin.copy_(dist_dev, non_blocking=True)
-            down = torch.cuda.Event()
-            down.record(cstream)
+            dist_free.record(cstream)
             stream.wait_event(up)
         elif use_batch:
             sssp_batched(e2e)
@@ -388,11 +391,13 @@ def run_ours(args, rank, world):
         st = e_c.run_schedule(schedule, max_iterations=MAX_ITERS, stream=sp)
         iters["cc"] = st.iterations
         launches[0] += st.kernel_launches + 1
-        if e2e:
-            e_c.download_vertex_data_ptr(res_c.data_ptr(), sp)
         if e2e and use_batch:
-            stream.wait_event(down)
-            prev_done.record(stream)
+            cc_done = torch.cuda.Event()
+            cc_done.record(stream)
+            cstream.wait_event(cc_done)
+            e_c.download_vertex_data_ptr(res_c.data_ptr(), csp, wait=False)
+        elif e2e:
+            e_c.download_vertex_data_ptr(res_c.data_ptr(), sp)
 
     if args.launch_list:
         # one device-resident step and nothing else (for an ncu launch list)
@@ -421,8 +426,10 @@ def run_ours(args, rank, world):
         end = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         start.record(stream)
+        cstream.wait_event(start)    # the copies of the first step start after it
         for _ in range(steps):
             one_step(e2e, schedule, use_batch)
+        stream.wait_stream(cstream)  # and the last step's copies end before `end`
         end.record(stream)
         torch.cuda.synchronize()
         ms = start.elapsed_time(end)
@@ -433,7 +440,7 @@ def run_ours(args, rank, world):
     clocks = clk.summary()
     launches_per_step = launches[0]
     iters_step = {"sssp": list(iters["sssp"]), "cc": iters["cc"]}
-    ms_e2e = timed(True, max(1, args.steps), 1)
+    ms_e2e = timed(True, max(1, args.steps), args.warmup)
     comparisons = {}
     # the same step with one SSSP run per source (learned schedule), and the
     # plain form: one run per source under the fixed heuristic (AUTO), both
@@ -485,8 +492,10 @@ def run_ours(args, rank, world):
                                            "iterations": iters_step}),
         "e2e": {"value": round(e2e, 4), "unit": "GTEPS", "ms_per_step": round(ms_e2e, 3),
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "copies": ("pinned host buffers; CC labels up while the SSSP lanes run and "
-                           "distances down while CC runs (second stream)" if batched else
+                "copies": ("pinned host buffers; CC labels up while the SSSP lanes run, "
+                           "distances down while CC runs, CC labels down while the next "
+                           "step's SSSP lanes run (second stream; every step's copies "
+                           "inside the timed region)" if batched else
                            "pinned host buffers, on the compute stream")},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roof,

@@ -134,6 +134,7 @@ _SIGS = {
     "gas_engine_vertex_data_device": ("status", [c_vp, C.POINTER(c_vp)]),
     "gas_engine_upload_vertex_data": ("status", [c_vp, c_vp, c_vp]),
     "gas_engine_download_vertex_data": ("status", [c_vp, c_vp, c_vp]),
+    "gas_engine_download_vertex_data_async": ("status", [c_vp, c_vp, c_vp]),
     "gas_engine_run_schedule": ("status", [c_vp, c_i32, c_i32, C.POINTER(RunStats), c_vp]),
     "gas_engine_run_user": ("status", [c_vp, c_vp, c_vp, c_i32, c_i32, C.POINTER(RunStats),
                                        c_vp]),

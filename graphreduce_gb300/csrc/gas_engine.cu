@@ -1157,6 +1157,14 @@ gas_status_t gas_engine_download_vertex_data(gas_engine *e, void *host,
   return GAS_OK;
 }
 
+gas_status_t gas_engine_download_vertex_data_async(gas_engine *e, void *dst,
+                                                   void *stream) {
+  if (!e || !dst || !e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
+  CUDA_TRY(cudaMemcpyAsync(dst, e->vd, (size_t)e->nV * e->vbytes, cudaMemcpyDefault,
+                           S(stream)));
+  return GAS_OK;
+}
+
 gas_status_t gas_engine_view_get(gas_engine *e, gas_engine_view *v) {
   if (!e || !v || !e->has_graph) return gas::fail(GAS_ERR_STATE, "no graph");
   v->nV = e->nV;

@@ -166,10 +166,12 @@ class GASEngineGPU:
         engine's device vertex data."""
         L.call("gas_engine_upload_vertex_data", self._h, ptr, _stream_ptr(stream))
 
-    def download_vertex_data_ptr(self, ptr: int, stream=None) -> None:
-        """Copies the device vertex data to any host or device address
-        (synchronises the stream)."""
-        L.call("gas_engine_download_vertex_data", self._h, ptr, _stream_ptr(stream))
+    def download_vertex_data_ptr(self, ptr: int, stream=None, wait: bool = True) -> None:
+        """Copies the device vertex data to any host or device address;
+        wait=True synchronises the stream, wait=False only queues the copy
+        on it (the destination must stay valid until it completes)."""
+        L.call("gas_engine_download_vertex_data" if wait else
+               "gas_engine_download_vertex_data_async", self._h, ptr, _stream_ptr(stream))
 
     def set_profiling(self, on: bool) -> None:
         """Kernel-level timing of later runs (direct launches, CUDA events)."""

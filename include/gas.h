@@ -224,6 +224,11 @@ gas_status_t gas_engine_upload_vertex_data(gas_engine *e, const void *host,
                                            void *stream);
 gas_status_t gas_engine_download_vertex_data(gas_engine *e, void *host,
                                              void *stream);
+/* The same copy out without waiting for it: it is queued on stream, and dst
+ * must stay valid (and the vertex data unchanged) until it completes.  For
+ * callers that overlap the read-back of one run with the next run's work. */
+gas_status_t gas_engine_download_vertex_data_async(gas_engine *e, void *dst,
+                                                   void *stream);
 
 /* Schedule of the built-in fast runs.  For BFS the pull is the bottom-up
  * level (each unvisited vertex stops at its first in-neighbour of the

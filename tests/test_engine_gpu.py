@@ -255,6 +255,31 @@ def test_iteration_cap_reports_error_without_fault(schedule):
     assert st.iterations == rit
 
 
+def test_async_download_matches_the_blocking_one():
+    """gas_engine_download_vertex_data_async queues the same copy on the
+    stream without waiting; after a synchronise it holds what the blocking
+    download returns."""
+    torch = pytest.importorskip("torch")
+    el = EdgeList.rmat(12, 16, seed=3).with_uniform_weights(1, 64, 4)
+    s = int(el.sample_sources(1, 3)[0])
+    eng = GASEngineGPU("sssp")
+    eng.setGraph(el.nV, initial_vertex_data("sssp", el.nV, s), el.nE, el.weights,
+                 el.src, el.dst)
+    eng.setActive(0, el.nV)
+    eng.run_schedule("push", max_iterations=el.nV + 2)
+    blocking = np.empty(el.nV, np.int32)
+    eng.download_vertex_data(blocking)
+    stream = torch.cuda.Stream()
+    pinned = torch.full((el.nV,), -7, dtype=torch.int32).pin_memory()
+    eng.download_vertex_data_ptr(pinned.data_ptr(), stream.cuda_stream, wait=False)
+    stream.synchronize()
+    np.testing.assert_array_equal(pinned.numpy(), blocking)
+    np.testing.assert_array_equal(blocking, oracle.sssp(el.nV, el.src, el.dst, el.weights, s)[0])
+    with pytest.raises(GasError):
+        GASEngineGPU("cc").download_vertex_data_ptr(pinned.data_ptr(), wait=False)
+    eng.close()
+
+
 def test_invalid_arguments_raise():
     g = load_golden("path6")
     el = golden_el(g)
