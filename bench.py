@@ -160,10 +160,29 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# What bounds each kernel, from its ncu capture under profiles/ (bound is
+# "hbm" in the line's two-valued sense: a memory-side kernel, no tensor
+# work; frac counts algorithmic bytes against the HBM peak, dram_frac the
+# bytes that reached DRAM).
+LIMITER = {
+    "mss_push": "L1 data pipe (68 % of peak) and L2 tag lookups (51 %); DRAM 15.5 %: most "
+                "algorithmic bytes are L2 hits (profiles/k_mss_push_sssp8-batched_rmat-s20.md)",
+    "push": "latency of dependent loads per light row with 93 % of warp slots occupied; "
+            "L2 tags 36 %, DRAM 25 % (profiles/k_push_cc-islands_rmat-s20.md)",
+    "pr_gather": "L1 data pipe (70 %): one wavefront per random contribution gather; DRAM "
+                 "18 % (profiles/k_pr_merge_pagerank_rmat-s24.md)",
+    "ppr_iteration": "latency of the 64-byte contribution-row gathers, 62 % of warp slots "
+                     "occupied (profiles/k_ppr_pieces_batched-8graphs.md)",
+    "bfs_small": "latency: one cooperative kernel, a few microseconds per level, the graph in "
+                 "L2 (profiles/k_bfs_small_bfs_rmat-s16.md)",
+}
+
+
 def roofline(kernel, key, total_bytes, total_ms, launches, workload, extra=None):
     """The dominant kernel's roofline: algorithmic bytes over its measured
     time (CUDA events around its launches), and where an ncu capture of the
-    kernel on this workload is recorded, its DRAM bytes over the same time."""
+    kernel on this workload is recorded, its DRAM bytes over the same time
+    and what its counters show bounds it."""
     peak, kind = measured_peaks()
     launches = max(1, int(launches))
     ms_l = total_ms / launches
@@ -176,6 +195,8 @@ def roofline(kernel, key, total_bytes, total_ms, launches, workload, extra=None)
          "launches": launches, "traffic": dram,
          "dram_achieved": round(dram / (ms_l * 1e-3) / 1e9, 1) if dram and ms_l > 0 else None,
          "dram_frac": round(dram / (ms_l * 1e-3) / 1e9 / peak, 4) if dram and ms_l > 0 else None}
+    if key in LIMITER and (dram is not None or key == "bfs_small"):  # captured on this workload
+        r["limiter"] = LIMITER[key]
     if extra:
         r.update(extra)
     return r
