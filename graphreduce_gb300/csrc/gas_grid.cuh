@@ -21,8 +21,11 @@ struct Barrier {
 };
 
 // Every CTA of a cooperative launch calls it; one atomic per CTA.  Returns
-// false once err is set (a wait ran out, or a kernel raised an error), and
-// the caller leaves the kernel.
+// false once err is set, and the caller leaves the kernel.  err is read
+// after the release, so a CTA still leaving one barrier sees a value that
+// another CTA wrote after passing it: write err only to end the kernel
+// with an error, never as a signal the kernel goes on from (an iteration
+// cap, say).
 __device__ __forceinline__ bool barrier(Barrier *b) {
   __syncthreads();
   if (threadIdx.x == 0) {

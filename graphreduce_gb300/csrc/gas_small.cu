@@ -49,7 +49,7 @@ constexpr int kSbHeavy = 256;   // out-edges of a member walked by the grid
 using gasgrid::warp_add;
 
 struct SmallCtl {
-  gasgrid::Barrier bar;  // bar.err: 1 a barrier wait gave up, 2 iteration cap
+  gasgrid::Barrier bar;  // bar.err: 1 a barrier wait gave up
   int iterations;
   int n_push, n_pull;
   int n_heavy[2];        // heavy members listed at a level (by level parity)
@@ -90,12 +90,15 @@ __global__ void __launch_bounds__(kSbNT, 1)
   warp_add(found, &c->f_edges[0]);
   SB_SYNC();
   int it = 1;
+  // the cap stays in each CTA: marked in the barrier's error word, a CTA
+  // still leaving the previous barrier would read it as a failed wait
+  bool capped = false;
   for (int k = 0;; ++k) {
     const int cur = k % 3, nxt = (k + 1) % 3, old = (k + 2) % 3;
     const long long fe = *(volatile long long *)&c->f_edges[cur];
     if (fe == 0) break;  // A_{k+1} = N(C_k) is empty
-    if (it >= max_iter) {
-      if (tid == 0) atomicExch(&c->bar.err, 2);
+    if (it >= max_iter) {  // every CTA stops here at the same level
+      capped = true;
       break;
     }
     ++it;
@@ -196,12 +199,13 @@ __global__ void __launch_bounds__(kSbNT, 1)
   for (int w = tid; w < 3 * nW; w += nthr) bits[w] = 0u;
   if (tid == 0) {
     // the engine's counters, as the fast schedule leaves them
-    const int err = c->bar.err;
+    // a wait that gave up in another CTA has written GAS_ERR_DEVICE already
+    const bool failed = *(volatile int *)&c->bar.err != 0;
     cnt->iteration = it;
     cnt->n_push = c->n_push;
     cnt->n_pull = c->n_pull;
-    cnt->error = err == 2 ? GAS_ERR_ITER_CAP : 0;
-    if (!err) cnt->n_active = 0;
+    if (!failed) cnt->error = capped ? GAS_ERR_ITER_CAP : 0;
+    if (!failed && !capped) cnt->n_active = 0;
     // and the control word clear for the next run: its counts are read by
     // no thread after the loop (a thread still to test f_edges reads 0 and
     // leaves as well)
@@ -209,7 +213,6 @@ __global__ void __launch_bounds__(kSbNT, 1)
     c->n_push = c->n_pull = 0;
     c->n_heavy[0] = c->n_heavy[1] = 0;
     c->f_edges[0] = c->f_edges[1] = c->f_edges[2] = 0;
-    c->bar.err = 0;
   }
 #undef SB_SYNC
 }
