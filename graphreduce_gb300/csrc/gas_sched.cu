@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include <climits>
+#include <cstring>
 #include <vector>
 
 #include "gas.h"
@@ -670,44 +671,51 @@ __device__ __forceinline__ void sched_logits_cta(SchedSmem &sm, float *lg) {
 // head (weights already staged when `learned`), or the fixed heuristic --
 // pull when the frontier's out-edges are more than 1/pull_div of all edges.
 // With tracing, records the iteration.
+// The loop state schedule_next decides from, as thread 0 of the spine holds
+// it in registers (the new queue's counts and the counters it read once at
+// the kernel's start).
+struct LoopVals {
+  int sched;  // 0 auto, 1 push, 2 pull, 3 learned
+  int it;     // the iteration being scheduled
+  int n_changed, n_scatter_edges, pull_div, cond;
+};
+
 __device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now,
-                              SchedSmem &sm, bool learned) {
+                              SchedSmem &sm, bool learned, const LoopVals &v) {
   const int t = threadIdx.x;
-  const int forced = cnt->sched;  // 0 auto, 1 push, 2 pull, 3 learned
-  const int it = cnt->iteration;   // the iteration being scheduled
   float lg[2] = {0.f, 0.f};
   if (learned) {  // CTA-uniform
     if (t == 0)
-      gasfeat::schedule_features(cnt->n_changed, cnt->n_scatter_edges, c.hist, it, c.nV,
-                                 c.nE, c.weighted, sm.f);
+      gasfeat::schedule_features(v.n_changed, v.n_scatter_edges, c.hist, v.it, c.nV, c.nE,
+                                 c.weighted, sm.f);
     __syncthreads();
     sched_logits_cta(sm, lg);
   }
   if (t == 0) {
     int mode;
-    if (forced == 1)
+    if (v.sched == 1)
       mode = kModePush;
-    else if (forced == 2)
+    else if (v.sched == 2)
       mode = kModePull;
     else if (learned)
       mode = lg[1] > lg[0] ? kModePull : kModePush;
     else
-      mode = ((long long)cnt->n_scatter_edges * cnt->pull_div > (long long)c.nE)
-                 ? kModePull : kModePush;
+      mode = ((long long)v.n_scatter_edges * v.pull_div > (long long)c.nE) ? kModePull
+                                                                           : kModePush;
     cnt->mode = mode;
-    if (c.trace && it < GAS_TRACE_CAP && cnt->cond) {
-      gas_trace_record &r = c.trace[it];
-      r.iteration = it;
+    if (c.trace && v.it < GAS_TRACE_CAP && v.cond) {
+      gas_trace_record &r = c.trace[v.it];
+      r.iteration = v.it;
       r.mode = mode;
-      r.n_queue = cnt->n_changed;
-      r.n_edges_out = cnt->n_scatter_edges;
+      r.n_queue = v.n_changed;
+      r.n_edges_out = v.n_scatter_edges;
       for (int b = 0; b < 8; ++b) r.hist[b] = c.hist ? c.hist[b] : 0;
       r.t_start_ns = now;
       r.t_end_ns = 0;
     }
     if (c.hist)
       for (int b = 0; b < 8; ++b) c.hist[b] = 0;
-    if (c.in_graph) cudaGraphSetConditional(c.h, cnt->cond);
+    if (c.in_graph) cudaGraphSetConditional(c.h, v.cond);
   }
 }
 
@@ -736,6 +744,18 @@ __global__ void __launch_bounds__(kSpineNT)
   __shared__ __align__(16) SchedSmem sm;
   const bool learned = cnt->sched == 3 && c.model != nullptr;
   if (learned) sched_stage_weights(sm, c.model);
+  // thread 0: every counter the loop control reads, in four 16-byte loads
+  // issued with the block totals' (gas_counters is 64 bytes at the start of
+  // a cudaMalloc block), instead of one dependent load after each store
+  gas_counters k;
+  if (threadIdx.x == 0) {
+    static_assert(sizeof(gas_counters) == 4 * sizeof(int4), "gas_counters layout");
+    const int4 *p = reinterpret_cast<const int4 *>(cnt);
+    int4 r[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r[i] = p[i];
+    memcpy(&k, r, sizeof(k));
+  }
   const int per = (nb + kSpineNT - 1) / kSpineNT;
   const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
   const bool in_regs = per <= kSpineRegs;
@@ -788,35 +808,42 @@ __global__ void __launch_bounds__(kSpineNT)
       pre = add4(pre, y);
     }
   }
+  LoopVals v{};
   if (threadIdx.x == 0) {
-    cnt->n_changed = tot.x + tot.z;        // queue length (members with out-edges)
-    cnt->n_scatter_edges = tot.y + tot.w;  // their out-edges
+    v.sched = k.sched;
+    v.pull_div = k.pull_div;
+    v.n_changed = tot.x + tot.z;        // queue length (members with out-edges)
+    v.n_scatter_edges = tot.y + tot.w;  // their out-edges
+    cnt->n_changed = v.n_changed;
+    cnt->n_scatter_edges = v.n_scatter_edges;
     cnt->q_heavy = tot.x;
     cnt->q_heavy_edges = tot.y;
     int cl = gasdev::kSlabChunkLog2;
     while (cl > gasdev::kSlabChunkMinLog2 && (tot.y >> cl) < 2 * push_warps) --cl;
     cnt->push_chunk_log2 = cl;
-    const bool edges = tot.y + tot.w > 0;
+    const bool edges = v.n_scatter_edges > 0;
     if (phase == 0) {
       const int done = seeded ? 0 : 1;  // iterations run by the prologue
-      cnt->iteration = done;
       const bool more = seeded ? true : edges;
-      if (more && done >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
-      cnt->cond = (more && done < cnt->max_iter) ? 1 : 0;
+      if (more && done >= k.max_iter) cnt->error = GAS_ERR_ITER_CAP;
+      v.it = done;
+      v.cond = (more && done < k.max_iter) ? 1 : 0;
     } else {
       *c.fix_n = 0;  // the pull fixup of this iteration has run
-      if (cnt->mode == kModePush)
-        ++cnt->n_push;
+      if (k.mode == kModePush)
+        cnt->n_push = k.n_push + 1;
       else
-        ++cnt->n_pull;
-      if (c.trace && cnt->iteration < GAS_TRACE_CAP) c.trace[cnt->iteration].t_end_ns = now;
-      const int it = ++cnt->iteration;
-      if (edges && it >= cnt->max_iter) cnt->error = GAS_ERR_ITER_CAP;
-      cnt->cond = (edges && it < cnt->max_iter) ? 1 : 0;
+        cnt->n_pull = k.n_pull + 1;
+      if (c.trace && k.iteration < GAS_TRACE_CAP) c.trace[k.iteration].t_end_ns = now;
+      v.it = k.iteration + 1;
+      if (edges && v.it >= k.max_iter) cnt->error = GAS_ERR_ITER_CAP;
+      v.cond = (edges && v.it < k.max_iter) ? 1 : 0;
     }
+    cnt->iteration = v.it;
+    cnt->cond = v.cond;
   }
-  __syncthreads();  // the counters above, and the staged weights
-  schedule_next(cnt, c, now, sm, learned);
+  __syncthreads();  // the staged weights
+  schedule_next(cnt, c, now, sm, learned, v);
 }
 
 
