@@ -140,102 +140,126 @@ __global__ void k_ms_seed(const int32_t *src_global, const BatchParams *prm, int
 }
 
 // The touched-vertex traversal shared by the two compaction passes: a warp
-// owns 8 words of the touched bitmap (lanes 0..7 load them), lane l takes
-// vertex 32 w + l of each word, and all 8 words' loads are issued before
-// any is used.  For a touched vertex: its new lanes and out-edge range.
-constexpr int kMsWarpWords = 8;
-constexpr int kMsBlockWords = kMsWarpWords * (kNT / 32);  // 64 words
+// owns a run of 16 words of the touched bitmap (lanes 0..15 load them) and
+// walks it in two rounds of 8 words, skipping a round whose words are all
+// clear; lane l takes vertex 32 w + l of each word, and a round's 8 words'
+// loads are issued before any is used.  For a touched vertex: its new lanes
+// and out-edge range.  The count pass keeps each warp's totals, so the
+// write passes take their offsets without counting again.
+constexpr int kMsWarpWords = 16;
+constexpr int kMsRound = 8;
+constexpr int kMsWarps = kNT / 32;
+constexpr int kMsBlockWords = kMsWarpWords * kMsWarps;  // 128 words
 
-struct MsWarp {
-  uint32_t myword;
-  uint32_t nw[kMsWarpWords];  // new lanes (0: not touched or nothing new)
-  int off[kMsWarpWords];
-  int deg[kMsWarpWords];
+struct MsRound {
+  uint32_t nw[kMsRound];  // new lanes (0: not touched or nothing new)
+  int off[kMsRound];
+  int deg[kMsRound];
 };
 
-// next: the SSSP's changed-lane words; vn (BFS, next unused): the
-// {visited, next} pairs, new lanes = next & ~visited
-__device__ __forceinline__ void ms_load(const uint32_t *tbits, const uint32_t *next,
-                                        const uint32_t *vn, const int32_t *csr_off,
-                                        int nW, int w0, MsWarp &w) {
+// The lane's word of the warp's run (lanes 0..15; 0 past the bitmap).
+__device__ __forceinline__ uint32_t ms_word(const uint32_t *tbits, int nW, int w0) {
   const int lane = threadIdx.x & 31;
-  w.myword = (lane < kMsWarpWords && w0 + lane < nW) ? tbits[w0 + lane] : 0u;
+  return lane < kMsWarpWords && w0 + lane < nW ? tbits[w0 + lane] : 0u;
+}
+
+__device__ __forceinline__ bool ms_round_live(unsigned nz, int r) {
+  return ((nz >> r) & ((1u << kMsRound) - 1u)) != 0u;
+}
+
+// Round r (words w0 + r .. w0 + r + 7).  next: the SSSP's changed-lane
+// words; vn (BFS, next unused): the {visited, next} pairs, new lanes =
+// next & ~visited.
+__device__ __forceinline__ void ms_round_load(uint32_t myword, const uint32_t *next,
+                                              const uint32_t *vn, const int32_t *csr_off,
+                                              int w0, int r, MsRound &m) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int i = 0; i < kMsWarpWords; ++i) {
-    const uint32_t word = __shfl_sync(0xffffffffu, w.myword, i);
-    w.nw[i] = 0u;
-    w.off[i] = 0;
-    w.deg[i] = 0;
+  for (int i = 0; i < kMsRound; ++i) {
+    const uint32_t word = __shfl_sync(0xffffffffu, myword, r + i);
+    m.nw[i] = 0u;
+    m.off[i] = 0;
+    m.deg[i] = 0;
     if ((word >> lane) & 1u) {
-      const int v = (w0 + i) * 32 + lane;
+      const int v = (w0 + r + i) * 32 + lane;
       if (vn) {
         const uint2 p = reinterpret_cast<const uint2 *>(vn)[v];
-        w.nw[i] = p.y & ~p.x;
+        m.nw[i] = p.y & ~p.x;
       } else {
-        w.nw[i] = next[v];
+        m.nw[i] = next[v];
       }
-      w.off[i] = csr_off[v];
-      w.deg[i] = csr_off[v + 1] - w.off[i];
+      m.off[i] = csr_off[v];
+      m.deg[i] = csr_off[v + 1] - m.off[i];
     }
   }
 }
 
-// queue entries (vertices with new lanes and out-edges) and their out-edges
-__device__ __forceinline__ void ms_totals(const MsWarp &w, int &q, int &d) {
-  q = 0;
-  d = 0;
+// Pass 1: per block (queue entries, out-edges) for the spine and per warp
+// for the write pass; with lanes_active, also the OR of the new lanes of the
+// queue's entries (the SSSP loop).
+__global__ void __launch_bounds__(kNT)
+    k_ms_count(const uint32_t *tbits, const uint32_t *next, const uint32_t *vn,
+               const int32_t *csr_off, int nW, int32_t *part, int2 *wpart,
+               uint32_t *lanes_active) {
+  __shared__ int s_q[kMsWarps], s_d[kMsWarps];
+  __shared__ uint32_t s_l[kMsWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = (blockIdx.x * kMsWarps + warp) * kMsWarpWords;
+  const uint32_t myword = ms_word(tbits, nW, w0);
+  const unsigned nz = __ballot_sync(0xffffffffu, myword != 0u);
+  int q = 0, d = 0;
+  uint32_t lanes = 0u;
+#pragma unroll 1
+  for (int r = 0; r < kMsWarpWords; r += kMsRound) {
+    if (!ms_round_live(nz, r)) continue;  // warp-uniform
+    MsRound m;
+    ms_round_load(myword, next, vn, csr_off, w0, r, m);
 #pragma unroll
-  for (int i = 0; i < kMsWarpWords; ++i) {
-    const bool in = w.nw[i] && w.deg[i] > 0;
-    q += in;
-    d += in ? w.deg[i] : 0;
+    for (int i = 0; i < kMsRound; ++i) {
+      const bool in = m.nw[i] && m.deg[i] > 0;
+      q += in;
+      d += in ? m.deg[i] : 0;
+      if (m.deg[i] > 0) lanes |= m.nw[i];
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     q += __shfl_xor_sync(0xffffffffu, q, o);
     d += __shfl_xor_sync(0xffffffffu, d, o);
-  }
-}
-
-// Pass 1: per block (queue entries, out-edges); with lanes_active, also
-// the OR of the new lanes of the queue's entries (the SSSP loop).
-__global__ void __launch_bounds__(kNT)
-    k_ms_count(const uint32_t *tbits, const uint32_t *next, const uint32_t *vn,
-               const int32_t *csr_off, int nW, int32_t *part, uint32_t *lanes_active) {
-  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
-  __shared__ uint32_t s_l[kNT / 32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
-  MsWarp w;
-  ms_load(tbits, next, vn, csr_off, nW, w0, w);
-  int q, d;
-  ms_totals(w, q, d);
-  uint32_t lanes = 0u;
-  if (lanes_active) {
-#pragma unroll
-    for (int i = 0; i < kMsWarpWords; ++i)
-      if (w.deg[i] > 0) lanes |= w.nw[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lanes |= __shfl_xor_sync(0xffffffffu, lanes, o);
+    lanes |= __shfl_xor_sync(0xffffffffu, lanes, o);
   }
   if (lane == 0) {
     s_q[warp] = q;
     s_d[warp] = d;
     s_l[warp] = lanes;
+    wpart[blockIdx.x * kMsWarps + warp] = make_int2(q, d);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     int tq = 0, td = 0;
     uint32_t tl = 0u;
-    for (int k = 0; k < kNT / 32; ++k) {
+    for (int k = 0; k < kMsWarps; ++k) {
       tq += s_q[k];
       td += s_d[k];
       tl |= s_l[k];
     }
     part[2 * blockIdx.x] = tq;
     part[2 * blockIdx.x + 1] = td;
-    if (tl) atomicOr(lanes_active, tl);
+    if (lanes_active && tl) atomicOr(lanes_active, tl);
   }
+}
+
+// The warp's first queue entry and out-edge offset: its block's (scanned by
+// the spine) plus the totals of the block's earlier warps.
+__device__ __forceinline__ int2 ms_warp_base(const int32_t *part, const int2 *wpart,
+                                             int warp) {
+  int2 b = make_int2(part[2 * blockIdx.x], part[2 * blockIdx.x + 1]);
+  for (int k = 0; k < warp; ++k) {
+    const int2 t = wpart[blockIdx.x * kMsWarps + k];
+    b.x += t.x;
+    b.y += t.y;
+  }
+  return b;
 }
 
 // Pass 2: depths of the new lanes (level = the iteration the spine just
@@ -243,78 +267,75 @@ __global__ void __launch_bounds__(kNT)
 // chunk size the spine chose; clears next and the touched bitmap.
 __global__ void __launch_bounds__(kNT, 5)
     k_ms_write(uint32_t *tbits, uint32_t *vn, const int32_t *csr_off,
-               int nW, const int32_t *part, int L, const gas_counters *cnt,
+               int nW, const int32_t *part, const int2 *wpart, int L, const gas_counters *cnt,
                int32_t *depth, int32_t *q_mask, int32_t *q_end, int32_t *q_delta,
                int32_t *chunk_row) {
-  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   // rows spanning many chunks (hubs), written by the whole warp at the end
   constexpr int kBig = 64;
-  __shared__ int3 s_big[kNT / 32][kBig];
-  __shared__ int s_nbig[kNT / 32];
+  __shared__ int3 s_big[kMsWarps][kBig];
+  __shared__ int s_nbig[kMsWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = (blockIdx.x * kMsWarps + warp) * kMsWarpWords;
+  const uint32_t myword = ms_word(tbits, nW, w0);
+  const unsigned nz = __ballot_sync(0xffffffffu, myword != 0u);
+  if (!nz) return;  // warp-uniform: nothing touched in the run
   const int level = cnt->iteration;
   const int cl = cnt->push_chunk_log2;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) s_nbig[warp] = 0;
-  const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
-  MsWarp w;
-  ms_load(tbits, nullptr, vn, csr_off, nW, w0, w);
-  int q, d;
-  ms_totals(w, q, d);
-  if (lane == 0) {
-    s_q[warp] = q;
-    s_d[warp] = d;
-  }
-  __syncthreads();
-  int bq = part[2 * blockIdx.x], bd = part[2 * blockIdx.x + 1];
-  for (int k = 0; k < warp; ++k) {
-    bq += s_q[k];
-    bd += s_d[k];
-  }
-  if (w.myword) tbits[w0 + lane] = 0u;
+  __syncwarp();
+  const int2 base = ms_warp_base(part, wpart, warp);
+  int bq = base.x, bd = base.y;
+  if (myword) tbits[w0 + lane] = 0u;
+#pragma unroll 1
+  for (int r = 0; r < kMsWarpWords; r += kMsRound) {
+    if (!ms_round_live(nz, r)) continue;  // warp-uniform
+    MsRound m;
+    ms_round_load(myword, nullptr, vn, csr_off, w0, r, m);
 #pragma unroll
-  for (int i = 0; i < kMsWarpWords; ++i) {
-    const int v = (w0 + i) * 32 + lane;
-    const uint32_t word = __shfl_sync(0xffffffffu, w.myword, i);
-    if (!word) continue;  // warp-uniform
-    const bool touched = (word >> lane) & 1u;
-    const uint32_t nw = w.nw[i];
-    if (touched) vn[2 * (size_t)v + 1] = 0u;
-    if (nw) {
-      vn[2 * (size_t)v] |= nw;
-      for (uint32_t m = nw; m; m &= m - 1) depth[(size_t)v * L + (__ffs(m) - 1)] = level;
-    }
-    const int deg = nw ? w.deg[i] : 0;
-    const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
-    if (!qb) continue;
-    int incl = deg;
+    for (int i = 0; i < kMsRound; ++i) {
+      const int v = (w0 + r + i) * 32 + lane;
+      const uint32_t word = __shfl_sync(0xffffffffu, myword, r + i);
+      if (!word) continue;  // warp-uniform
+      const bool touched = (word >> lane) & 1u;
+      const uint32_t nw = m.nw[i];
+      if (touched) vn[2 * (size_t)v + 1] = 0u;
+      if (nw) {
+        vn[2 * (size_t)v] |= nw;
+        for (uint32_t k = nw; k; k &= k - 1) depth[(size_t)v * L + (__ffs(k) - 1)] = level;
+      }
+      const int deg = nw ? m.deg[i] : 0;
+      const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
+      if (!qb) continue;
+      int incl = deg;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (deg > 0) {
+        const int pos = bq + __popc(qb & ((1u << lane) - 1u));
+        const int end = bd + incl;
+        q_mask[pos] = (int32_t)nw;
+        q_end[pos] = end;
+        q_delta[pos] = m.off[i] - (end - deg);
+        // chunk partition of the next push (chunks starting in this range)
+        const int c0 = (end - deg + (1 << cl) - 1) >> cl, c1 = (end + (1 << cl) - 1) >> cl;
+        int slot = kBig;
+        if (c1 - c0 > 4) slot = atomicAdd(&s_nbig[warp], 1);
+        if (slot < kBig)
+          s_big[warp][slot] = make_int3(pos, c0, c1);
+        else
+          for (int c = c0; c < c1; ++c) chunk_row[c] = pos;
+      }
+      bq += __popc(qb);
+      bd += __shfl_sync(0xffffffffu, incl, 31);
     }
-    if (deg > 0) {
-      const int pos = bq + __popc(qb & ((1u << lane) - 1u));
-      const int end = bd + incl;
-      q_mask[pos] = (int32_t)nw;
-      q_end[pos] = end;
-      q_delta[pos] = w.off[i] - (end - deg);
-      // chunk partition of the next push (chunks starting in this range)
-      const int c0 = (end - deg + (1 << cl) - 1) >> cl, c1 = (end + (1 << cl) - 1) >> cl;
-      int slot = kBig;
-      if (c1 - c0 > 4) slot = atomicAdd(&s_nbig[warp], 1);
-      if (slot < kBig)
-        s_big[warp][slot] = make_int3(pos, c0, c1);
-      else
-        for (int c = c0; c < c1; ++c) chunk_row[c] = pos;
-    }
-    bq += __popc(qb);
-    bd += __shfl_sync(0xffffffffu, incl, 31);
   }
   __syncwarp();
   const int nbig = min(s_nbig[warp], kBig);
   for (int k = 0; k < nbig; ++k) {
-    const int3 r = s_big[warp][k];
-    for (int c = r.y + lane; c < r.z; c += 32) chunk_row[c] = r.x;
+    const int3 rr = s_big[warp][k];
+    for (int c = rr.y + lane; c < rr.z; c += 32) chunk_row[c] = rr.x;
   }
 }
 
@@ -509,74 +530,71 @@ __global__ void k_mss_seed(const int32_t *src_global, const BatchParams *prm, in
 // cmask and the touched bitmap.
 __global__ void __launch_bounds__(kNT, 4)
     k_mss_write(uint32_t *tbits, uint32_t *cmask, const int32_t *csr_off, int nW,
-                const int32_t *part, int LS, const int32_t *dist,
+                const int32_t *part, const int2 *wpart, int LS, const int32_t *dist,
                 int32_t *q_mask, int32_t *q_vals, int32_t *q_end, int32_t *q_delta,
                 int32_t *chunk_row, const gas_counters *cnt) {
-  __shared__ int s_q[kNT / 32], s_d[kNT / 32];
   // rows spanning many chunks (hubs), written by the whole warp at the end
   constexpr int kBig = 64;
-  __shared__ int3 s_big[kNT / 32][kBig];
-  __shared__ int s_nbig[kNT / 32];
-  const int cl = cnt->push_chunk_log2;
+  __shared__ int3 s_big[kMsWarps][kBig];
+  __shared__ int s_nbig[kMsWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = (blockIdx.x * kMsWarps + warp) * kMsWarpWords;
+  const uint32_t myword = ms_word(tbits, nW, w0);
+  const unsigned nz = __ballot_sync(0xffffffffu, myword != 0u);
+  if (!nz) return;  // warp-uniform: nothing touched in the run
+  const int cl = cnt->push_chunk_log2;
   if (lane == 0) s_nbig[warp] = 0;
-  const int w0 = blockIdx.x * kMsBlockWords + warp * kMsWarpWords;
-  MsWarp w;
-  ms_load(tbits, cmask, nullptr, csr_off, nW, w0, w);
-  int q, d;
-  ms_totals(w, q, d);
-  if (lane == 0) {
-    s_q[warp] = q;
-    s_d[warp] = d;
-  }
-  __syncthreads();
-  int bq = part[2 * blockIdx.x], bd = part[2 * blockIdx.x + 1];
-  for (int k = 0; k < warp; ++k) {
-    bq += s_q[k];
-    bd += s_d[k];
-  }
-  if (w.myword) tbits[w0 + lane] = 0u;
+  __syncwarp();
+  const int2 base = ms_warp_base(part, wpart, warp);
+  int bq = base.x, bd = base.y;
+  if (myword) tbits[w0 + lane] = 0u;
+#pragma unroll 1
+  for (int r = 0; r < kMsWarpWords; r += kMsRound) {
+    if (!ms_round_live(nz, r)) continue;  // warp-uniform
+    MsRound m;
+    ms_round_load(myword, cmask, nullptr, csr_off, w0, r, m);
 #pragma unroll
-  for (int i = 0; i < kMsWarpWords; ++i) {
-    const int v = (w0 + i) * 32 + lane;
-    const uint32_t word = __shfl_sync(0xffffffffu, w.myword, i);
-    if (!word) continue;  // warp-uniform
-    if ((word >> lane) & 1u) cmask[v] = 0u;
-    const uint32_t nw = w.nw[i];
-    const int deg = nw ? w.deg[i] : 0;
-    const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
-    if (!qb) continue;
-    int incl = deg;
+    for (int i = 0; i < kMsRound; ++i) {
+      const int v = (w0 + r + i) * 32 + lane;
+      const uint32_t word = __shfl_sync(0xffffffffu, myword, r + i);
+      if (!word) continue;  // warp-uniform
+      if ((word >> lane) & 1u) cmask[v] = 0u;
+      const uint32_t nw = m.nw[i];
+      const int deg = nw ? m.deg[i] : 0;
+      const unsigned qb = __ballot_sync(0xffffffffu, deg > 0);
+      if (!qb) continue;
+      int incl = deg;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (deg > 0) {
+        const int pos = bq + __popc(qb & ((1u << lane) - 1u));
+        const int end = bd + incl;
+        if (LS > 8) q_mask[pos] = (int32_t)nw;  // rows of up to 8 lanes try every lane
+        q_end[pos] = end;
+        q_delta[pos] = m.off[i] - (end - deg);
+        const int4 *src4 = reinterpret_cast<const int4 *>(dist + (size_t)v * LS);
+        int4 *dst4 = reinterpret_cast<int4 *>(q_vals + (size_t)pos * LS);
+        for (int c = 0; c < (LS >> 2); ++c) dst4[c] = src4[c];
+        const int c0 = (end - deg + (1 << cl) - 1) >> cl, c1 = (end + (1 << cl) - 1) >> cl;
+        int slot = kBig;
+        if (c1 - c0 > 4) slot = atomicAdd(&s_nbig[warp], 1);
+        if (slot < kBig)
+          s_big[warp][slot] = make_int3(pos, c0, c1);
+        else
+          for (int c = c0; c < c1; ++c) chunk_row[c] = pos;
+      }
+      bq += __popc(qb);
+      bd += __shfl_sync(0xffffffffu, incl, 31);
     }
-    if (deg > 0) {
-      const int pos = bq + __popc(qb & ((1u << lane) - 1u));
-      const int end = bd + incl;
-      if (LS > 8) q_mask[pos] = (int32_t)nw;  // rows of up to 8 lanes try every lane
-      q_end[pos] = end;
-      q_delta[pos] = w.off[i] - (end - deg);
-      const int4 *src4 = reinterpret_cast<const int4 *>(dist + (size_t)v * LS);
-      int4 *dst4 = reinterpret_cast<int4 *>(q_vals + (size_t)pos * LS);
-      for (int c = 0; c < (LS >> 2); ++c) dst4[c] = src4[c];
-      const int c0 = (end - deg + (1 << cl) - 1) >> cl, c1 = (end + (1 << cl) - 1) >> cl;
-      int slot = kBig;
-      if (c1 - c0 > 4) slot = atomicAdd(&s_nbig[warp], 1);
-      if (slot < kBig)
-        s_big[warp][slot] = make_int3(pos, c0, c1);
-      else
-        for (int c = c0; c < c1; ++c) chunk_row[c] = pos;
-    }
-    bq += __popc(qb);
-    bd += __shfl_sync(0xffffffffu, incl, 31);
   }
   __syncwarp();
   const int nbig = min(s_nbig[warp], kBig);
   for (int k = 0; k < nbig; ++k) {
-    const int3 r = s_big[warp][k];
-    for (int c = r.y + lane; c < r.z; c += 32) chunk_row[c] = r.x;
+    const int3 rr = s_big[warp][k];
+    for (int c = rr.y + lane; c < rr.z; c += 32) chunk_row[c] = rr.x;
   }
 }
 
@@ -971,6 +989,11 @@ int nwords(const gas_batch *b) { return (b->eng->nV + 31) / 32; }
 int ms_blocks(const gas_batch *b) {
   return std::max(1, (nwords(b) + kMsBlockWords - 1) / kMsBlockWords);
 }
+// qpart: the blocks' (entries, out-edges) pairs, one spare pair, then the
+// blocks' per-warp pairs
+int2 *ms_wpart(const gas_batch *b) {
+  return reinterpret_cast<int2 *>(b->qpart + 2 * ((size_t)ms_blocks(b) + 1));
+}
 
 // The frontier arrays the BFS and SSSP loops share (they run one after the
 // other, each prologue resetting them).
@@ -984,7 +1007,8 @@ gas_status_t ensure_frontier(gas_batch *b) {
       CUDA_TRY(cudaMalloc(p, nV * 4));
     // the SSSP push cuts its queue's edges into chunks of 64 to 512 edges
     CUDA_TRY(cudaMalloc(&b->part, (((size_t)e->nE >> gasdev::kSlabChunkMinLog2) + 2) * 4));
-    CUDA_TRY(cudaMalloc(&b->qpart, 2 * ((size_t)ms_blocks(b) + 1) * 4));
+    CUDA_TRY(cudaMalloc(&b->qpart,
+                        2 * ((size_t)ms_blocks(b) + 1 + (size_t)ms_blocks(b) * kMsWarps) * 4));
   }
   return GAS_OK;
 }
@@ -1145,12 +1169,12 @@ gas_status_t bfs_compact(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle h
   gas_engine *e = b->eng;
   const int nb = ms_blocks(b);
   k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, nullptr, b->vn, e->csr_off, nwords(b), b->qpart,
-                                nullptr);
+                                ms_wpart(b), nullptr);
   k_mss_spine<<<1, kMssSpineNT, 0, s>>>(reinterpret_cast<int2 *>(b->qpart), nb, b->cnt,
                                         c->slab_grid * (kNT / 32), b->edges, nullptr, nullptr,
                                         h, ig, first);
   k_ms_write<<<nb, kNT, 0, s>>>(b->tbits, b->vn, e->csr_off, nwords(b), b->qpart,
-                               c->bfs_lanes, b->cnt, b->depth, b->q_mask, b->q_end, b->q_delta,
+                               ms_wpart(b), c->bfs_lanes, b->cnt, b->depth, b->q_mask, b->q_end, b->q_delta,
                                b->part);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
@@ -1210,12 +1234,12 @@ gas_status_t sssp_compact(RunCtx *c, cudaStream_t s, cudaGraphConditionalHandle 
   gas_engine *e = b->eng;
   const int nb = ms_blocks(b);
   k_ms_count<<<nb, kNT, 0, s>>>(b->tbits, b->next, nullptr, e->csr_off, nwords(b), b->qpart,
-                                b->lanes_active);
+                                ms_wpart(b), b->lanes_active);
   k_mss_spine<<<1, kMssSpineNT, 0, s>>>(reinterpret_cast<int2 *>(b->qpart), nb, b->cnt + 2,
                                         c->sssp_grid * (kNT / 32), b->sssp_edges,
                                         b->lanes_active, b->lane_rounds, h, ig, first);
   k_mss_write<<<nb, kNT, 0, s>>>(b->tbits, b->next, e->csr_off, nwords(b), b->qpart,
-                                 b->dist_ls, b->dist, b->q_mask, b->q_vals, b->q_end,
+                                 ms_wpart(b), b->dist_ls, b->dist, b->q_mask, b->q_vals, b->q_end,
                                  b->q_delta, b->part, b->cnt + 2);
   CUDA_TRY(cudaGetLastError());
   return GAS_OK;
