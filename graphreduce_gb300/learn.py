@@ -11,8 +11,8 @@ kernels, on data the engine records about itself:
   so iteration k of the two runs differs only in the kernel that ran; the
   device trace gives each iteration's duration, the label is the faster
   mode and the sample weight the time difference.  The fixed heuristic
-  (AUTO) stays the fallback and the judge: the learned schedule gives the
-  same vertex data and iteration count by construction.
+  (AUTO) stays the fallback and the yardstick: the learned schedule gives
+  the same vertex data and iteration count by construction.
 * warm-start head -- per-vertex log in/out-degree (+ graph size) ->
   log(N * rank) of the converged precision-form PageRank; a run then starts
   from the prediction and iterates to the same tolerance.
