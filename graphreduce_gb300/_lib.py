@@ -71,7 +71,8 @@ class Counters(C.Structure):
                 ("n_changed", c_i32), ("max_iter", c_i32), ("mode", c_i32),
                 ("n_push", c_i32), ("n_pull", c_i32), ("pull_div", c_i32),
                 ("sched", c_i32), ("push_chunk_log2", c_i32), ("q_heavy", c_i32),
-                ("q_heavy_edges", c_i32)]
+                ("q_heavy_edges", c_i32), ("seen_edges", c_i32), ("prev_changed", c_i32),
+                ("pad", c_i32 * 2)]
 
 
 GAS_BATCH_MAX_LANES = 32

@@ -235,7 +235,15 @@ __global__ void __launch_bounds__(kNT)
 }
 
 constexpr int kSpineNT = 1024;  // k_q_spine (with the loop control, below)
-constexpr int kBfsPullDiv = 16;  // BFS: bottom-up while out-edges(C_k) * 16 > E
+constexpr int kBfsPullDiv = 16;  // BFS pull_div of the counters (unused by its AUTO rule)
+// BFS AUTO: the direction rule of Beamer, Asanovic & Patterson ("Direction-
+// Optimizing Breadth-First Search", SC'12) with the paper's constants.  A
+// top-down level is followed by a bottom-up one when the queue's out-edges
+// exceed 1/alpha of the edges not yet explored (E minus the out-edges of
+// every earlier level's queue); bottom-up levels continue while the queue
+// grows or holds more than V/beta vertices.
+constexpr int kBfsAlpha = 14;
+constexpr int kBfsBeta = 24;
 constexpr int kSpineRegs = 4;
 
 // Queue positions of a warp's next rows: heavy row, heavy-edge offset,
@@ -594,6 +602,7 @@ struct LoopCtl {
   int nV;
   int nE;
   int weighted;
+  int bfs;
   const __nv_bfloat16 *model;  // schedule head (LEARNED), or null
   gas_trace_record *trace;     // per-iteration records, or null
   int32_t *hist;               // degree histogram of the queue, or null
@@ -678,6 +687,8 @@ struct LoopVals {
   int sched;  // 0 auto, 1 push, 2 pull, 3 learned
   int it;     // the iteration being scheduled
   int n_changed, n_scatter_edges, pull_div, cond;
+  int mode;                     // the mode of the iteration that built the queue
+  int seen_edges, prev_changed;  // BFS: see gas_counters
 };
 
 __device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now,
@@ -699,6 +710,12 @@ __device__ void schedule_next(gas_counters *cnt, const LoopCtl &c, long long now
       mode = kModePull;
     else if (learned)
       mode = lg[1] > lg[0] ? kModePull : kModePush;
+    else if (c.bfs && v.mode == kModePush)
+      mode = (long long)v.n_scatter_edges * kBfsAlpha > (long long)c.nE - v.seen_edges
+                 ? kModePull : kModePush;
+    else if (c.bfs)
+      mode = (v.n_changed >= v.prev_changed || (long long)v.n_changed * kBfsBeta > c.nV)
+                 ? kModePull : kModePush;
     else
       mode = ((long long)v.n_scatter_edges * v.pull_div > (long long)c.nE) ? kModePull
                                                                            : kModePush;
@@ -744,16 +761,17 @@ __global__ void __launch_bounds__(kSpineNT)
   __shared__ __align__(16) SchedSmem sm;
   const bool learned = cnt->sched == 3 && c.model != nullptr;
   if (learned) sched_stage_weights(sm, c.model);
-  // thread 0: every counter the loop control reads, in four 16-byte loads
-  // issued with the block totals' (gas_counters is 64 bytes at the start of
+  // thread 0: every counter the loop control reads, in five 16-byte loads
+  // issued with the block totals' (gas_counters is 80 bytes at the start of
   // a cudaMalloc block), instead of one dependent load after each store
   gas_counters k;
   if (threadIdx.x == 0) {
-    static_assert(sizeof(gas_counters) == 4 * sizeof(int4), "gas_counters layout");
+    constexpr int kWords = (int)(sizeof(gas_counters) / sizeof(int4));
+    static_assert(sizeof(gas_counters) == kWords * sizeof(int4), "gas_counters layout");
     const int4 *p = reinterpret_cast<const int4 *>(cnt);
-    int4 r[4];
+    int4 r[kWords];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) r[i] = p[i];
+    for (int i = 0; i < kWords; ++i) r[i] = p[i];
     memcpy(&k, r, sizeof(k));
   }
   const int per = (nb + kSpineNT - 1) / kSpineNT;
@@ -812,8 +830,14 @@ __global__ void __launch_bounds__(kSpineNT)
   if (threadIdx.x == 0) {
     v.sched = k.sched;
     v.pull_div = k.pull_div;
+    v.mode = phase == 0 ? kModePush : k.mode;
     v.n_changed = tot.x + tot.z;        // queue length (members with out-edges)
     v.n_scatter_edges = tot.y + tot.w;  // their out-edges
+    // the queue just expanded joins the explored levels
+    v.seen_edges = phase == 0 ? 0 : k.seen_edges + k.n_scatter_edges;
+    v.prev_changed = phase == 0 ? 0 : k.n_changed;
+    cnt->seen_edges = v.seen_edges;
+    cnt->prev_changed = v.prev_changed;
     cnt->n_changed = v.n_changed;
     cnt->n_scatter_edges = v.n_scatter_edges;
     cnt->q_heavy = tot.x;
@@ -880,6 +904,7 @@ LoopCtl loop_ctl(const gas_engine *e, cudaGraphConditionalHandle h) {
   c.nV = e->nV;
   c.nE = e->nE;
   c.weighted = e->prog == GAS_PROG_SSSP ? 1 : 0;
+  c.bfs = e->prog == GAS_PROG_BFS ? 1 : 0;
   c.model = static_cast<const __nv_bfloat16 *>(e->sched_model);
   c.trace = e->trace_on ? e->trace : nullptr;
   c.hist = (e->trace_on || e->sched_model) ? e->hist : nullptr;

@@ -232,8 +232,12 @@ gas_status_t gas_engine_download_vertex_data_async(gas_engine *e, void *dst,
 
 /* Schedule of the built-in fast runs.  For BFS the pull is the bottom-up
  * level (each unvisited vertex stops at its first in-neighbour of the
- * previous level), and AUTO and LEARNED both take the direction rule
- * "bottom-up while the frontier's out-edges exceed E/16". */
+ * previous level), and AUTO and LEARNED both take a direction rule: graphs
+ * of more than 2^18 vertices Beamer, Asanovic and Patterson's (SC'12;
+ * bottom-up once the frontier's out-edges exceed 1/14 of the edges not yet
+ * explored, top-down again once it shrinks below V/24 vertices), smaller
+ * ones (one cooperative kernel) "bottom-up while the frontier's out-edges
+ * exceed E/16". */
 typedef enum {
   GAS_SCHED_AUTO = 0,      /* fixed heuristic per iteration                */
   GAS_SCHED_GENERIC = 1,   /* the step-API kernels (pull over active set)  */
@@ -534,6 +538,10 @@ typedef struct {
   int32_t q_heavy;         /* fast runs: queue rows [0, q_heavy) have more */
                            /* out-edges than a thread takes alone          */
   int32_t q_heavy_edges;   /* fast runs: out-edges of those rows           */
+  int32_t seen_edges;      /* BFS fast runs: out-edges of the levels before */
+                           /* the current queue                           */
+  int32_t prev_changed;    /* BFS fast runs: the previous queue's length    */
+  int32_t pad[2];
 } gas_counters;
 
 typedef struct {
